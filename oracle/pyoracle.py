@@ -1,0 +1,156 @@
+"""TEST INFRASTRUCTURE — ctypes front end of the CPU oracle (oracle/mpm_oracle.cpp).
+
+Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module, and only
+as the checker or the timed CPU baseline. It builds ``oracle/_build/liboracle.so`` with ``make`` on
+first use.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build(force=False):
+    src = os.path.join(HERE, "mpm_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, d, i32, i64, u64 = C.c_void_p, C.c_double, C.c_int, C.c_int64, C.c_uint64
+        P = C.POINTER
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [i32, d, d, P(d), d, d]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_add_material.restype = i32
+        L.orc_add_material.argtypes = [vp, i32, d, d, i32, d, d, d, d, d]
+        L.orc_add_halfspace.argtypes = [vp, P(d), P(d), i32, d, P(d)]
+        L.orc_set_particles.argtypes = [vp, i64] + [P(d)] * 8 + [P(C.c_int32)]
+        L.orc_step.restype = i32
+        L.orc_step.argtypes = [vp, i32]
+        L.orc_get_state.argtypes = [vp] + [P(d)] * 5
+        L.orc_time.restype = d
+        L.orc_time.argtypes = [vp]
+        L.orc_bin.restype = i64
+        L.orc_bin.argtypes = [vp, P(u64), P(C.c_int32), P(C.c_int32), P(C.c_int32), P(u64), P(u64), P(i64)]
+        L.orc_linear_offset.restype = u64
+        L.orc_linear_offset.argtypes = [i32, i32, i32, i32]
+        L.orc_packed_add.restype = u64
+        L.orc_packed_add.argtypes = [i32, u64, u64]
+        L.orc_masks.argtypes = [i32, P(u64)]
+        L.orc_svd3.argtypes = [i32, P(d), P(d), P(d), P(d)]
+        L.orc_reductions.argtypes = [vp, P(d)]
+        L.orc_num_threads.restype = i32
+        _lib = L
+    return _lib
+
+
+def _p(a, ct=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class OracleScene:
+    """One scene of the oracle. precision 4 = float, 8 = double. Arrays are float64 at the interface."""
+
+    def __init__(self, precision, dx, dt, gravity=(0.0, 0.0, 0.0), apic_ratio=1.0, cfl=0.6):
+        self.L = lib()
+        g = np.asarray(gravity, dtype=np.float64)
+        self.h = self.L.orc_create(precision, dx, dt, _p(g), apic_ratio, cfl)
+        self.precision = precision
+        self.n = 0
+
+    def close(self):
+        if self.h:
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_material(self, model, E, nu, damage=False, alpha=0.0, l0=0.0, eta=1.0, zeta=1.0, residual=0.0):
+        return self.L.orc_add_material(self.h, model, E, nu, int(damage), alpha, l0, eta, zeta, residual)
+
+    def add_halfspace(self, origin, normal, type_, friction=0.0, velocity=(0.0, 0.0, 0.0)):
+        o, n, v = (np.asarray(a, dtype=np.float64) for a in (origin, normal, velocity))
+        self.L.orc_add_halfspace(self.h, _p(o), _p(n), type_, friction, _p(v))
+
+    def set_particles(self, x, v, m, V0, F=None, C_=None, d=None, sigma_c=None, material=None):
+        x, v, m, V0, F, C_, d, sigma_c = (_f64(a) for a in (x, v, m, V0, F, C_, d, sigma_c))
+        mat = None if material is None else np.ascontiguousarray(material, dtype=np.int32)
+        self.n = x.shape[0]
+        self._keep = (x, v, m, V0, F, C_, d, sigma_c, mat)
+        self.L.orc_set_particles(self.h, self.n, _p(x), _p(v), _p(m), _p(V0), _p(F), _p(C_), _p(d), _p(sigma_c), _p(mat, C.c_int32))
+
+    def step(self, n=1):
+        return self.L.orc_step(self.h, n)
+
+    def state(self):
+        n = self.n
+        x, v, Cm, F, d = (np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 9)), np.zeros((n, 9)), np.zeros(n))
+        self.L.orc_get_state(self.h, _p(x), _p(v), _p(Cm), _p(F), _p(d))
+        return {"x": x, "v": v, "C": Cm, "F": F, "d": d}
+
+    def time(self):
+        return self.L.orc_time(self.h)
+
+    def bin(self):
+        n = self.n
+        sorter = np.zeros(n, np.uint64)
+        order = np.zeros(n, np.int32)
+        gf = np.zeros(n, np.int32)
+        gl = np.zeros(n, np.int32)
+        bo = np.zeros(n, np.uint64)
+        pages = np.zeros(8 * n, np.uint64)
+        npg = C.c_int64(0)
+        ng = self.L.orc_bin(self.h, _p(sorter, C.c_uint64), _p(order, C.c_int32), _p(gf, C.c_int32), _p(gl, C.c_int32),
+                            _p(bo, C.c_uint64), _p(pages, C.c_uint64), C.byref(npg))
+        return {"sorted": sorter, "order": order, "group_first": gf[:ng], "group_last": gl[:ng],
+                "block_offset": bo[:ng], "pages": pages[:npg.value]}
+
+    def reductions(self):
+        out = np.zeros(6)
+        self.L.orc_reductions(self.h, _p(out))
+        return out
+
+
+def linear_offset(precision, i, j, k):
+    return int(lib().orc_linear_offset(precision, i, j, k))
+
+
+def packed_add(precision, a, b):
+    return int(lib().orc_packed_add(precision, a, b))
+
+
+def masks(precision):
+    out = np.zeros(6, np.uint64)
+    lib().orc_masks(precision, _p(out, C.c_uint64))
+    return out
+
+
+def svd3(precision, A):
+    A = np.ascontiguousarray(A, dtype=np.float64).reshape(9)
+    U, s, V = np.zeros(9), np.zeros(3), np.zeros(9)
+    lib().orc_svd3(precision, _p(A), _p(U), _p(s), _p(V))
+    return U.reshape(3, 3), s, V.reshape(3, 3)
+
+
+def num_threads():
+    return int(lib().orc_num_threads())
