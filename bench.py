@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the explicit MPM substep on GB300: particle-substeps/s, FP32 path beside the plain FP64
+GPU path, with the FP32-vs-FP64 error, the roofline of the dominant kernel and the CPU baseline.
+
+Workload (one GPU): the AnisoMPM slab at dx = 1/256 — 0.5 x 0.1 x 0.5 m, 8 particles per cell
+(128 x 26 x 128 cells = 3,407,872 particles), Neo-Hookean (Borden) E=5e4 Pa, nu=0.25, rho=800,
+fibres vMF(kappa=20) about +x, anisotropic damage alpha=-1, l0=0.5 dx, sigma_c ~ N(400, 40) Pa,
+ends pulled apart at +-0.5 m/s, dt = 5e-5, seeded synthetic inputs. One "step" is one substep of the
+whole scene. The particle state (~0.8 GB in FP32, two alternating copies) is larger than L2, so no L2
+flush is needed between substeps.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank advances its own scene (replicas, weak scaling); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (recipe kind, overrides)
+    "aniso_slab_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256)),
+    "aniso_slab_dx128": (1, dict()),
+    "elastic_box_dx64": (0, dict()),
+}
+# CPU sample: the same slab at the same resolution, cropped to a 0.125 x 0.1 x 0.125 m piece
+CPU_SAMPLE = {"aniso_slab_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125)),
+              "aniso_slab_dx128": dict(size=(0.25, 0.1, 0.25)),
+              "elastic_box_dx64": dict()}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="aniso_slab_dx256", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------- helpers
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devs = vis.split(",") if vis else [str(i) for i in range(64)]
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local]
+        import torch.distributed as td
+
+        td.init_process_group("gloo")  # host-side barrier and max only: scenes are independent replicas
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+
+        td.barrier()
+
+
+def allreduce_max(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as td
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as td
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the GPU works (started before, stopped after)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [t.strip() for t in line.split(",")]
+                if len(parts) == 9 and parts[0] == vis:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/*.txt), or None."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith(".txt"):
+            continue
+        with open(os.path.join(pdir, fn)) as fh:
+            for line in fh:
+                # line format: "traffic_per_launch <kernel> <workload> <bytes>"
+                t = line.split()
+                if len(t) == 4 and t[0] == "traffic_per_launch" and t[1] == kernel and t[2] == workload:
+                    return float(t[3])
+    return None
+
+
+def algorithmic_bytes(s_bytes, n, blocks, nodes_per_block, damage):
+    """Compulsory DRAM bytes per launch of each phase (inputs read once, outputs written once).
+
+    particle fields: x3 v3 C9 F9 m V0 (+ d, sigma_c with damage), a 4-byte id; grid accumulators:
+    m, m v (3), f (3), phase field (2); grid velocities: v (3) + phase field."""
+    ns = n * s_bytes
+    nodes = blocks * nodes_per_block
+    dmg = 1 if damage else 0
+    p2g = ns * (26 + dmg) + 4 * n + nodes * s_bytes * 9
+    grid = nodes * s_bytes * (9 + 9 + 4)  # read accumulators, clear them, write velocities
+    g2p_read = ns * (12 + 2 + 2 * dmg) + 4 * n + nodes * s_bytes * 4
+    g2p_write = ns * (24 + 2 + 2 * dmg) + 4 * n + 8 * n
+    return {"p2g": p2g, "grid": grid, "g2p": g2p_read + g2p_write, "sort": n * (8 + 4) * 2}
+
+
+# ------------------------------------------------------------------------------------------- arms
+def run_reference(args, world, rank):
+    """The reference's CPU algorithm (the oracle restatement: the reference itself cannot be built here)
+    on all host threads, FP64 as the reference's AnisoMPM driver is compiled (anisofracture.cpp:13-14)."""
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle as po
+    import scenes
+
+    kind, over = WORKLOADS[args.workload]
+    smp = CPU_SAMPLE[args.workload]
+    desc = _desc_for(kind, smp, scenes)
+    o = scenes.oracle_scene(desc, 8)
+    n = len(desc["m"])
+    o.step(max(1, args.warmup))
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    el = time.perf_counter() - t0
+    val = n * args.steps / el
+    return {"impl": "reference", "metric": "particle-substeps/sec", "value": val, "unit": "particle-substeps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": _config(args),
+            "cpu_baseline": {"value": val, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port",
+                             "sample": f"{n} particles of the same slab at the same dx (cropped {smp.get('size')}), {args.steps} substeps"},
+            "e2e": {"value": val, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def _desc_for(kind, over, scenes):
+    if kind == 1:
+        dx = over.get("dx", 1 / 128)
+        return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345)
+    return scenes.elastic_box(size=over.get("size", 0.25), dx=over.get("dx", 1 / 64), seed=12345)
+
+
+def _config(args):
+    return {"workload": args.workload, "particles": None, "substeps_timed": args.steps, "precision_path": "fp32",
+            "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{args.gpus}"}
+
+
+def run_ours(args, world, rank):
+    import numpy as np
+
+    import ziran2020_gb300 as zr
+
+    kind, over = WORKLOADS[args.workload]
+    r = zr.recipe(kind, seed=12345 + rank, **over)
+    n = zr.recipe_count(r)
+    damage = kind == 1
+
+    s = zr.Scene(zr.F32)
+    s.from_recipe(r)
+    clocks = ClockSampler()
+    clocks.start()
+    s.step(args.warmup)
+    barrier(world)
+    s.step(args.steps)
+    ms = s.last_step_ms
+    barrier(world)
+    clock_info = clocks.stop()
+    ms_max = allreduce_max(world, ms)
+    n_total = allreduce_sum(world, n)
+    value = n_total * args.steps / (ms_max / 1e3)
+    stats = s.stats()
+    groups, blocks = s.last_grid()
+
+    # per-phase kernel durations (CUDA events on the engine's stream, substeps run without graphs)
+    kt_steps = min(args.steps, 20)
+    s.set_timing(True)
+    s.step(kt_steps)
+    phases, ksteps = s.timing()
+    s.set_timing(False)
+    per = {k: v / ksteps for k, v in phases.items()}
+    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(4, n, blocks, 64, damage)
+    dom = max(("p2g", "g2p"), key=lambda k: per[k])
+    achieved = alg[dom] / (per[dom] / 1e3) / 1e9
+    traffic = profiled_traffic(dom, args.workload)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6800 GB/s",
+            "traffic": traffic, "algorithmic_bytes": alg[dom], "kernel_ms": round(per[dom], 4),
+            "phase_ms_per_substep": {k: round(v, 4) for k, v in per.items()},
+            "frac_by_phase": {k: round(alg[k] / (per[k] / 1e3) / 1e9 / peak, 4) for k in ("p2g", "g2p", "grid") if per.get(k)}}
+
+    # end to end through the C ABI with pinned host buffers: upload state, one substep, download state
+    e2e = None
+    try:
+        import torch
+
+        host = torch.empty((n, 25), dtype=torch.float32).pin_memory().numpy()
+        s.get_state(host)
+        s.set_state(host)
+        s.step(1)
+        s.get_state(host)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            s.set_state(host)
+            s.step(1)
+            s.get_state(host)
+        el = time.perf_counter() - t0
+        nbytes = n * 25 * 4
+        e2e = {"value": allreduce_sum(world, n) * args.e2e_steps / allreduce_max(world, el), "unit": "particle-substeps/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "what": "per step: zr_scene_set_state from pinned FP32 host memory (x,v,C,F,d), zr_scene_step(1), zr_scene_get_state"}
+    except Exception as ex:  # pinned memory needs torch; report instead of failing the line
+        e2e = {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None, "error": str(ex)}
+    del s
+
+    # plain FP64 GPU path on the same workload
+    s64 = zr.Scene(zr.F64)
+    s64.from_recipe(r)
+    s64.step(2)
+    s64.step(args.fp64_steps)
+    fp64_value = n * args.fp64_steps / (s64.last_step_ms / 1e3)
+    del s64
+
+    # FP32 vs FP64 after the same number of substeps from the same seeded inputs
+    acc = None
+    if args.accuracy_steps > 0 and rank == 0:
+        a32, a64 = zr.Scene(zr.F32), zr.Scene(zr.F64)
+        a32.from_recipe(r)
+        a64.from_recipe(r)
+        a32.step(args.accuracy_steps)
+        a64.step(args.accuracy_steps)
+        acc = {"substeps": args.accuracy_steps, "reference": "FP64 GPU path (pinned to the FP64 oracle by tests/test_gpu_parity.py)"}
+        for f in ("x", "v", "F", "d"):
+            e = np.abs(a32.get(f) - a64.get(f))
+            acc[f] = {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
+        acc["x"]["note"] = "metres in a unit domain (domain-relative)"
+        del a32, a64
+
+    # CPU baseline: the oracle restatement on a bounded sample of the same workload, all host threads
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import pyoracle as po
+        import scenes
+
+        desc = _desc_for(kind, CPU_SAMPLE[args.workload], scenes)
+        o = scenes.oracle_scene(desc, 8)
+        ns = len(desc["m"])
+        t0 = time.perf_counter()
+        o.step(1)
+        one = time.perf_counter() - t0
+        k = max(1, min(50, int(args.cpu_seconds / max(one, 1e-3))))
+        t0 = time.perf_counter()
+        o.step(k)
+        el = time.perf_counter() - t0
+        cpu = {"value": ns * k / el, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
+               "sample": f"{ns} particles ({desc['dx']:.6g} m cells, cropped slab piece), {k} substeps, {el:.1f} s"}
+
+    cfg = _config(args)
+    cfg["particles"] = int(n)
+    cfg["active_blocks"] = int(blocks)
+    cfg["particle_groups"] = int(groups)
+    line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded recipe)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
+            "clocks": clock_info, "fp64_path": {"value": fp64_value, "unit": "particle-substeps/s", "fp32_over_fp64": value / world / fp64_value},
+            "fp32_vs_fp64_error": acc, "fp64_fallbacks": stats["fallbacks"]}
+    return line if rank == 0 else None
+
+
+def main():
+    args = parse()
+    world, rank = dist_setup()
+    if args.impl == "reference":
+        line = run_reference(args, world, rank)
+    else:
+        line = run_ours(args, world, rank)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

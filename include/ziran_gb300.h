@@ -1,0 +1,200 @@
+/*
+ * ziran_gb300.h — C ABI of the GB300-native explicit MPM substep.
+ *
+ * Drop-in boundary for Ziran's explicit MPM path (Lib/MPM over Lib/SPGrid, as driven by
+ * Projects/anisofracture). Plain pointers and sizes only. Every call returns an int status
+ * (ZR_OK = 0) and never throws; the message of the last failure is available per handle.
+ * A handle is used by one host thread at a time; different handles may be driven concurrently
+ * (each owns a CUDA stream). Host arrays are owned by the caller and copied; device state lives in
+ * HBM for the lifetime of the handle (the reference's Particles own their DataArrays the same way,
+ * Lib/Ziran/CS/DataStructure/DataManager.h:67-140).
+ *
+ * Conventions: positions in metres in the positive octant; 3x3 matrices row-major, 9 values per
+ * particle; "first/count" are particle ranges in the order particles were added.
+ */
+#ifndef ZIRAN_GB300_H
+#define ZIRAN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference throws: Debug.h:19-37, RestartException MpmSimulationBase.cpp:1498) ---- */
+#define ZR_OK 0
+#define ZR_ERR_ARG 1           /* invalid argument */
+#define ZR_ERR_CUDA 2          /* CUDA runtime failure or no device */
+#define ZR_ERR_CFL 3           /* a particle moved more than one cell; state is left at the start of that substep */
+#define ZR_ERR_NONFINITE 4     /* NaN/Inf in the particle state; state is left at the start of that substep */
+#define ZR_ERR_OUT_OF_DOMAIN 5 /* a base node left the scene domain; state is left at the start of that substep */
+#define ZR_ERR_BUDGET 6        /* request does not fit the serving memory budget */
+#define ZR_ERR_TIMEOUT 7       /* a bounded device wait gave up */
+#define ZR_ERR_CAPACITY 8      /* active-block table could not grow */
+#define ZR_ERR_STATE 9         /* call not valid in the handle's current state */
+
+/* ---- precision of the device state ---- */
+#define ZR_F32 4
+#define ZR_F64 8
+
+/* ---- constitutive models ---- */
+#define ZR_COROTATED 0           /* Physics/ConstitutiveModel/CorotatedElasticity.cpp */
+#define ZR_NEOHOOKEAN_BORDEN 1   /* Physics/ConstitutiveModel/NeoHookeanBorden.cpp */
+
+/* ---- collision object types (Math/Geometry/CollisionObject.h:47-50) ---- */
+#define ZR_STICKY 1
+#define ZR_SLIP 2
+#define ZR_SEPARATE 3
+
+/* ---- particle fields ---- */
+#define ZR_FIELD_X 0       /* 3 values */
+#define ZR_FIELD_V 1       /* 3 */
+#define ZR_FIELD_C 2       /* 9, APIC affine matrix */
+#define ZR_FIELD_F 3       /* 9, deformation gradient */
+#define ZR_FIELD_D 4       /* 1, damage */
+#define ZR_FIELD_M 5       /* 1, mass */
+#define ZR_FIELD_V0 6      /* 1, initial volume (element measure) */
+#define ZR_FIELD_SIGMA_C 7 /* 1, critical stress */
+
+typedef struct zr_scene zr_scene;
+typedef struct zr_batch zr_batch;
+typedef struct zr_server zr_server;
+
+/* Simulation knobs: the public members of MpmSimulationBase<T,3> (MpmSimulationBase.h:47-76).
+ * dt is the substep size (the reference's step.max_dt when the CFL bound does not bind).
+ * domain_cells bounds base-node coordinates to [0, domain_cells) (0 = the full 4096^3 SPGrid). */
+typedef struct zr_sim_params {
+    double dx;
+    double dt;
+    double gravity[3];
+    double apic_rpic_ratio; /* 1 = APIC, 0 = RPIC (MpmSimulationBase.cpp:39-40) */
+    double cfl;             /* default 0.6 (MpmSimulationBase.cpp:46) */
+    int32_t domain_cells;
+    int32_t reserved;
+} zr_sim_params;
+
+/* ======================= scene: one MpmSimulationBase<T,3> / AnisoFractureSimulation ======================= */
+
+/* MpmSimulationBase<T,3>::MpmSimulationBase() (MpmSimulationBase.cpp:36-67); precision ZR_F32 or ZR_F64. */
+int zr_scene_create(int precision, zr_scene** out);
+int zr_scene_destroy(zr_scene* s);
+/* sim.dx / sim.step.max_dt / sim.gravity / sim.apic_rpic_ratio / sim.cfl (MpmSimulationBase.h:47-76). */
+int zr_scene_set_params(zr_scene* s, const zr_sim_params* p);
+/* MpmInitializationHelper samplers + MpmParticleHandleBase (MpmInitializationHelper.h:114-123,1344-1414,
+ * MpmParticleHandleBase.cpp:72-79): adds n particles; v and F may be NULL (zero / identity).
+ * *first receives the index of the first added particle. */
+int zr_scene_add_particles(zr_scene* s, int64_t n, const double* x, const double* v, const double* m, const double* V0, const double* F,
+    int64_t* first);
+/* MpmParticleHandleBase::addFBasedMpmForce(CorotatedElasticity(E, nu)) (MpmParticleHandleBase.cpp:132-145). */
+int zr_scene_add_corotated(zr_scene* s, int64_t first, int64_t count, double E, double nu);
+/* MpmParticleHandleBase::addFBasedMpmForce(NeoHookeanBorden(E, nu)). */
+int zr_scene_add_neohookean_borden(zr_scene* s, int64_t first, int64_t count, double E, double nu);
+/* MpmParticleHandleBase::addFBasedMpmForceWithAnisotropicPhaseField (MpmParticleHandleBase.cpp:175-222) for a
+ * range that already has a Neo-Hookean (Borden) model: one structural director a0 = e1 with weight alpha
+ * (fibre directions are encoded in the initial F, see zr_rotated_F), length scale l0, viscosity eta,
+ * scale zeta, residual stiffness; sigma_crit holds one critical stress per particle of the range. */
+int zr_scene_add_aniso_damage(zr_scene* s, int64_t first, int64_t count, double alpha, double l0, double eta, double zeta, double residual,
+    const double* sigma_crit);
+/* init_helper.addAnalyticCollisionObject(AnalyticCollisionObject(HalfSpace(origin, normal), type)) with a
+ * translation b(t) = velocity * t (MpmInitializationHelper.h:1421-1424, CollisionObject.h:144-148). */
+int zr_scene_add_halfspace(zr_scene* s, const double origin[3], const double normal[3], int type, double friction, const double velocity[3]);
+/* nsteps calls of MpmSimulationBase::advanceOneTimeStep(dt) (MpmSimulationBase.cpp:262-357). On ZR_ERR_CFL,
+ * ZR_ERR_NONFINITE or ZR_ERR_OUT_OF_DOMAIN the state is left at the start of the failing substep and
+ * *done (may be NULL) tells how many substeps completed. */
+int zr_scene_step(zr_scene* s, int nsteps, int* done);
+/* Field read/write in the order particles were added; dtype ZR_F32 or ZR_F64 for the host buffer. */
+int zr_scene_get_field(zr_scene* s, int field, void* out, int dtype);
+int zr_scene_set_field(zr_scene* s, int field, const void* in, int dtype);
+/* Whole dynamic state, 25 values per particle: x(3) v(3) C(9) F(9) d(1). */
+int zr_scene_get_state(zr_scene* s, void* out, int dtype);
+int zr_scene_set_state(zr_scene* s, const void* in, int dtype);
+/* FP64-accumulated reductions (MpmSimulationDataAnalysis.h:67-151): total mass, momentum x/y/z, kinetic
+ * energy, max particle speed, grid mass of the last substep. */
+int zr_scene_reductions(zr_scene* s, double out[7]);
+int zr_scene_set_dt(zr_scene* s, double dt);
+double zr_scene_time(zr_scene* s);
+int64_t zr_scene_count(zr_scene* s);
+const char* zr_scene_last_error(zr_scene* s);
+/* device time (ms) of the substeps of the last zr_scene_step call: CUDA events on the scene's stream */
+double zr_scene_last_step_ms(zr_scene* s);
+/* largest number of particle groups (occupied SPGrid blocks) and active blocks seen in the last zr_scene_step */
+int zr_scene_last_grid(zr_scene* s, int64_t* n_groups, int64_t* n_blocks);
+/* Binning of the current positions (MpmSimulationBase::sortParticlesAndPolluteGrid,
+ * MpmSimulationBase.cpp:1531-1573, MpmGrid::pollute MpmGrid.h:153-193): the sorted 64-bit keys in the
+ * reference's layout (n), the sorted particle order (n), the first sorted index of every particle group
+ * (*n_groups, at most n) and the active SPGrid pages in ascending order (*n_pages, at most 8n). */
+int zr_scene_binning(zr_scene* s, uint64_t* sorted_keys, int32_t* order, int32_t* group_first, int64_t* n_groups, uint64_t* pages,
+    int64_t* n_pages);
+/* Per-phase device time (ms) of substeps run while timing is enabled: sort+groups, activate, p2g, grid,
+ * g2p; and the number of timed substeps. Timing runs the substeps without CUDA graphs. */
+int zr_scene_set_timing(zr_scene* s, int on);
+int zr_scene_get_timing(zr_scene* s, double out5[5], int64_t* steps);
+/* kernels launched per substep (CUDA-graph node count) and device bytes held by the scene. */
+int zr_scene_stats(zr_scene* s, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
+
+/* ================================ scene recipes (seeded synthetic scenes) ================================ */
+#define ZR_RECIPE_ELASTIC_BOX 0 /* falling corotated cube over a sticky ground plane */
+#define ZR_RECIPE_ANISO_SLAB 1  /* Neo-Hookean slab with vMF fibres and anisotropic damage, ends pulled apart */
+
+typedef struct zr_scene_recipe {
+    int32_t kind;
+    int32_t ppc_side;     /* particles per cell = ppc_side^3 (2 -> 8) */
+    uint64_t seed;
+    double dx, dt;
+    double size[3];       /* extents in metres, snapped to whole cells */
+    double center[3];
+    double velocity[3];   /* initial velocity */
+    double gravity[3];
+    double E, nu, rho;
+    double apic_rpic_ratio;
+    double ground_y;      /* ELASTIC_BOX: sticky half-space y <= ground_y */
+    double kappa_vmf;     /* ANISO_SLAB: von Mises-Fisher concentration of fibres about +x */
+    double alpha, l0, eta, zeta, residual;
+    double sigma_c_mean, sigma_c_std;
+    double pull_speed;    /* ANISO_SLAB: the two x ends move apart at +-pull_speed */
+    double grip_cells;    /* ANISO_SLAB: width of each sticky end plate in cells */
+    int32_t domain_cells; /* 0 = round(1/dx) + 4 (the unit box) */
+    int32_t reserved;
+} zr_scene_recipe;
+
+/* Defaults: ELASTIC_BOX = unit box, dx 1/64, cube side 0.25 at (0.5,0.6,0.5), 8 ppc, corotated E=1e4
+ * nu=0.3 rho=1000, v0=(0,-1,0), gravity -9.8, ground y=0.05, dt=1e-4, APIC. ANISO_SLAB = dx 1/128,
+ * 0.5x0.1x0.5 slab at (0.5,0.5,0.5), 8 ppc, Neo-Hookean E=5e4 nu=0.25 rho=800, kappa=20, alpha=-1,
+ * l0=0.5dx, eta=0.1, zeta=1, k=0.01, sigma_c ~ N(400,40), ends pulled at 0.5 m/s, dt=5e-5, RPIC. */
+int zr_recipe_default(int kind, zr_scene_recipe* out);
+/* number of particles the recipe generates */
+int64_t zr_recipe_count(const zr_scene_recipe* r);
+/* Generate the recipe's particles into caller arrays (any may be NULL): x(3n) v(3n) m(n) V0(n) F(9n) sigma_c(n). */
+int zr_recipe_generate(const zr_scene_recipe* r, double* x, double* v, double* m, double* V0, double* F, double* sigma_c);
+/* Build a whole scene (params, particles, materials, damage, collision objects) from a recipe. */
+int zr_scene_from_recipe(zr_scene* s, const zr_scene_recipe* r);
+/* MpmParticleHandleBase::initializeRotatedFHelper (MpmParticleHandleBase.cpp:224-268) for one unit director. */
+void zr_rotated_F(const double a0[3], double F[9]);
+/* NeoHookeanBorden::getSigmaCrit(percentage) (NeoHookeanBorden.cpp:38-44): psi at F = (1+p) I. */
+double zr_nhb_sigma_crit(double E, double nu, double percentage);
+
+/* ================================ batch: many scenes, one launch per kernel ================================ */
+int zr_batch_create(int precision, zr_batch** out);
+int zr_batch_destroy(zr_batch* b);
+/* Copies the scene's current description into the batch (the scene handle stays usable). *slot receives
+ * its index in the batch. Scenes must be added before zr_batch_commit. */
+int zr_batch_add_scene(zr_batch* b, zr_scene* s, int* slot);
+int zr_batch_add_recipe(zr_batch* b, const zr_scene_recipe* r, int* slot);
+int zr_batch_commit(zr_batch* b);
+int zr_batch_step(zr_batch* b, int nsteps, int* done);
+int zr_batch_get_field(zr_batch* b, int slot, int field, void* out, int dtype);
+int zr_batch_reductions(zr_batch* b, int slot, double out[7]);
+int64_t zr_batch_count(zr_batch* b, int slot);
+int zr_batch_set_timing(zr_batch* b, int on);
+int zr_batch_get_timing(zr_batch* b, double out5[5], int64_t* steps);
+int zr_batch_stats(zr_batch* b, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
+const char* zr_batch_last_error(zr_batch* b);
+double zr_batch_last_step_ms(zr_batch* b);
+
+/* library version string */
+const char* zr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

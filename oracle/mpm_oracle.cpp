@@ -43,7 +43,6 @@
 #include <cstring>
 #include <limits>
 #include <type_traits>
-#include <unordered_map>
 #include <utility>
 #include <vector>
 #ifdef _OPENMP
@@ -79,14 +78,30 @@ struct Layout {
     static constexpr int nodes_per_block = 1 << block_bits;
 
     // Bit deposit: the low bits of v go, in order, to the set bits of mask (SPGrid_Utilities.h Bit_Spread).
+    // A negative value is sign-extended, so all mask bits above its magnitude receive ones.
+    struct Positions {
+        int pos[64];
+        int count;
+    };
+    static Positions positions(uint64_t mask)
+    {
+        Positions P{};
+        for (int b = 0; b < 64; b++)
+            if (mask & (1ULL << b)) P.pos[P.count++] = b;
+        return P;
+    }
     static uint64_t deposit(int64_t sv, uint64_t mask)
     {
+        static const Positions PX = positions(xmask), PY = positions(ymask), PZ = positions(zmask);
+        const Positions& P = mask == xmask ? PX : (mask == ymask ? PY : (mask == zmask ? PZ : positions(mask)));
         uint64_t v = (uint64_t)sv, r = 0;
-        for (uint64_t bit = 1; bit; bit <<= 1)
-            if (mask & bit) {
-                if (v & 1) r |= bit;
-                v >>= 1;
-            }
+        if (sv < 0) {
+            for (int k = 0; k < P.count; k++)
+                if (k >= 64 || ((v >> k) & 1)) r |= 1ULL << P.pos[k];
+            return r;
+        }
+        for (int k = 0; v && k < P.count; k++, v >>= 1)
+            if (v & 1) r |= 1ULL << P.pos[k];
         return r;
     }
     // Bit extract, the inverse of deposit (SPGrid Bit_Pack).
@@ -675,6 +690,66 @@ inline void multi_object_collision(const std::vector<HalfSpace<T>>& objs, T time
 // ----------------------------------------------------------------------------------------------
 // Scene
 // ----------------------------------------------------------------------------------------------
+// Open-addressing page -> block-slot table (stands in for SPGrid_Page_Map's bitmap, SPGrid_Page_Map.h:61-95).
+struct PageTable {
+    std::vector<uint64_t> keys;
+    std::vector<int> vals;
+    uint64_t mask = 0;
+    int count = 0;
+    void reset(size_t expect)
+    {
+        size_t cap = 1024;
+        while (cap < 2 * expect) cap <<= 1;
+        keys.assign(cap, ~0ULL);
+        vals.assign(cap, -1);
+        mask = cap - 1;
+        count = 0;
+    }
+    static uint64_t h(uint64_t k)
+    {
+        k ^= k >> 31;
+        k *= 0x9e3779b97f4a7c15ULL;
+        return k ^ (k >> 29);
+    }
+    // returns true when the page was not present (and inserts it with slot = count)
+    bool insert(uint64_t page)
+    {
+        if (2 * (size_t)(count + 1) > keys.size()) grow();
+        uint64_t i = h(page) & mask;
+        while (keys[i] != ~0ULL) {
+            if (keys[i] == page) return false;
+            i = (i + 1) & mask;
+        }
+        keys[i] = page;
+        vals[i] = count++;
+        return true;
+    }
+    int at(uint64_t page) const
+    {
+        uint64_t i = h(page) & mask;
+        while (keys[i] != ~0ULL) {
+            if (keys[i] == page) return vals[i];
+            i = (i + 1) & mask;
+        }
+        return -1;
+    }
+    void grow()
+    {
+        std::vector<uint64_t> ok = keys;
+        std::vector<int> ov = vals;
+        keys.assign(ok.size() * 2, ~0ULL);
+        vals.assign(ok.size() * 2, -1);
+        mask = keys.size() - 1;
+        for (size_t q = 0; q < ok.size(); q++)
+            if (ok[q] != ~0ULL) {
+                uint64_t i = h(ok[q]) & mask;
+                while (keys[i] != ~0ULL) i = (i + 1) & mask;
+                keys[i] = ok[q];
+                vals[i] = ov[q];
+            }
+    }
+};
+
 template <class T>
 struct Node {
     T v[3];
@@ -703,10 +778,11 @@ struct Scene {
     std::vector<int32_t> order;
     std::vector<std::pair<int, int>> groups;
     std::vector<uint64_t> pages; // first-touch order (MpmGrid.h:157-183, SPGrid_Page_Map.h:61-70)
-    std::unordered_map<uint64_t, int> page_slot;
+    PageTable page_slot;
     std::vector<Node<T>> grid; // pages.size() * nodes_per_block
     std::vector<std::array<int, 8>> group_nbr; // neighbour block slots of each group, index dx*4+dy*2+dz
     int cfl_flags = 0;
+    size_t pages_hint = 1024;
 
     void bin()
     {
@@ -741,29 +817,26 @@ struct Scene {
         }
         // pollute: original particle order, consecutive dedup, page of base node + 7 neighbours
         pages.clear();
-        page_slot.clear();
+        page_slot.reset(pages_hint);
         auto set_page = [&](uint64_t off) {
             uint64_t p = off >> 12;
-            if (page_slot.emplace(p, (int)pages.size()).second) pages.push_back(p);
+            if (page_slot.insert(p)) pages.push_back(p);
         };
+        uint64_t nbr_disp[8];
+        for (int a = 0; a < 8; a++) nbr_disp[a] = L::linear_offset(L::sx * (a >> 2), L::sy * ((a >> 1) & 1), L::sz * (a & 1));
         for (int64_t i = 0; i < n; i++) {
             uint64_t off = base_offset[i];
             if (i == 0 || off != base_offset[i - 1]) {
                 set_page(off);
-                for (int a = 0; a <= 1; a++)
-                    for (int b = 0; b <= 1; b++)
-                        for (int c = 0; c <= 1; c++)
-                            set_page(L::packed_add(off, L::linear_offset(L::sx * a, L::sy * b, L::sz * c)));
+                for (int a = 0; a < 8; a++) set_page(L::packed_add(off, nbr_disp[a]));
             }
         }
+        pages_hint = pages.size();
         grid.assign(pages.size() * L::nodes_per_block, Node<T>{});
         group_nbr.resize(groups.size());
         for (size_t g = 0; g < groups.size(); g++) {
             uint64_t off = block_offset[g] << 12;
-            for (int a = 0; a < 8; a++) {
-                uint64_t no = L::packed_add(off, L::linear_offset(L::sx * (a >> 2), L::sy * ((a >> 1) & 1), L::sz * (a & 1)));
-                group_nbr[g][a] = page_slot.at(no >> 12);
-            }
+            for (int a = 0; a < 8; a++) group_nbr[g][a] = page_slot.at(L::packed_add(off, nbr_disp[a]) >> 12);
         }
     }
 

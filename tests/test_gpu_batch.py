@@ -1,0 +1,29 @@
+"""GPU: a batch of independent scenes gives each scene's result as when it runs alone."""
+import numpy as np
+import pytest
+
+import ziran2020_gb300 as zr
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_batch_matches_single_scenes(prec):
+    descs = [scenes.elastic_box(size=0.0625, seed=1, center=(0.4, 0.5, 0.5)),
+             scenes.elastic_box(size=0.125, seed=2, E=3e4, v0=(0.5, -0.5, 0.2)),
+             scenes.aniso_slab(size=(0.08, 0.04, 0.08), sigma_c=(20.0, 2.0), pull=1.0)]
+    b = zr.Batch(prec)
+    singles = []
+    for d in descs:
+        sc = scenes.gpu_scene(d, prec)
+        b.add_scene(sc)
+        singles.append(sc)
+    b.commit()
+    b.step(25)
+    tol = 1e-11 if prec == 8 else 2e-6
+    for k, sc in enumerate(singles):
+        sc.step(25)
+        for f in ("x", "v", "F", "d"):
+            a, c = b.get(k, f), sc.get(f)
+            assert np.abs(a - c).max() <= tol * max(1.0, np.abs(c).max()), (k, f, np.abs(a - c).max())

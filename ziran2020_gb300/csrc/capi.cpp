@@ -1,0 +1,766 @@
+// C ABI of the GB300 explicit-MPM engine (declared in include/ziran_gb300.h).
+#include "../../include/ziran_gb300.h"
+#include "engine.h"
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+using namespace zr;
+
+struct zr_scene {
+    double last_ms = 0;
+    int64_t last_groups = 0, last_blocks = 0;
+    int precision = ZR_F32;
+    SceneDesc desc;
+    std::unique_ptr<EngineBase> eng;
+    std::string err;
+    bool committed = false;
+    int64_t fallbacks = 0;
+};
+
+struct zr_batch {
+    double last_ms = 0;
+    int precision = ZR_F32;
+    std::vector<std::unique_ptr<SceneDesc>> descs;
+    std::unique_ptr<EngineBase> eng;
+    std::string err;
+    bool committed = false;
+    int64_t fallbacks = 0;
+};
+
+namespace {
+
+const char* kVersion = "ziran2020_gb300 0.1 (sm_103a)";
+
+int set_err(std::string& e, int code, const std::string& m)
+{
+    e = m;
+    return code;
+}
+
+std::unique_ptr<EngineBase> make_engine(int precision)
+{
+    return precision == ZR_F64 ? make_engine_f64() : make_engine_f32();
+}
+
+// assign a material to a particle range, creating a new material entry
+int assign_material(SceneDesc& d, int64_t first, int64_t count, const SceneDesc::Mat& m, std::string& err)
+{
+    if (first < 0 || count < 0 || first + count > d.n) return set_err(err, ZR_ERR_ARG, "particle range out of bounds");
+    if ((int)d.materials.size() >= 16) return set_err(err, ZR_ERR_ARG, "at most 16 materials per scene");
+    if (d.material.empty() && !d.materials.empty()) d.material.assign(d.n, 0);
+    if (d.material.size() < (size_t)d.n) d.material.resize(d.n, 0);
+    d.materials.push_back(m);
+    const uint8_t id = (uint8_t)(d.materials.size() - 1);
+    for (int64_t i = first; i < first + count; i++) d.material[i] = id;
+    return ZR_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// seeded generators (identical on every host: raw mt19937_64 outputs, own uniform / normal / vMF)
+// ---------------------------------------------------------------------------------------------------
+struct Rng {
+    std::mt19937_64 g;
+    explicit Rng(uint64_t seed) : g(seed) {}
+    double uniform() { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); } // [0,1)
+    double normal()
+    {
+        double u1 = uniform(), u2 = uniform();
+        if (u1 < 1e-300) u1 = 1e-300;
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+    // von Mises-Fisher on the unit sphere about +x (Wood's method for three dimensions)
+    void vmf(double kappa, double out[3])
+    {
+        double u = uniform();
+        double w = 1.0 + std::log(u + (1.0 - u) * std::exp(-2.0 * kappa)) / kappa;
+        if (w > 1) w = 1;
+        if (w < -1) w = -1;
+        double phi = 6.283185307179586 * uniform();
+        double r = std::sqrt(std::max(0.0, 1.0 - w * w));
+        out[0] = w;
+        out[1] = r * std::cos(phi);
+        out[2] = r * std::sin(phi);
+    }
+};
+
+void recipe_cells(const zr_scene_recipe* r, int64_t nc[3], int64_t lo[3])
+{
+    for (int a = 0; a < 3; a++) {
+        nc[a] = std::max<int64_t>(1, std::llround(r->size[a] / r->dx));
+        lo[a] = std::llround((r->center[a] - 0.5 * (double)nc[a] * r->dx) / r->dx);
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+const char* zr_version(void) { return kVersion; }
+
+// MpmParticleHandleBase::initializeRotatedFHelper, one director (MpmParticleHandleBase.cpp:224-268):
+// columns a0, a0_perp = normalize(-a0y, a0x, 0) (e1 when a0 is along z), a0 x a0_perp
+void zr_rotated_F(const double a0[3], double F[9])
+{
+    double c1[3];
+    if (std::fabs(a0[0]) < 1e-6 && std::fabs(a0[1]) < 1e-6) {
+        c1[0] = 1;
+        c1[1] = 0;
+        c1[2] = 0;
+    }
+    else {
+        c1[0] = -a0[1];
+        c1[1] = a0[0];
+        c1[2] = 0;
+        double nn = std::sqrt(c1[0] * c1[0] + c1[1] * c1[1]);
+        c1[0] /= nn;
+        c1[1] /= nn;
+    }
+    double c2[3] = { a0[1] * c1[2] - a0[2] * c1[1], a0[2] * c1[0] - a0[0] * c1[2], a0[0] * c1[1] - a0[1] * c1[0] };
+    for (int r = 0; r < 3; r++) {
+        F[3 * r + 0] = a0[r];
+        F[3 * r + 1] = c1[r];
+        F[3 * r + 2] = c2[r];
+    }
+}
+
+// NeoHookeanBorden::getSigmaCrit: psi((1+p) I) with g = 1 (NeoHookeanBorden.cpp:38-68)
+double zr_nhb_sigma_crit(double E, double nu, double p)
+{
+    double lambda = E * nu / ((1 + nu) * (1 - 2 * nu));
+    double mu = E / (2 * (1 + nu));
+    double kappa = 0.666666 * mu + lambda;
+    double J = (1 + p) * (1 + p) * (1 + p);
+    // the deviatoric part vanishes for an isotropic stretch; psi = psi_vol whether J >= 1 or not
+    return kappa / 2 * ((J * J - 1) / 2 - std::log(J));
+}
+
+int zr_recipe_default(int kind, zr_scene_recipe* r)
+{
+    if (!r) return ZR_ERR_ARG;
+    std::memset(r, 0, sizeof *r);
+    r->kind = kind;
+    r->ppc_side = 2;
+    r->seed = 12345;
+    if (kind == ZR_RECIPE_ELASTIC_BOX) {
+        r->dx = 1.0 / 64;
+        r->dt = 1e-4;
+        r->size[0] = r->size[1] = r->size[2] = 0.25;
+        r->center[0] = 0.5;
+        r->center[1] = 0.6;
+        r->center[2] = 0.5;
+        r->velocity[1] = -1.0;
+        r->gravity[1] = -9.8;
+        r->E = 1e4;
+        r->nu = 0.3;
+        r->rho = 1000;
+        r->apic_rpic_ratio = 1.0;
+        r->ground_y = 0.05;
+        return ZR_OK;
+    }
+    if (kind == ZR_RECIPE_ANISO_SLAB) {
+        r->dx = 1.0 / 128;
+        r->dt = 5e-5;
+        r->size[0] = 0.5;
+        r->size[1] = 0.1;
+        r->size[2] = 0.5;
+        r->center[0] = r->center[1] = r->center[2] = 0.5;
+        r->E = 5e4;
+        r->nu = 0.25;
+        r->rho = 800;
+        r->apic_rpic_ratio = 0.0; // the AnisoMPM demos run RPIC (examples/vonMisesTear.h:28)
+        r->kappa_vmf = 20;
+        r->alpha = -1;
+        r->l0 = 0.5 * r->dx;
+        r->eta = 0.1;
+        r->zeta = 1;
+        r->residual = 0.01;
+        r->sigma_c_mean = 400;
+        r->sigma_c_std = 40;
+        r->pull_speed = 0.5;
+        r->grip_cells = 2;
+        return ZR_OK;
+    }
+    return ZR_ERR_ARG;
+}
+
+int64_t zr_recipe_count(const zr_scene_recipe* r)
+{
+    if (!r || r->dx <= 0 || r->ppc_side <= 0) return -1;
+    int64_t nc[3], lo[3];
+    recipe_cells(r, nc, lo);
+    int64_t p = r->ppc_side;
+    return nc[0] * nc[1] * nc[2] * p * p * p;
+}
+
+int zr_recipe_generate(const zr_scene_recipe* r, double* x, double* v, double* m, double* V0, double* F, double* sigma_c)
+{
+    if (!r || r->dx <= 0 || r->ppc_side <= 0) return ZR_ERR_ARG;
+    int64_t nc[3], lo[3];
+    recipe_cells(r, nc, lo);
+    const int ps = r->ppc_side;
+    const double sub = r->dx / ps;
+    const double vol = r->dx * r->dx * r->dx / (double)(ps * ps * ps);
+    Rng rng(r->seed);
+    int64_t p = 0;
+    for (int64_t i = 0; i < nc[0]; i++)
+        for (int64_t j = 0; j < nc[1]; j++)
+            for (int64_t k = 0; k < nc[2]; k++)
+                for (int a = 0; a < ps; a++)
+                    for (int b = 0; b < ps; b++)
+                        for (int c = 0; c < ps; c++, p++) {
+                            const int64_t cell[3] = { lo[0] + i, lo[1] + j, lo[2] + k };
+                            const int s[3] = { a, b, c };
+                            for (int d = 0; d < 3; d++) {
+                                double u = rng.uniform();
+                                if (x) x[3 * p + d] = (double)cell[d] * r->dx + ((double)s[d] + u) * sub;
+                                if (v) v[3 * p + d] = r->velocity[d];
+                            }
+                            if (m) m[p] = r->rho * vol;
+                            if (V0) V0[p] = vol;
+                            if (r->kind == ZR_RECIPE_ANISO_SLAB) {
+                                double a0[3];
+                                rng.vmf(r->kappa_vmf, a0);
+                                if (F) zr_rotated_F(a0, F + 9 * p);
+                                double sc = r->sigma_c_mean + r->sigma_c_std * rng.normal();
+                                if (sigma_c) sigma_c[p] = sc;
+                            }
+                            else {
+                                if (F)
+                                    for (int q = 0; q < 9; q++) F[9 * p + q] = (q % 4 == 0) ? 1.0 : 0.0;
+                                if (sigma_c) sigma_c[p] = 1.0;
+                            }
+                        }
+    return ZR_OK;
+}
+
+// ------------------------------------------------------------------------------------------- scene
+int zr_scene_create(int precision, zr_scene** out)
+{
+    if (!out || (precision != ZR_F32 && precision != ZR_F64)) return ZR_ERR_ARG;
+    zr_scene* s = new (std::nothrow) zr_scene();
+    if (!s) return ZR_ERR_ARG;
+    s->precision = precision;
+    *out = s;
+    return ZR_OK;
+}
+
+int zr_scene_destroy(zr_scene* s)
+{
+    delete s;
+    return ZR_OK;
+}
+
+int zr_scene_set_params(zr_scene* s, const zr_sim_params* p)
+{
+    if (!s || !p) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "parameters are fixed once the scene has stepped; use zr_scene_set_dt");
+    if (!(p->dx > 0) || !(p->dt > 0)) return set_err(s->err, ZR_ERR_ARG, "dx and dt must be positive");
+    if (p->apic_rpic_ratio < 0 || p->apic_rpic_ratio > 1) return set_err(s->err, ZR_ERR_ARG, "apic_rpic_ratio must be in [0,1] (MpmSimulationBase.cpp:125)");
+    s->desc.dx = p->dx;
+    s->desc.dt = p->dt;
+    for (int a = 0; a < 3; a++) s->desc.gravity[a] = p->gravity[a];
+    s->desc.apic_rpic_ratio = p->apic_rpic_ratio;
+    s->desc.cfl = p->cfl > 0 ? p->cfl : 0.6;
+    s->desc.domain_cells = p->domain_cells;
+    return ZR_OK;
+}
+
+int zr_scene_add_particles(zr_scene* s, int64_t n, const double* x, const double* v, const double* m, const double* V0, const double* F, int64_t* first)
+{
+    if (!s || n <= 0 || !x || !m || !V0) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "particles must be added before the first substep");
+    SceneDesc& d = s->desc;
+    const int64_t f0 = d.n;
+    d.x.insert(d.x.end(), x, x + 3 * n);
+    if (v)
+        d.v.insert(d.v.end(), v, v + 3 * n);
+    else
+        d.v.insert(d.v.end(), 3 * n, 0.0);
+    d.m.insert(d.m.end(), m, m + n);
+    d.V0.insert(d.V0.end(), V0, V0 + n);
+    if (F)
+        d.F.insert(d.F.end(), F, F + 9 * n);
+    else
+        for (int64_t i = 0; i < n; i++)
+            for (int q = 0; q < 9; q++) d.F.push_back((q % 4 == 0) ? 1.0 : 0.0);
+    d.C.insert(d.C.end(), 9 * n, 0.0);
+    d.d.insert(d.d.end(), n, 0.0);
+    d.sigma_c.insert(d.sigma_c.end(), n, 1.0);
+    if (!d.material.empty()) d.material.resize(f0 + n, 0);
+    d.n = f0 + n;
+    if (first) *first = f0;
+    return ZR_OK;
+}
+
+static int add_model(zr_scene* s, int64_t first, int64_t count, int model, double E, double nu)
+{
+    if (!s) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "materials must be attached before the first substep");
+    if (!(E > 0) || !(nu > -1 && nu < 0.5)) return set_err(s->err, ZR_ERR_ARG, "need E > 0 and -1 < nu < 0.5");
+    SceneDesc::Mat m;
+    m.model = model;
+    m.E = E;
+    m.nu = nu;
+    return assign_material(s->desc, first, count, m, s->err);
+}
+
+int zr_scene_add_corotated(zr_scene* s, int64_t first, int64_t count, double E, double nu) { return add_model(s, first, count, ZR_COROTATED, E, nu); }
+int zr_scene_add_neohookean_borden(zr_scene* s, int64_t first, int64_t count, double E, double nu)
+{
+    return add_model(s, first, count, ZR_NEOHOOKEAN_BORDEN, E, nu);
+}
+
+int zr_scene_add_aniso_damage(zr_scene* s, int64_t first, int64_t count, double alpha, double l0, double eta, double zeta, double residual,
+    const double* sigma_crit)
+{
+    if (!s || !sigma_crit) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "damage must be attached before the first substep");
+    SceneDesc& d = s->desc;
+    if (first < 0 || count <= 0 || first + count > d.n) return set_err(s->err, ZR_ERR_ARG, "particle range out of bounds");
+    if (d.material.empty() || d.materials.empty()) return set_err(s->err, ZR_ERR_ARG, "attach a Neo-Hookean (Borden) model to the range first");
+    const uint8_t base = d.material[first];
+    for (int64_t i = first; i < first + count; i++)
+        if (d.material[i] != base) return set_err(s->err, ZR_ERR_ARG, "the range must carry a single model");
+    if (d.materials[base].model != ZR_NEOHOOKEAN_BORDEN)
+        return set_err(s->err, ZR_ERR_ARG, "anisotropic damage is defined for the Neo-Hookean (Borden) model");
+    if (!(eta > 0)) return set_err(s->err, ZR_ERR_ARG, "eta must be positive");
+    SceneDesc::Mat m = d.materials[base];
+    m.damage = 1;
+    m.alpha = alpha;
+    m.l0 = l0;
+    m.eta = eta;
+    m.zeta = zeta;
+    m.residual = residual;
+    int rc = assign_material(d, first, count, m, s->err);
+    if (rc) return rc;
+    for (int64_t i = 0; i < count; i++) {
+        if (!(sigma_crit[i] > 0)) return set_err(s->err, ZR_ERR_ARG, "sigma_crit must be positive");
+        d.sigma_c[first + i] = sigma_crit[i];
+    }
+    return ZR_OK;
+}
+
+int zr_scene_add_halfspace(zr_scene* s, const double origin[3], const double normal[3], int type, double friction, const double velocity[3])
+{
+    if (!s || !origin || !normal) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "collision objects must be added before the first substep");
+    if (type < ZR_STICKY || type > ZR_SEPARATE) return set_err(s->err, ZR_ERR_ARG, "type must be ZR_STICKY, ZR_SLIP or ZR_SEPARATE");
+    if ((int)s->desc.objects.size() >= 8) return set_err(s->err, ZR_ERR_ARG, "at most 8 collision objects per scene");
+    SceneDesc::Obj o;
+    for (int a = 0; a < 3; a++) {
+        o.origin[a] = origin[a];
+        o.normal[a] = normal[a];
+        o.vel[a] = velocity ? velocity[a] : 0.0;
+    }
+    o.friction = friction;
+    o.type = type;
+    s->desc.objects.push_back(o);
+    return ZR_OK;
+}
+
+static int commit(zr_scene* s)
+{
+    if (s->committed) return ZR_OK;
+    if (s->desc.n <= 0) return set_err(s->err, ZR_ERR_STATE, "no particles");
+    if (s->desc.materials.empty()) return set_err(s->err, ZR_ERR_STATE, "no constitutive model attached");
+    // particles without an explicit model take the first one
+    s->eng = make_engine(s->precision);
+    std::vector<const SceneDesc*> v{ &s->desc };
+    int rc = s->eng->load(v);
+    if (rc) {
+        s->err = s->eng->last_error();
+        s->eng.reset();
+        return rc;
+    }
+    s->committed = true;
+    return ZR_OK;
+}
+
+int zr_scene_step(zr_scene* s, int nsteps, int* done)
+{
+    if (!s) return ZR_ERR_ARG;
+    if (done) *done = 0;
+    int rc = commit(s);
+    if (rc) return rc;
+    StepReport rep;
+    rc = s->eng->step(nsteps, &rep);
+    s->fallbacks += rep.fallback;
+    s->last_ms = rep.device_ms;
+    s->last_groups = rep.n_groups;
+    s->last_blocks = rep.n_blocks;
+    if (done) *done = rep.steps_done;
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+#define NEED_ENGINE(s)            \
+    do {                          \
+        if (!s) return ZR_ERR_ARG; \
+        int rc_ = commit(s);      \
+        if (rc_) return rc_;      \
+    } while (0)
+
+int zr_scene_get_field(zr_scene* s, int field, void* out, int dtype)
+{
+    NEED_ENGINE(s);
+    if (!out || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = s->eng->get_field(0, field, out, dtype == ZR_F32);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+int zr_scene_set_field(zr_scene* s, int field, const void* in, int dtype)
+{
+    NEED_ENGINE(s);
+    if (!in || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = s->eng->set_field(0, field, in, dtype == ZR_F32);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+int zr_scene_get_state(zr_scene* s, void* out, int dtype)
+{
+    NEED_ENGINE(s);
+    if (!out || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = s->eng->get_state(0, out, dtype == ZR_F32);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+int zr_scene_set_state(zr_scene* s, const void* in, int dtype)
+{
+    NEED_ENGINE(s);
+    if (!in || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = s->eng->set_state(0, in, dtype == ZR_F32);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+int zr_scene_reductions(zr_scene* s, double out[7])
+{
+    NEED_ENGINE(s);
+    if (!out) return ZR_ERR_ARG;
+    int rc = s->eng->reductions(0, out);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+int zr_scene_set_dt(zr_scene* s, double dt)
+{
+    if (!s || !(dt > 0)) return ZR_ERR_ARG;
+    s->desc.dt = dt;
+    if (!s->committed) return ZR_OK;
+    int rc = s->eng->set_dt(0, dt);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
+double zr_scene_time(zr_scene* s)
+{
+    if (!s) return NAN;
+    if (!s->committed) return s->desc.time;
+    return s->eng->time(0);
+}
+
+int64_t zr_scene_count(zr_scene* s) { return s ? s->desc.n : -1; }
+
+const char* zr_scene_last_error(zr_scene* s) { return s ? s->err.c_str() : "null scene"; }
+
+double zr_scene_last_step_ms(zr_scene* s) { return s ? s->last_ms : -1.0; }
+
+int zr_scene_last_grid(zr_scene* s, int64_t* n_groups, int64_t* n_blocks)
+{
+    if (!s) return ZR_ERR_ARG;
+    if (n_groups) *n_groups = s->last_groups;
+    if (n_blocks) *n_blocks = s->last_blocks;
+    return ZR_OK;
+}
+double zr_batch_last_step_ms(zr_batch* b) { return b ? b->last_ms : -1.0; }
+
+int zr_scene_binning(zr_scene* s, uint64_t* sorted_keys, int32_t* order, int32_t* group_first, int64_t* n_groups, uint64_t* pages, int64_t* n_pages)
+{
+    NEED_ENGINE(s);
+    std::vector<uint64_t> k, pg;
+    std::vector<int32_t> o, gf;
+    int rc = s->eng->binning(0, k, o, gf, pg);
+    if (rc) {
+        s->err = s->eng->last_error();
+        return rc;
+    }
+    if (sorted_keys) std::memcpy(sorted_keys, k.data(), 8 * k.size());
+    if (order) std::memcpy(order, o.data(), 4 * o.size());
+    if (group_first) std::memcpy(group_first, gf.data(), 4 * gf.size());
+    if (n_groups) *n_groups = (int64_t)gf.size();
+    if (pages) std::memcpy(pages, pg.data(), 8 * pg.size());
+    if (n_pages) *n_pages = (int64_t)pg.size();
+    return ZR_OK;
+}
+
+int zr_scene_set_timing(zr_scene* s, int on)
+{
+    NEED_ENGINE(s);
+    s->eng->set_timing(on != 0);
+    s->eng->reset_timing();
+    return ZR_OK;
+}
+
+int zr_scene_get_timing(zr_scene* s, double out5[5], int64_t* steps)
+{
+    NEED_ENGINE(s);
+    KernelTimes t = s->eng->timing();
+    if (out5) {
+        out5[0] = t.sort;
+        out5[1] = t.blocks;
+        out5[2] = t.p2g;
+        out5[3] = t.grid;
+        out5[4] = t.g2p;
+    }
+    if (steps) *steps = t.steps;
+    return ZR_OK;
+}
+
+int zr_scene_stats(zr_scene* s, int64_t* launches, int64_t* bytes, int64_t* fallbacks)
+{
+    NEED_ENGINE(s);
+    if (launches) *launches = s->eng->kernel_launches_per_step();
+    if (bytes) *bytes = s->eng->device_bytes();
+    if (fallbacks) *fallbacks = s->fallbacks;
+    return ZR_OK;
+}
+
+static int desc_from_recipe(SceneDesc& d, const zr_scene_recipe* r, std::string& err)
+{
+    int64_t n = zr_recipe_count(r);
+    if (n <= 0) return set_err(err, ZR_ERR_ARG, "bad recipe");
+    d = SceneDesc();
+    d.dx = r->dx;
+    d.dt = r->dt;
+    for (int a = 0; a < 3; a++) d.gravity[a] = r->gravity[a];
+    d.apic_rpic_ratio = r->apic_rpic_ratio;
+    d.cfl = 0.6;
+    d.domain_cells = r->domain_cells > 0 ? r->domain_cells : (int32_t)std::lround(1.0 / r->dx) + 4;
+    d.n = n;
+    d.x.resize(3 * n);
+    d.v.resize(3 * n);
+    d.m.resize(n);
+    d.V0.resize(n);
+    d.F.resize(9 * n);
+    d.C.assign(9 * n, 0.0);
+    d.d.assign(n, 0.0);
+    d.sigma_c.resize(n);
+    int rc = zr_recipe_generate(r, d.x.data(), d.v.data(), d.m.data(), d.V0.data(), d.F.data(), d.sigma_c.data());
+    if (rc) return set_err(err, rc, "recipe generation failed");
+    SceneDesc::Mat m;
+    m.E = r->E;
+    m.nu = r->nu;
+    if (r->kind == ZR_RECIPE_ELASTIC_BOX) {
+        m.model = ZR_COROTATED;
+        d.materials.push_back(m);
+        SceneDesc::Obj g;
+        g.origin[1] = r->ground_y;
+        g.normal[0] = 0;
+        g.normal[1] = 1;
+        g.normal[2] = 0;
+        g.type = ZR_STICKY;
+        d.objects.push_back(g);
+    }
+    else if (r->kind == ZR_RECIPE_ANISO_SLAB) {
+        m.model = ZR_NEOHOOKEAN_BORDEN;
+        m.damage = 1;
+        m.alpha = r->alpha;
+        m.l0 = r->l0;
+        m.eta = r->eta;
+        m.zeta = r->zeta;
+        m.residual = r->residual;
+        d.materials.push_back(m);
+        int64_t nc[3], lo[3];
+        recipe_cells(r, nc, lo);
+        const double x_lo = (double)lo[0] * r->dx, x_hi = (double)(lo[0] + nc[0]) * r->dx;
+        SceneDesc::Obj left, right;
+        left.origin[0] = x_lo + r->grip_cells * r->dx; // nodes with x <= x_lo + grip follow the left plate
+        left.normal[0] = 1;
+        left.normal[1] = 0;
+        left.vel[0] = -r->pull_speed;
+        left.type = ZR_STICKY;
+        right.origin[0] = x_hi - r->grip_cells * r->dx;
+        right.normal[0] = -1;
+        right.normal[1] = 0;
+        right.vel[0] = r->pull_speed;
+        right.type = ZR_STICKY;
+        d.objects.push_back(left);
+        d.objects.push_back(right);
+    }
+    else
+        return set_err(err, ZR_ERR_ARG, "unknown recipe kind");
+    return ZR_OK;
+}
+
+int zr_scene_from_recipe(zr_scene* s, const zr_scene_recipe* r)
+{
+    if (!s || !r) return ZR_ERR_ARG;
+    if (s->committed || s->desc.n) return set_err(s->err, ZR_ERR_STATE, "zr_scene_from_recipe needs an empty scene");
+    return desc_from_recipe(s->desc, r, s->err);
+}
+
+// ------------------------------------------------------------------------------------------- batch
+int zr_batch_create(int precision, zr_batch** out)
+{
+    if (!out || (precision != ZR_F32 && precision != ZR_F64)) return ZR_ERR_ARG;
+    zr_batch* b = new (std::nothrow) zr_batch();
+    if (!b) return ZR_ERR_ARG;
+    b->precision = precision;
+    *out = b;
+    return ZR_OK;
+}
+
+int zr_batch_destroy(zr_batch* b)
+{
+    delete b;
+    return ZR_OK;
+}
+
+int zr_batch_add_scene(zr_batch* b, zr_scene* s, int* slot)
+{
+    if (!b || !s) return ZR_ERR_ARG;
+    if (b->committed) return set_err(b->err, ZR_ERR_STATE, "scenes must be added before zr_batch_commit");
+    if (s->desc.n <= 0 || s->desc.materials.empty()) return set_err(b->err, ZR_ERR_ARG, "scene has no particles or no model");
+    b->descs.push_back(std::unique_ptr<SceneDesc>(new SceneDesc(s->desc)));
+    if (slot) *slot = (int)b->descs.size() - 1;
+    return ZR_OK;
+}
+
+int zr_batch_add_recipe(zr_batch* b, const zr_scene_recipe* r, int* slot)
+{
+    if (!b || !r) return ZR_ERR_ARG;
+    if (b->committed) return set_err(b->err, ZR_ERR_STATE, "scenes must be added before zr_batch_commit");
+    std::unique_ptr<SceneDesc> d(new SceneDesc());
+    int rc = desc_from_recipe(*d, r, b->err);
+    if (rc) return rc;
+    b->descs.push_back(std::move(d));
+    if (slot) *slot = (int)b->descs.size() - 1;
+    return ZR_OK;
+}
+
+int zr_batch_commit(zr_batch* b)
+{
+    if (!b) return ZR_ERR_ARG;
+    if (b->committed) return ZR_OK;
+    if (b->descs.empty()) return set_err(b->err, ZR_ERR_STATE, "empty batch");
+    b->eng = make_engine(b->precision);
+    std::vector<const SceneDesc*> v;
+    for (auto& d : b->descs) v.push_back(d.get());
+    int rc = b->eng->load(v);
+    if (rc) {
+        b->err = b->eng->last_error();
+        b->eng.reset();
+        return rc;
+    }
+    b->committed = true;
+    // host copies are no longer needed once the device holds the state
+    for (auto& d : b->descs) {
+        d->x.clear();
+        d->x.shrink_to_fit();
+        d->v.clear();
+        d->v.shrink_to_fit();
+        d->C.clear();
+        d->C.shrink_to_fit();
+        d->F.clear();
+        d->F.shrink_to_fit();
+        d->m.clear();
+        d->m.shrink_to_fit();
+        d->V0.clear();
+        d->V0.shrink_to_fit();
+        d->d.clear();
+        d->d.shrink_to_fit();
+        d->sigma_c.clear();
+        d->sigma_c.shrink_to_fit();
+        d->material.clear();
+        d->material.shrink_to_fit();
+    }
+    return ZR_OK;
+}
+
+#define NEED_BATCH(b)                 \
+    do {                              \
+        if (!b) return ZR_ERR_ARG;    \
+        int rc_ = zr_batch_commit(b); \
+        if (rc_) return rc_;          \
+    } while (0)
+
+int zr_batch_step(zr_batch* b, int nsteps, int* done)
+{
+    if (done) *done = 0;
+    NEED_BATCH(b);
+    StepReport rep;
+    int rc = b->eng->step(nsteps, &rep);
+    b->fallbacks += rep.fallback;
+    b->last_ms = rep.device_ms;
+    if (done) *done = rep.steps_done;
+    if (rc) b->err = b->eng->last_error();
+    return rc;
+}
+
+int zr_batch_get_field(zr_batch* b, int slot, int field, void* out, int dtype)
+{
+    NEED_BATCH(b);
+    if (!out || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = b->eng->get_field(slot, field, out, dtype == ZR_F32);
+    if (rc) b->err = b->eng->last_error();
+    return rc;
+}
+
+int zr_batch_reductions(zr_batch* b, int slot, double out[7])
+{
+    NEED_BATCH(b);
+    int rc = b->eng->reductions(slot, out);
+    if (rc) b->err = b->eng->last_error();
+    return rc;
+}
+
+int64_t zr_batch_count(zr_batch* b, int slot)
+{
+    if (!b || slot < 0 || slot >= (int)b->descs.size()) return -1;
+    return b->descs[slot]->n;
+}
+
+int zr_batch_set_timing(zr_batch* b, int on)
+{
+    NEED_BATCH(b);
+    b->eng->set_timing(on != 0);
+    b->eng->reset_timing();
+    return ZR_OK;
+}
+
+int zr_batch_get_timing(zr_batch* b, double out5[5], int64_t* steps)
+{
+    NEED_BATCH(b);
+    KernelTimes t = b->eng->timing();
+    if (out5) {
+        out5[0] = t.sort;
+        out5[1] = t.blocks;
+        out5[2] = t.p2g;
+        out5[3] = t.grid;
+        out5[4] = t.g2p;
+    }
+    if (steps) *steps = t.steps;
+    return ZR_OK;
+}
+
+int zr_batch_stats(zr_batch* b, int64_t* launches, int64_t* bytes, int64_t* fallbacks)
+{
+    NEED_BATCH(b);
+    if (launches) *launches = b->eng->kernel_launches_per_step();
+    if (bytes) *bytes = b->eng->device_bytes();
+    if (fallbacks) *fallbacks = b->fallbacks;
+    return ZR_OK;
+}
+
+const char* zr_batch_last_error(zr_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+} // extern "C"

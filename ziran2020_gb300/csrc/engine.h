@@ -1,0 +1,105 @@
+// Host-side interface of the GB300 explicit-MPM engine. Plain C++ (no CUDA types), so the C-ABI layer
+// and the serving loop can be compiled without nvcc.
+//
+// One Engine<T> owns the device state of a batch of independent scenes: a particle pool in HBM
+// (structure of arrays, two copies that alternate every substep), the sort buffers, the active-block
+// table and the sparse grid. A single scene is a batch of one.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace zr {
+
+// host description of one scene (all arrays in the caller's particle order, float64)
+struct SceneDesc {
+    double dx = 1.0 / 64;
+    double dt = 1e-4;
+    double gravity[3] = { 0, 0, 0 };
+    double apic_rpic_ratio = 1.0; // 1 = APIC, 0 = RPIC (MpmSimulationBase.cpp:39-40)
+    double cfl = 0.6;
+    double time = 0;
+    int32_t domain_cells = 0; // base nodes must stay in [0, domain_cells); 0 = the full 4096^3 SPGrid range
+    struct Mat {
+        int model = 0; // 0 fixed corotated, 1 Neo-Hookean (Borden)
+        double E = 1e4, nu = 0.3;
+        int damage = 0;
+        double alpha = 0, l0 = 0, eta = 1, zeta = 1, residual = 0;
+    };
+    struct Obj {
+        double origin[3] = { 0, 0, 0 }, normal[3] = { 0, 1, 0 }, vel[3] = { 0, 0, 0 };
+        double friction = 0;
+        int type = 1; // 1 STICKY, 2 SLIP, 3 SEPARATE
+    };
+    std::vector<Mat> materials;
+    std::vector<Obj> objects;
+    int64_t n = 0;
+    std::vector<double> x, v, C, F, m, V0, d, sigma_c; // C, F row-major 3x3 per particle
+    std::vector<uint8_t> material; // per particle material index (empty = all 0)
+};
+
+enum Field : int {
+    FIELD_X = 0, // 3
+    FIELD_V = 1, // 3
+    FIELD_C = 2, // 9
+    FIELD_F = 3, // 9
+    FIELD_D = 4, // 1 damage
+    FIELD_M = 5, // 1 mass
+    FIELD_V0 = 6, // 1 initial volume
+    FIELD_SIGMA_C = 7, // 1 critical stress
+};
+
+struct StepReport {
+    double device_ms = 0; // device time of the substeps, CUDA events on the engine's stream
+    uint32_t flags = 0;
+    int32_t steps_done = 0;
+    uint32_t n_groups = 0, n_blocks = 0, fallback = 0;
+};
+
+struct KernelTimes {
+    // milliseconds accumulated per phase while timing is enabled
+    double sort = 0, blocks = 0, p2g = 0, grid = 0, g2p = 0;
+    int64_t steps = 0;
+};
+
+class EngineBase {
+public:
+    virtual ~EngineBase() = default;
+    virtual int precision() const = 0;
+    // Build device state for the given scenes (replaces any previous batch).
+    virtual int load(const std::vector<const SceneDesc*>& scenes) = 0;
+    // Advance every scene of the batch by nsteps substeps. Returns 0 or a ZR_ERR code; rep gets details.
+    virtual int step(int nsteps, StepReport* rep) = 0;
+    // Copy one field of one scene, in the caller's particle order, into out (float64 or float32).
+    virtual int get_field(int scene, int field, void* out, int out_is_f32) = 0;
+    // Overwrite one field of one scene from host memory (caller's particle order).
+    virtual int set_field(int scene, int field, const void* in, int in_is_f32) = 0;
+    // Dynamic state in one call: x,v,C,F,d interleaved per particle as 25 values (d = 0 without damage).
+    virtual int get_state(int scene, void* out25, int out_is_f32) = 0;
+    virtual int set_state(int scene, const void* in25, int in_is_f32) = 0;
+    // FP64-accumulated reductions: mass, momentum(3), kinetic energy, max speed, grid mass
+    virtual int reductions(int scene, double* out7) = 0;
+    virtual int set_dt(int scene, double dt) = 0;
+    virtual double time(int scene) const = 0;
+    virtual int64_t count(int scene) const = 0;
+    virtual int n_scenes() const = 0;
+    // Binning products of the current substep input (for parity tests): sorted keys (scene bits
+    // removed), sorted original indices, group starts, active pages.
+    virtual int binning(int scene, std::vector<uint64_t>& keys, std::vector<int32_t>& order, std::vector<int32_t>& group_first,
+        std::vector<uint64_t>& pages) = 0;
+    virtual void set_timing(bool on) = 0;
+    virtual KernelTimes timing() const = 0;
+    virtual void reset_timing() = 0;
+    virtual int sync() = 0;
+    virtual void* stream() const = 0;
+    virtual int64_t device_bytes() const = 0;
+    virtual int use_graph(bool on) = 0;
+    virtual int kernel_launches_per_step() const = 0;
+    virtual std::string last_error() const = 0;
+};
+
+std::unique_ptr<EngineBase> make_engine_f32();
+std::unique_ptr<EngineBase> make_engine_f64();
+
+} // namespace zr

@@ -1,0 +1,768 @@
+// Host orchestration of Engine<T>: allocation, CUDA-graph capture of the substep, recovery after an
+// aborted substep, transfers and timing. Included after engine_impl.cuh by engine_f32.cu / engine_f64.cu.
+#pragma once
+#include "engine_impl.cuh"
+
+#define ZR_CUDA(call)                                                                                      \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess) {                                                                           \
+            err_ = std::string(#call) + ": " + cudaGetErrorString(e_);                                     \
+            return ZR_ERR_CUDA_;                                                                           \
+        }                                                                                                  \
+    } while (0)
+
+namespace zr {
+
+enum { ZR_OK_ = 0, ZR_ERR_ARG_ = 1, ZR_ERR_CUDA_ = 2, ZR_ERR_CFL_ = 3, ZR_ERR_NONFINITE_ = 4, ZR_ERR_OUT_OF_DOMAIN_ = 5, ZR_ERR_BUDGET_ = 6,
+    ZR_ERR_TIMEOUT_ = 7, ZR_ERR_CAPACITY_ = 8, ZR_ERR_STATE_ = 9 };
+
+inline int bitlen(uint64_t v)
+{
+    int b = 0;
+    while (v) {
+        b++;
+        v >>= 1;
+    }
+    return b;
+}
+
+template <class T>
+class Engine final : public EngineBase {
+    using L = typename LayoutOf<T>::type;
+    static constexpr int NT_P2G = 256;
+    static constexpr int NT_G2P = 256;
+    static constexpr int GRAPH_K = 8; // substeps per multi-step graph (even: returns to the same buffer)
+
+public:
+    Engine() { init_device(); }
+    ~Engine() override { release(); }
+    int precision() const override { return (int)sizeof(T); }
+    std::string last_error() const override { return err_; }
+    void* stream() const override { return (void*)stream_; }
+    int n_scenes() const override { return (int)h_scenes_.size(); }
+    int64_t count(int s) const override { return (s >= 0 && s < n_scenes()) ? h_scenes_[s].count : -1; }
+    int64_t device_bytes() const override { return dev_bytes_; }
+
+    int load(const std::vector<const SceneDesc*>& scenes) override
+    {
+        if (init_err_) return init_err_;
+        release_batch();
+        if (scenes.empty()) return arg("empty batch");
+        h_scenes_.clear();
+        int64_t N = 0, max_n = 1;
+        int max_domain = 0;
+        for (auto* sd : scenes) {
+            if (!sd || sd->n <= 0) return arg("scene without particles");
+            if (sd->n >= (int64_t)(1u << L::index_bits)) return arg("too many particles in one scene for the SPGrid key (limit 2^" + std::to_string(L::index_bits) + ")");
+            if ((int)sd->materials.size() > MAX_MATERIALS || sd->materials.empty()) return arg("a scene needs 1.." + std::to_string(MAX_MATERIALS) + " materials");
+            if ((int)sd->objects.size() > MAX_OBJECTS) return arg("at most " + std::to_string(MAX_OBJECTS) + " collision objects per scene");
+            if (!(sd->dx > 0) || !(sd->dt > 0)) return arg("dx and dt must be positive");
+            int dc = sd->domain_cells > 0 ? sd->domain_cells : 4096 - 8;
+            if (dc > 4096 - 8 || dc < 8) return arg("domain_cells must be in [8, 4088]");
+            SceneParams<T> sp;
+            std::memset(&sp, 0, sizeof sp);
+            sp.dx = (T)sd->dx;
+            sp.inv_dx = (T)1 / sp.dx; // BSplineWeights one_over_dx(1 / dx) (MpmGrid.h:69)
+            sp.dt = (T)sd->dt;
+            T dx2 = sp.dx * sp.dx;
+            sp.D_inv = (T)4 / dx2;
+            for (int c = 0; c < 3; c++) sp.gravity[c] = (T)sd->gravity[c];
+            T r = (T)sd->apic_rpic_ratio;
+            sp.apic_a = (r + 1) * (T)0.5;
+            sp.apic_b = (r - 1) * (T)0.5;
+            sp.cfl = (T)sd->cfl;
+            sp.time = sd->time;
+            sp.first = N;
+            sp.count = sd->n;
+            sp.domain_cells = dc;
+            sp.n_objects = (int)sd->objects.size();
+            sp.n_materials = (int)sd->materials.size();
+            sp.damage = 0;
+            for (int k = 0; k < sp.n_materials; k++) {
+                const auto& m = sd->materials[k];
+                Material<T>& mt = sp.materials[k];
+                T E = (T)m.E, nu = (T)m.nu;
+                mt.model = m.model;
+                mt.damage = m.damage;
+                mt.lambda = E * nu / (((T)1 + nu) * ((T)1 - (T)2 * nu)); // CorotatedElasticity.cpp:16-21
+                mt.mu = E / ((T)2 * ((T)1 + nu));
+                mt.kappa = (T).666666 * mt.mu + mt.lambda; // NeoHookeanBorden.cpp:20
+                mt.alpha = (T)m.alpha;
+                mt.l0 = (T)m.l0;
+                mt.eta = (T)m.eta;
+                mt.zeta = (T)m.zeta;
+                mt.residual = (T)m.residual;
+                if (m.damage) sp.damage = 1;
+            }
+            for (int k = 0; k < sp.n_objects; k++) {
+                const auto& o = sd->objects[k];
+                double nn = std::sqrt(o.normal[0] * o.normal[0] + o.normal[1] * o.normal[1] + o.normal[2] * o.normal[2]);
+                if (!(nn > 0)) return arg("half-space normal must be non-zero");
+                if (o.type < 1 || o.type > 3) return arg("collision type must be STICKY(1), SLIP(2) or SEPARATE(3)");
+                HalfSpaceObj<T>& h = sp.objects[k];
+                for (int c = 0; c < 3; c++) {
+                    h.origin[c] = (T)o.origin[c];
+                    h.normal[c] = (T)(o.normal[c] / nn); // AnalyticLevelSet.cpp:318-323 normalises
+                    h.vel[c] = (T)o.vel[c];
+                }
+                h.friction = (T)o.friction;
+                h.type = o.type;
+            }
+            h_scenes_.push_back(sp);
+            N += sd->n;
+            max_n = std::max<int64_t>(max_n, sd->n);
+            max_domain = std::max(max_domain, dc);
+        }
+        if (N >= (int64_t)0xffffffffLL) return arg("batch too large");
+        N_ = (uint32_t)N;
+        // key layout
+        int cb = bitlen((uint64_t)(max_domain + 2 * std::max(L::sx, std::max(L::sy, L::sz)) - 1));
+        uint32_t maxc = (1u << cb) - 1;
+        kl_.ib = std::max(1, bitlen((uint64_t)(max_n - 1)));
+        kl_.cp = bitlen(L::offset(maxc, maxc, maxc)) - L::data_bits;
+        kl_.sb = bitlen((uint64_t)(h_scenes_.size() - 1));
+        kl_.block_bits = L::block_bits;
+        if (kl_.total() > 64) return arg("batch too large for 64-bit keys: reduce the number of scenes or their domain");
+        // device buffers
+        const int64_t n = N_;
+        if (alloc((void**)&pool_[0], sizeof(T) * P_NF * n) || alloc((void**)&pool_[1], sizeof(T) * P_NF * n) || alloc((void**)&pid_[0], 4 * n)
+            || alloc((void**)&pid_[1], 4 * n) || alloc((void**)&keys_in_, 8 * n) || alloc((void**)&keys_sorted_, 8 * n) || alloc((void**)&iota_, 4 * n)
+            || alloc((void**)&vals_sorted_, 4 * n) || alloc((void**)&g_start_, 4 * n) || alloc((void**)&d_scenes_, sizeof(SceneParams<T>) * h_scenes_.size())
+            || alloc((void**)&grid_mass_, 8 * h_scenes_.size()) || alloc((void**)&st_, sizeof(DevStatus)))
+            return ZR_ERR_CUDA_;
+        ZR_CUDA(cudaMemsetAsync(pool_[0], 0, sizeof(T) * P_NF * n, stream_));
+        ZR_CUDA(cudaMemsetAsync(pool_[1], 0, sizeof(T) * P_NF * n, stream_));
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * h_scenes_.size(), stream_));
+        ZR_CUDA(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), sizeof(SceneParams<T>) * h_scenes_.size(), cudaMemcpyHostToDevice, stream_));
+        k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, N_);
+        // CUB scratch
+        size_t sb = 0, se = 0;
+        ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)n, 0, kl_.total(), stream_));
+        GroupHead gh{ keys_sorted_, kl_ };
+        ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)n, gh, stream_));
+        sort_bytes_ = sb;
+        sel_bytes_ = se;
+        if (alloc(&sort_tmp_, sort_bytes_) || alloc(&sel_tmp_, sel_bytes_)) return ZR_ERR_CUDA_;
+        // particles
+        cur_ = 0;
+        std::vector<T> buf;
+        uint8_t* d_mat = nullptr;
+        if (alloc((void**)&d_mat, (size_t)max_n)) return ZR_ERR_CUDA_;
+        for (size_t s = 0; s < scenes.size(); s++) {
+            const SceneDesc& sd = *scenes[s];
+            const int64_t first = h_scenes_[s].first, cnt = sd.n;
+            auto put = [&](int f0, int nc, const std::vector<double>& src, double dflt_diag, double dflt) -> int {
+                buf.resize(cnt);
+                for (int c = 0; c < nc; c++) {
+                    for (int64_t i = 0; i < cnt; i++) {
+                        if (!src.empty())
+                            buf[i] = (T)src[(size_t)i * nc + c];
+                        else
+                            buf[i] = (T)((nc == 9 && (c % 4) == 0) ? dflt_diag : dflt);
+                    }
+                    ZR_CUDA(cudaMemcpy(pool_[0] + (size_t)(f0 + c) * n + first, buf.data(), sizeof(T) * cnt, cudaMemcpyHostToDevice));
+                }
+                return 0;
+            };
+            if ((int64_t)sd.x.size() != 3 * cnt || (int64_t)sd.m.size() != cnt || (int64_t)sd.V0.size() != cnt) return arg("x, m, V0 are required");
+            if (!sd.v.empty() && (int64_t)sd.v.size() != 3 * cnt) return arg("v must have 3n values");
+            if (!sd.F.empty() && (int64_t)sd.F.size() != 9 * cnt) return arg("F must have 9n values");
+            if (!sd.C.empty() && (int64_t)sd.C.size() != 9 * cnt) return arg("C must have 9n values");
+            if (!sd.d.empty() && (int64_t)sd.d.size() != cnt) return arg("d must have n values");
+            if (!sd.sigma_c.empty() && (int64_t)sd.sigma_c.size() != cnt) return arg("sigma_c must have n values");
+            int rc;
+            if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
+                || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1)))
+                return rc;
+            const uint8_t* mp = nullptr;
+            if (!sd.material.empty()) {
+                if ((int64_t)sd.material.size() != cnt) return arg("material must have n values");
+                for (auto mm : sd.material)
+                    if ((int)mm >= (int)sd.materials.size()) return arg("material index out of range");
+                ZR_CUDA(cudaMemcpy(d_mat, sd.material.data(), cnt, cudaMemcpyHostToDevice));
+                mp = d_mat;
+            }
+            k_iota_pid<T><<<nsm_ * 4, 256, 0, stream_>>>(pid_[0], mp, first, cnt);
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+        }
+        cudaFree(d_mat);
+        dev_bytes_ -= (int64_t)max_n;
+        // first binning pass sizes the grid: groups G0 -> capacity for 4 G0 active blocks (at least 4096)
+        k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(0), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
+        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)n, 0, kl_.total(), stream_));
+        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)n, gh, stream_));
+        DevStatus hs;
+        ZR_CUDA(cudaMemcpyAsync(&hs, st_, sizeof hs, cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        if (hs.flags & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle lies outside its scene's domain");
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        int rc = alloc_grid(std::max<uint32_t>(4096, 4 * hs.n_groups + 512));
+        if (rc) return rc;
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int step(int nsteps, StepReport* rep) override
+    {
+        if (init_err_) return init_err_;
+        if (!N_) return fail(ZR_ERR_STATE_, "no scenes loaded");
+        if (nsteps < 0) return arg("nsteps must be >= 0");
+        int done = 0;
+        StepReport r;
+        int grow_rounds = 0;
+        while (done < nsteps) {
+            ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+            const int cur0 = cur_;
+            int todo = nsteps - done;
+            if (!timing_ && graphs_on_) {
+                int rcg = prepare_graphs(todo);
+                if (rcg) return rcg;
+            }
+            ZR_CUDA(cudaEventRecord(t0_, stream_));
+            int rc = launch_steps(todo);
+            if (rc) return rc;
+            ZR_CUDA(cudaEventRecord(t1_, stream_));
+            ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, t0_, t1_);
+            r.device_ms += ms;
+            if (timing_) collect_timing(todo);
+            r.fallback += hst_->fallback;
+            r.n_groups = hst_->max_groups_seen;
+            r.n_blocks = hst_->max_blocks_seen;
+            r.flags |= hst_->flags;
+            if (!(hst_->flags & FLAG_ABORT)) {
+                cur_ = (cur0 + todo) & 1;
+                done += todo;
+                break;
+            }
+            const int k = hst_->abort_step;
+            done += k;
+            cur_ = (cur0 + k) & 1;
+            // the aborted substep may have left partial grid sums, hash entries or next keys behind
+            ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
+            ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+            ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+            k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+            const uint32_t f = hst_->flags;
+            if ((f & FLAG_CAPACITY) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT)) && grow_rounds < 6) {
+                grow_rounds++;
+                int rc2 = alloc_grid(b_cap_ * 2);
+                if (rc2) return rc2;
+                continue; // retry the aborted substep with a larger grid
+            }
+            r.steps_done = done;
+            if (rep) *rep = r;
+            if (f & FLAG_NONFINITE) return fail(ZR_ERR_NONFINITE_, "non-finite particle state at substep " + std::to_string(done));
+            if (f & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle left its scene's domain at substep " + std::to_string(done));
+            if (f & FLAG_CFL) return fail(ZR_ERR_CFL_, "a particle moved more than one cell at substep " + std::to_string(done) + " (reduce dt)");
+            if (f & FLAG_TIMEOUT) return fail(ZR_ERR_TIMEOUT_, "bounded wait expired at substep " + std::to_string(done));
+            return fail(ZR_ERR_CAPACITY_, "active-block capacity exhausted");
+        }
+        r.steps_done = done;
+        if (rep) *rep = r;
+        return 0;
+    }
+
+    int get_field(int s, int field, void* out, int f32) override
+    {
+        int f0, nc;
+        if (!field_range(field, f0, nc)) return arg("unknown field");
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const int64_t n = h_scenes_[s].count;
+        int rc = ensure_stage((size_t)n * nc * (f32 ? 4 : 8));
+        if (rc) return rc;
+        if (f32)
+            k_export<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (float*)stage_, nc, 0);
+        else
+            k_export<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (double*)stage_, nc, 0);
+        ZR_CUDA(cudaMemcpyAsync(out, stage_, (size_t)n * nc * (f32 ? 4 : 8), cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int set_field(int s, int field, const void* in, int f32) override
+    {
+        int f0, nc;
+        if (!field_range(field, f0, nc)) return arg("unknown field");
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const int64_t n = h_scenes_[s].count;
+        int rc = ensure_stage((size_t)n * nc * (f32 ? 4 : 8));
+        if (rc) return rc;
+        ZR_CUDA(cudaMemcpyAsync(stage_, in, (size_t)n * nc * (f32 ? 4 : 8), cudaMemcpyHostToDevice, stream_));
+        if (f32)
+            k_import<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const float*)stage_, nc, 0);
+        else
+            k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const double*)stage_, nc, 0);
+        if (field == FIELD_X) return rekey();
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int get_state(int s, void* out, int f32) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const int64_t n = h_scenes_[s].count;
+        const size_t es = f32 ? 4 : 8;
+        int rc = ensure_stage((size_t)n * 25 * es);
+        if (rc) return rc;
+        const int f0s[5] = { P_X, P_V, P_C, P_F, P_D }, ncs[5] = { 3, 3, 9, 9, 1 }, offs[5] = { 0, 3, 6, 15, 24 };
+        for (int q = 0; q < 5; q++) {
+            if (f32)
+                k_export<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (float*)stage_, 25, offs[q]);
+            else
+                k_export<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (double*)stage_, 25, offs[q]);
+        }
+        ZR_CUDA(cudaMemcpyAsync(out, stage_, (size_t)n * 25 * es, cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int set_state(int s, const void* in, int f32) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const int64_t n = h_scenes_[s].count;
+        const size_t es = f32 ? 4 : 8;
+        int rc = ensure_stage((size_t)n * 25 * es);
+        if (rc) return rc;
+        ZR_CUDA(cudaMemcpyAsync(stage_, in, (size_t)n * 25 * es, cudaMemcpyHostToDevice, stream_));
+        const int f0s[5] = { P_X, P_V, P_C, P_F, P_D }, ncs[5] = { 3, 3, 9, 9, 1 }, offs[5] = { 0, 3, 6, 15, 24 };
+        for (int q = 0; q < 5; q++) {
+            if (f32)
+                k_import<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (const float*)stage_, 25, offs[q]);
+            else
+                k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (const double*)stage_, 25, offs[q]);
+        }
+        return rekey();
+    }
+
+    int reductions(int s, double* out7) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        int rc = ensure_stage(64);
+        if (rc) return rc;
+        ZR_CUDA(cudaMemsetAsync(stage_, 0, 64, stream_));
+        k_reduce<T><<<nsm_ * 2, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, h_scenes_[s].count, (double*)stage_);
+        ZR_CUDA(cudaMemcpyAsync(out7, stage_, 6 * 8, cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaMemcpyAsync(out7 + 6, grid_mass_ + s, 8, cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int set_dt(int s, double dt) override
+    {
+        if (s < 0 || s >= n_scenes() || !(dt > 0)) return arg("bad scene or dt");
+        h_scenes_[s].dt = (T)dt;
+        ZR_CUDA(cudaMemcpyAsync((char*)(d_scenes_ + s) + offsetof(SceneParams<T>, dt), &h_scenes_[s].dt, sizeof(T), cudaMemcpyHostToDevice, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    double time(int s) const override
+    {
+        if (s < 0 || s >= n_scenes()) return NAN;
+        double t = NAN;
+        if (cudaMemcpy(&t, (const char*)(d_scenes_ + s) + offsetof(SceneParams<T>, time), 8, cudaMemcpyDeviceToHost) != cudaSuccess) return NAN;
+        return t;
+    }
+
+    int binning(int s, std::vector<uint64_t>& keys, std::vector<int32_t>& order, std::vector<int32_t>& group_first, std::vector<uint64_t>& pages) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const int64_t n = N_;
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        StepArgs<T> a = args(cur_);
+        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
+        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
+        k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+        ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        const uint32_t G = hst_->n_groups, B = std::min(hst_->n_blocks, b_cap_);
+        std::vector<uint64_t> sk(n), bk(B);
+        std::vector<uint32_t> gs(G);
+        ZR_CUDA(cudaMemcpy(sk.data(), keys_sorted_, 8 * n, cudaMemcpyDeviceToHost));
+        ZR_CUDA(cudaMemcpy(gs.data(), g_start_, 4 * (size_t)G, cudaMemcpyDeviceToHost));
+        ZR_CUDA(cudaMemcpy(bk.data(), b_key_, 8 * (size_t)B, cudaMemcpyDeviceToHost));
+        // restore a clean grid for the next substep
+        ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        const int64_t first = h_scenes_[s].first, cnt = h_scenes_[s].count;
+        keys.resize(cnt);
+        order.resize(cnt);
+        const uint64_t cpmask = (1ULL << kl_.cp) - 1;
+        for (int64_t i = 0; i < cnt; i++) {
+            uint64_t k = sk[first + i];
+            uint32_t o = kl_.orig(k);
+            keys[i] = (((k >> kl_.ib) & cpmask) << L::index_bits) | o; // the reference's key layout
+            order[i] = (int32_t)o;
+        }
+        group_first.clear();
+        for (uint32_t g = 0; g < G; g++)
+            if ((int64_t)gs[g] >= first && (int64_t)gs[g] < first + cnt) group_first.push_back((int32_t)(gs[g] - first));
+        pages.clear();
+        for (uint32_t b = 0; b < B; b++)
+            if ((bk[b] >> 40) == (uint64_t)s) pages.push_back(bk[b] & ((1ULL << 40) - 1));
+        std::sort(pages.begin(), pages.end());
+        if (hst_->flags & FLAG_ABORT) return fail(ZR_ERR_CAPACITY_, "binning overflowed the active-block table");
+        return 0;
+    }
+
+    void set_timing(bool on) override { timing_ = on; }
+    KernelTimes timing() const override { return kt_; }
+    void reset_timing() override { kt_ = KernelTimes(); }
+    int sync() override
+    {
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+    int use_graph(bool on) override
+    {
+        graphs_on_ = on;
+        return 0;
+    }
+    int kernel_launches_per_step() const override { return launches_per_step_; }
+
+private:
+    int dev_ = 0, nsm_ = 0;
+    cudaStream_t stream_ = nullptr;
+    int init_err_ = 0;
+    std::string err_;
+    std::vector<SceneParams<T>> h_scenes_;
+    SceneParams<T>* d_scenes_ = nullptr;
+    uint32_t N_ = 0;
+    KeyLayout kl_{};
+    T* pool_[2] = { nullptr, nullptr };
+    uint32_t* pid_[2] = { nullptr, nullptr };
+    int cur_ = 0;
+    uint64_t *keys_in_ = nullptr, *keys_sorted_ = nullptr;
+    uint32_t *iota_ = nullptr, *vals_sorted_ = nullptr, *g_start_ = nullptr;
+    int32_t* g_nbr_ = nullptr;
+    uint64_t* b_key_ = nullptr;
+    T *acc_ = nullptr, *vel_ = nullptr;
+    uint64_t* h_keys_ = nullptr;
+    int32_t* h_vals_ = nullptr;
+    uint32_t h_mask_ = 0, b_cap_ = 0;
+    double* grid_mass_ = nullptr;
+    DevStatus* st_ = nullptr;
+    DevStatus* hst_ = nullptr;
+    void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
+    size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
+    int occ_p2g_ = 1, occ_g2p_ = 1;
+    bool graphs_on_ = true, timing_ = false;
+    cudaGraphExec_t g1_[2] = { nullptr, nullptr }, gk_[2] = { nullptr, nullptr };
+    int launches_per_step_ = 0;
+    std::vector<cudaEvent_t> ev_;
+    cudaEvent_t t0_ = nullptr, t1_ = nullptr;
+    KernelTimes kt_;
+    int64_t dev_bytes_ = 0;
+
+    Pool<T> pool(int which) const { return Pool<T>{ pool_[which], pid_[which], (int64_t)N_ }; }
+
+    int arg(const std::string& m) { return fail(ZR_ERR_ARG_, m); }
+    int fail(int code, const std::string& m)
+    {
+        err_ = m;
+        return code;
+    }
+
+    void init_device()
+    {
+        if (cudaGetDevice(&dev_) != cudaSuccess || cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_) != cudaSuccess) {
+            init_err_ = fail(ZR_ERR_CUDA_, "no CUDA device");
+            return;
+        }
+        if (cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking) != cudaSuccess || cudaMallocHost((void**)&hst_, sizeof(DevStatus)) != cudaSuccess
+            || cudaEventCreate(&t0_) != cudaSuccess || cudaEventCreate(&t1_) != cudaSuccess) {
+            init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
+            return;
+        }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p2g_, k_p2g<T, NT_P2G>, NT_P2G, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_, k_g2p<T, NT_G2P>, NT_G2P, 0);
+        occ_p2g_ = std::max(1, occ_p2g_);
+        occ_g2p_ = std::max(1, occ_g2p_);
+    }
+
+    int alloc(void** p, size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            err_ = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+            return ZR_ERR_CUDA_;
+        }
+        dev_bytes_ += (int64_t)bytes;
+        return 0;
+    }
+    void dfree(void*& p)
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+
+    int alloc_grid(uint32_t cap)
+    {
+        drop_graphs();
+        void* p;
+        p = g_nbr_;
+        dfree(p);
+        p = b_key_;
+        dfree(p);
+        p = acc_;
+        dfree(p);
+        p = vel_;
+        dfree(p);
+        p = h_keys_;
+        dfree(p);
+        p = h_vals_;
+        dfree(p);
+        g_nbr_ = nullptr;
+        b_key_ = nullptr;
+        acc_ = vel_ = nullptr;
+        h_keys_ = nullptr;
+        h_vals_ = nullptr;
+        b_cap_ = cap;
+        uint32_t hs = 1;
+        while (hs < 4 * cap) hs <<= 1;
+        h_mask_ = hs - 1;
+        if (alloc((void**)&g_nbr_, 32 * (size_t)cap) || alloc((void**)&b_key_, 8 * (size_t)cap) || alloc((void**)&acc_, sizeof(T) * (size_t)cap * NACC * L::nodes)
+            || alloc((void**)&vel_, sizeof(T) * (size_t)cap * NVEL * L::nodes) || alloc((void**)&h_keys_, 8 * (size_t)hs) || alloc((void**)&h_vals_, 4 * (size_t)hs))
+            return ZR_ERR_CUDA_;
+        ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)cap * NACC * L::nodes, stream_));
+        ZR_CUDA(cudaMemsetAsync(vel_, 0, sizeof(T) * (size_t)cap * NVEL * L::nodes, stream_));
+        ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)hs, stream_));
+        return 0;
+    }
+
+    int ensure_stage(size_t bytes)
+    {
+        if (bytes <= stage_bytes_) return 0;
+        dfree(stage_);
+        if (alloc(&stage_, bytes)) return ZR_ERR_CUDA_;
+        stage_bytes_ = bytes;
+        return 0;
+    }
+
+    int rekey()
+    {
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
+        ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        if (hst_->flags & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle lies outside its scene's domain");
+        return 0;
+    }
+
+    static bool field_range(int field, int& f0, int& nc)
+    {
+        switch (field) {
+        case FIELD_X: f0 = P_X; nc = 3; return true;
+        case FIELD_V: f0 = P_V; nc = 3; return true;
+        case FIELD_C: f0 = P_C; nc = 9; return true;
+        case FIELD_F: f0 = P_F; nc = 9; return true;
+        case FIELD_D: f0 = P_D; nc = 1; return true;
+        case FIELD_M: f0 = P_M; nc = 1; return true;
+        case FIELD_V0: f0 = P_V0; nc = 1; return true;
+        case FIELD_SIGMA_C: f0 = P_SC; nc = 1; return true;
+        }
+        return false;
+    }
+
+    StepArgs<T> args(int parity) const
+    {
+        StepArgs<T> a;
+        a.keys_sorted = keys_sorted_;
+        a.vals_sorted = vals_sorted_;
+        a.keys_next = keys_in_;
+        a.pin = pool(parity);
+        a.pout = pool(parity ^ 1);
+        a.g_start = g_start_;
+        a.g_nbr = g_nbr_;
+        a.b_key = b_key_;
+        a.acc = acc_;
+        a.vel = vel_;
+        a.h_keys = h_keys_;
+        a.h_vals = h_vals_;
+        a.h_mask = h_mask_;
+        a.scenes = d_scenes_;
+        a.grid_mass = grid_mass_;
+        a.st = st_;
+        a.n_total = N_;
+        a.b_cap = b_cap_;
+        a.kl = kl_;
+        return a;
+    }
+
+    // Enqueue one substep reading buffer `parity`. With ev != nullptr, events are recorded between the
+    // phases (sort+groups | activate | p2g | grid | g2p+end).
+    int enqueue_step(int parity, cudaEvent_t* ev)
+    {
+        StepArgs<T> a = args(parity);
+        const int64_t n = N_;
+        if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
+        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
+        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
+        if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
+        k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
+        k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+        if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
+        k_p2g<T, NT_P2G><<<nsm_ * occ_p2g_, NT_P2G, 0, stream_>>>(a);
+        if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
+        k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
+        if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));
+        k_g2p<T, NT_G2P><<<nsm_ * occ_g2p_, NT_G2P, 0, stream_>>>(a);
+        k_step_end<T><<<1, 256, 0, stream_>>>(d_scenes_, n_scenes(), st_);
+        if (ev) ZR_CUDA(cudaEventRecord(ev[5], stream_));
+        ZR_CUDA(cudaGetLastError());
+        return 0;
+    }
+
+    int build_graph(int parity, int nsub, cudaGraphExec_t* out)
+    {
+        cudaGraph_t g;
+        ZR_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        int rc = 0;
+        for (int s = 0; s < nsub && !rc; s++) rc = enqueue_step(parity ^ (s & 1), nullptr);
+        cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(ZR_ERR_CUDA_, std::string("graph capture: ") + cudaGetErrorString(e));
+        if (nsub == 1) {
+            size_t nn = 0;
+            cudaGraphGetNodes(g, nullptr, &nn);
+            launches_per_step_ = 0;
+            std::vector<cudaGraphNode_t> nodes(nn);
+            cudaGraphGetNodes(g, nodes.data(), &nn);
+            for (auto& nd : nodes) {
+                cudaGraphNodeType t;
+                cudaGraphNodeGetType(nd, &t);
+                if (t == cudaGraphNodeTypeKernel) launches_per_step_++;
+            }
+        }
+        e = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(ZR_ERR_CUDA_, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        return 0;
+    }
+
+    void drop_graphs()
+    {
+        for (int p = 0; p < 2; p++) {
+            if (g1_[p]) cudaGraphExecDestroy(g1_[p]);
+            if (gk_[p]) cudaGraphExecDestroy(gk_[p]);
+            g1_[p] = gk_[p] = nullptr;
+        }
+    }
+
+    int launch_steps(int nsteps)
+    {
+        if (timing_) {
+            if ((int)ev_.size() < 6 * nsteps) {
+                size_t old = ev_.size();
+                ev_.resize(6 * (size_t)nsteps);
+                for (size_t i = old; i < ev_.size(); i++) ZR_CUDA(cudaEventCreate(&ev_[i]));
+            }
+            for (int s = 0; s < nsteps; s++) {
+                int rc = enqueue_step((cur_ + s) & 1, &ev_[6 * (size_t)s]);
+                if (rc) return rc;
+            }
+            return 0;
+        }
+        if (!graphs_on_) {
+            for (int s = 0; s < nsteps; s++) {
+                int rc = enqueue_step((cur_ + s) & 1, nullptr);
+                if (rc) return rc;
+            }
+            return 0;
+        }
+        int rc = prepare_graphs(nsteps);
+        if (rc) return rc;
+        int par = cur_;
+        int s = 0;
+        if (nsteps >= GRAPH_K)
+            for (; s + GRAPH_K <= nsteps; s += GRAPH_K) ZR_CUDA(cudaGraphLaunch(gk_[par], stream_)); // GRAPH_K even: parity unchanged
+        for (; s < nsteps; s++) {
+            ZR_CUDA(cudaGraphLaunch(g1_[par], stream_));
+            par ^= 1;
+        }
+        return 0;
+    }
+
+    // capture the 1-substep graphs (both buffer parities) and, for long runs, the GRAPH_K-substep graphs
+    int prepare_graphs(int nsteps)
+    {
+        for (int p = 0; p < 2; p++)
+            if (!g1_[p]) {
+                int rc = build_graph(p, 1, &g1_[p]);
+                if (rc) return rc;
+            }
+        if (nsteps >= GRAPH_K)
+            for (int p = 0; p < 2; p++)
+                if (!gk_[p]) {
+                    int rc = build_graph(p, GRAPH_K, &gk_[p]);
+                    if (rc) return rc;
+                }
+        return 0;
+    }
+
+    void collect_timing(int nsteps)
+    {
+        for (int s = 0; s < nsteps; s++) {
+            float t[5];
+            for (int q = 0; q < 5; q++) cudaEventElapsedTime(&t[q], ev_[6 * s + q], ev_[6 * s + q + 1]);
+            kt_.sort += t[0];
+            kt_.blocks += t[1];
+            kt_.p2g += t[2];
+            kt_.grid += t[3];
+            kt_.g2p += t[4];
+            kt_.steps++;
+        }
+    }
+
+    void release_batch()
+    {
+        drop_graphs();
+        void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
+            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_ };
+        for (void* p : ps)
+            if (p) cudaFree(p);
+        pool_[0] = pool_[1] = nullptr;
+        pid_[0] = pid_[1] = nullptr;
+        keys_in_ = keys_sorted_ = nullptr;
+        iota_ = vals_sorted_ = g_start_ = nullptr;
+        g_nbr_ = nullptr;
+        b_key_ = nullptr;
+        acc_ = vel_ = nullptr;
+        h_keys_ = nullptr;
+        h_vals_ = nullptr;
+        d_scenes_ = nullptr;
+        grid_mass_ = nullptr;
+        st_ = nullptr;
+        sort_tmp_ = sel_tmp_ = stage_ = nullptr;
+        stage_bytes_ = 0;
+        N_ = 0;
+        b_cap_ = 0;
+        dev_bytes_ = 0;
+        h_scenes_.clear();
+    }
+
+    void release()
+    {
+        release_batch();
+        for (auto& e : ev_) cudaEventDestroy(e);
+        ev_.clear();
+        if (t0_) cudaEventDestroy(t0_);
+        if (t1_) cudaEventDestroy(t1_);
+        t0_ = t1_ = nullptr;
+        if (hst_) cudaFreeHost(hst_);
+        hst_ = nullptr;
+        if (stream_) cudaStreamDestroy(stream_);
+        stream_ = nullptr;
+    }
+};
+
+} // namespace zr

@@ -1,0 +1,706 @@
+// Kernels and host orchestration of the GB300 explicit-MPM substep (templated on the scalar type).
+// Included by engine_f32.cu and engine_f64.cu, which instantiate one precision each.
+//
+// One substep (MpmSimulationBase::advanceOneTimeStep, MpmSimulationBase.cpp:262-357, with the
+// AnisoFractureSimulation particlesToGrid override, AnisoFractureSimulation.h:129-141):
+//   1. sort      CUB radix sort of the 64-bit particle keys written by the previous G2P (or k_keys)
+//   2. groups    CUB select of the first sorted index of every (scene, SPGrid page)
+//   3. activate  every group inserts its page and the 7 pages at +1 block into a hash table; new
+//                entries get a grid slot (MpmGrid::pollute, MpmGrid.h:153-193)
+//   4. p2g       one CTA per group: stress V0*tau(F, g(d)) + APIC scatter of m, m v + m C (x_i - x_p),
+//                -V0 tau grad w and the phase-field pair (d w, w) into a shared node tile, then
+//                vector atomics into the 8 neighbouring grid blocks (MpmSimulationBase.cpp:669-855,
+//                FBasedMpmForceHelper.cpp:43-63, AnisoFractureSimulation.h:161-176)
+//   5. grid      v = m v / m, v += g dt + f dt / m, half-space BCs, phase field normalised; clears the
+//                accumulators and the hash table for the next substep (MpmSimulationBase.cpp:655-666,
+//                1179-1228, AnisoFractureSimulation.h:177-179)
+//   6. g2p       one CTA per group: gather v, C (APIC/RPIC blend), grad v and the damage Laplacian,
+//                damage update with the old F, F <- (I + dt grad v) F, x += dt v, CFL / finiteness /
+//                domain checks, next key; writes the particle to its sorted slot of the other buffer
+//                (MpmSimulationBase.cpp:1269-1515, FBasedMpmForceHelper.cpp:95-108,
+//                AnisoFractureSimulation.h:182-283)
+//   7. end       time += dt per scene, substep counter
+#pragma once
+#include "common.cuh"
+#include "engine.h"
+#include "physics.cuh"
+
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace zr {
+
+constexpr int NACC = 9; // m, m v (3), f (3), d w, w
+constexpr int NVEL = 4; // v_new (3), normalised phase field
+constexpr uint64_t HASH_EMPTY = ~0ULL;
+constexpr int HASH_PROBES = 64;
+
+// particle pool: field k of storage slot i at f[k * stride + i]
+enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_NF = 28 };
+
+template <class T>
+struct Pool {
+    T* f;
+    uint32_t* pid; // original index (low index_bits) | material << index_bits
+    int64_t stride;
+};
+
+struct KeyLayout {
+    int ib; // bits of the original particle index
+    int cp; // bits of (offset >> data_bits): page and in-block cell
+    int sb; // bits of the scene slot
+    int block_bits;
+    __host__ __device__ int total() const { return sb + cp + ib; }
+    __host__ __device__ uint32_t scene(uint64_t k) const { return (uint32_t)(k >> (cp + ib)); }
+    __host__ __device__ uint64_t page(uint64_t k) const { return (k >> (ib + block_bits)) & ((1ULL << (cp - block_bits)) - 1); }
+    __host__ __device__ uint64_t group(uint64_t k) const { return k >> (ib + block_bits); }
+    __host__ __device__ uint32_t orig(uint64_t k) const { return (uint32_t)(k & ((1ULL << ib) - 1)); }
+};
+
+template <class T>
+struct StepArgs {
+    const uint64_t* keys_sorted;
+    const uint32_t* vals_sorted;
+    uint64_t* keys_next;
+    Pool<T> pin, pout;
+    const uint32_t* g_start;
+    int32_t* g_nbr;
+    uint64_t* b_key;
+    T* acc;
+    T* vel;
+    uint64_t* h_keys;
+    int32_t* h_vals;
+    uint32_t h_mask;
+    SceneParams<T>* scenes;
+    double* grid_mass; // per scene, refreshed every substep
+    DevStatus* st;
+    uint32_t n_total;
+    uint32_t b_cap;
+    KeyLayout kl;
+};
+
+__host__ __device__ inline uint64_t hash64(uint64_t k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return k;
+}
+
+__device__ inline void raise_flag(DevStatus* st, uint32_t f)
+{
+    uint32_t old = atomicOr(&st->flags, f | ((f & ABORTING) ? FLAG_ABORT : 0u));
+    if ((f & ABORTING) && !(old & FLAG_ABORT)) atomicExch(&st->abort_step, (int32_t)st->step);
+}
+
+__device__ inline bool aborted(const DevStatus* st) { return (*(volatile const uint32_t*)&st->flags & FLAG_ABORT) != 0; }
+
+// the same decision for every thread of the CTA (kernels with barriers or full-warp shuffles must not
+// let some threads leave early)
+__device__ inline bool aborted_cta(const DevStatus* st)
+{
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) s_abort = aborted(st) ? 1 : 0;
+    __syncthreads();
+    bool r = s_abort != 0;
+    __syncthreads();
+    return r;
+}
+
+__device__ inline int hash_find(const uint64_t* hk, const int32_t* hv, uint32_t mask, uint64_t key)
+{
+    uint32_t h = (uint32_t)hash64(key) & mask;
+    for (int p = 0; p < HASH_PROBES; p++) {
+        uint64_t k = hk[h];
+        if (k == key) return hv[h];
+        if (k == HASH_EMPTY) return -1;
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// keys of the current particle positions (used after a load or a host upload; afterwards G2P writes
+// the keys of the next substep). Also checks that every base node lies in its scene's domain.
+// ---------------------------------------------------------------------------------------------------
+template <class T>
+__global__ void k_keys(Pool<T> p, const SceneParams<T>* scenes, int n_scenes, uint64_t* keys, uint32_t n_total, KeyLayout kl, DevStatus* st)
+{
+    using L = typename LayoutOf<T>::type;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_total; i += gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_scenes - 1; // scene owning storage slot i
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (scenes[mid].first <= (int64_t)i) lo = mid;
+            else hi = mid - 1;
+        }
+        const SceneParams<T>& sp = scenes[lo];
+        int b[3];
+        bool ok = true;
+        for (int a = 0; a < 3; a++) {
+            T x = p.f[(P_X + a) * p.stride + i];
+            b[a] = base_node(x, sp.inv_dx);
+            ok = ok && (x == x) && b[a] >= 0 && b[a] < sp.domain_cells - 3;
+        }
+        if (!ok) {
+            raise_flag(st, FLAG_OUT_OF_DOMAIN);
+            b[0] = b[1] = b[2] = 0;
+        }
+        uint32_t orig = p.pid[i] & ((1u << L::index_bits) - 1);
+        keys[i] = ((uint64_t)lo << (kl.cp + kl.ib)) | ((L::offset(b[0], b[1], b[2]) >> L::data_bits) << kl.ib) | orig;
+    }
+}
+
+// group heads of the sorted keys: first index of every (scene, page)
+struct GroupHead {
+    const uint64_t* k;
+    KeyLayout kl;
+    __device__ bool operator()(uint32_t i) const { return i == 0 || kl.group(k[i]) != kl.group(k[i - 1]); }
+};
+
+template <class T>
+__global__ void k_activate(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const uint32_t G = a.st->n_groups;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_groups_seen = max(a.st->max_groups_seen, G);
+    if (G > a.b_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise_flag(a.st, FLAG_CAPACITY);
+        return;
+    }
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
+        uint32_t g = t >> 3, dl = t & 7;
+        uint64_t key0 = a.keys_sorted[a.g_start[g]];
+        uint64_t scene = a.kl.scene(key0);
+        uint32_t bi, bj, bk;
+        L::block_of_page(a.kl.page(key0), bi, bj, bk);
+        uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
+        uint32_t h = (uint32_t)hash64(hk) & a.h_mask;
+        bool done = false;
+        for (int p = 0; p < HASH_PROBES && !done; p++) {
+            unsigned long long prev = atomicCAS((unsigned long long*)&a.h_keys[h], (unsigned long long)HASH_EMPTY, (unsigned long long)hk);
+            if (prev == HASH_EMPTY) {
+                uint32_t slot = atomicAdd(&a.st->n_blocks, 1u);
+                if (slot >= a.b_cap) {
+                    raise_flag(a.st, FLAG_CAPACITY);
+                    a.h_vals[h] = -1;
+                }
+                else {
+                    a.h_vals[h] = (int32_t)slot;
+                    a.b_key[slot] = hk;
+                }
+                done = true;
+            }
+            else if (prev == hk)
+                done = true;
+            else
+                h = (h + 1) & a.h_mask;
+        }
+        if (!done) raise_flag(a.st, FLAG_CAPACITY);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// P2G
+// ---------------------------------------------------------------------------------------------------
+template <class T>
+__device__ inline void flush_column(T* dst, const T* src, int n)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        if (n == 4) {
+            float4 v = make_float4(src[0], src[1], src[2], src[3]);
+            if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd((float4*)dst, v);
+        }
+        else {
+            float2 v = make_float2(src[0], src[1]);
+            if (v.x != 0.f || v.y != 0.f) atomicAdd((float2*)dst, v);
+        }
+    }
+    else {
+        for (int q = 0; q < n; q++)
+            if (src[q] != (T)0) atomicAdd(dst + q, src[q]);
+    }
+}
+
+template <class T, int NT>
+__global__ void __launch_bounds__(NT) k_p2g(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
+    __shared__ T tile[NACC * TN];
+    __shared__ int s_g, s_nbr[8], s_scene;
+    __shared__ int s_org[3];
+    if (aborted_cta(a.st)) return;
+    const uint32_t G = a.st->n_groups;
+    for (;;) {
+        if (threadIdx.x == 0) s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
+        __syncthreads();
+        const int g = s_g;
+        if (g >= (int)G) break;
+        const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
+        if (threadIdx.x < 8) {
+            uint64_t key0 = a.keys_sorted[start];
+            uint64_t scene = a.kl.scene(key0);
+            uint32_t bi, bj, bk;
+            L::block_of_page(a.kl.page(key0), bi, bj, bk);
+            int dl = threadIdx.x;
+            uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
+            int slot = hash_find(a.h_keys, a.h_vals, a.h_mask, hk);
+            if (slot < 0) raise_flag(a.st, FLAG_CAPACITY);
+            s_nbr[dl] = slot;
+            a.g_nbr[g * 8 + dl] = slot;
+            if (dl == 0) {
+                s_scene = (int)scene;
+                s_org[0] = (int)(bi * L::sx);
+                s_org[1] = (int)(bj * L::sy);
+                s_org[2] = (int)(bk * L::sz);
+            }
+        }
+        for (int q = threadIdx.x; q < NACC * TN; q += NT) tile[q] = (T)0;
+        __syncthreads();
+        bool bad_slot = false;
+        for (int d = 0; d < 8; d++) bad_slot |= s_nbr[d] < 0;
+        if (!bad_slot) {
+            const SceneParams<T>& sp = a.scenes[s_scene];
+            const T dx = sp.dx, inv_dx = sp.inv_dx;
+            const bool damage = sp.damage != 0;
+            const Pool<T>& P = a.pin;
+            for (uint32_t i = start + threadIdx.x; i < end; i += NT) {
+                const uint32_t j = a.vals_sorted[i];
+                T x[3], v[3], Cm[9], F[9];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    x[c] = P.f[(P_X + c) * P.stride + j];
+                    v[c] = P.f[(P_V + c) * P.stride + j];
+                }
+#pragma unroll
+                for (int c = 0; c < 9; c++) {
+                    Cm[c] = P.f[(P_C + c) * P.stride + j];
+                    F[c] = P.f[(P_F + c) * P.stride + j];
+                }
+                const T mass = P.f[P_M * P.stride + j], V0 = P.f[P_V0 * P.stride + j];
+                const T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
+                const uint32_t mat = P.pid[j] >> L::index_bits;
+                const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+                T tau[9];
+                if (mt.model == MODEL_COROTATED) {
+                    if (tau_corotated(mt, F, tau)) atomicAdd(&a.st->fallback, 1u);
+                }
+                else
+                    tau_nhb(mt, F, (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1, tau);
+                // -V0 tau, m C, m v
+                T S[9];
+#pragma unroll
+                for (int c = 0; c < 9; c++) {
+                    S[c] = -V0 * tau[c];
+                    Cm[c] *= mass;
+                }
+                T mom[3] = { mass * v[0], mass * v[1], mass * v[2] };
+                int b[3], l[3];
+                T w[3][3], dw[3][3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    T xs = mul_rn(x[c], inv_dx);
+                    b[c] = int_floor(sub_rn(xs, (T)0.5));
+                    bspline_w(xs, b[c], w[c], dw[c]);
+                    l[c] = b[c] - s_org[c];
+                }
+                if (l[0] < 0 || l[0] >= L::sx || l[1] < 0 || l[1] >= L::sy || l[2] < 0 || l[2] >= L::sz) {
+                    raise_flag(a.st, FLAG_CAPACITY);
+                    continue;
+                }
+#pragma unroll
+                for (int ii = 0; ii < 3; ii++) {
+                    const T xm0 = (T)(b[0] + ii) * dx - x[0];
+#pragma unroll
+                    for (int jj = 0; jj < 3; jj++) {
+                        const T xm1 = (T)(b[1] + jj) * dx - x[1];
+                        const T wij = w[0][ii] * w[1][jj];
+#pragma unroll
+                        for (int kk = 0; kk < 3; kk++) {
+                            const T xm2 = (T)(b[2] + kk) * dx - x[2];
+                            const T wk = w[2][kk];
+                            const T wijk = wij * wk;
+                            const T g0 = inv_dx * dw[0][ii] * w[1][jj] * wk;
+                            const T g1 = inv_dx * w[0][ii] * dw[1][jj] * wk;
+                            const T g2 = inv_dx * wij * dw[2][kk];
+                            T* t = tile + ((l[0] + ii) * TY + (l[1] + jj)) * TZ + (l[2] + kk);
+                            atomicAdd(t, wijk * mass);
+#pragma unroll
+                            for (int r = 0; r < 3; r++) {
+                                T mv = wijk * (mom[r] + Cm[3 * r] * xm0 + Cm[3 * r + 1] * xm1 + Cm[3 * r + 2] * xm2);
+                                T f = S[3 * r] * g0 + S[3 * r + 1] * g1 + S[3 * r + 2] * g2;
+                                atomicAdd(t + (1 + r) * TN, mv);
+                                atomicAdd(t + (4 + r) * TN, f);
+                            }
+                            if (damage) {
+                                atomicAdd(t + 7 * TN, wijk * dd);
+                                atomicAdd(t + 8 * TN, wijk);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (!bad_slot) {
+            // tile -> global: z columns split at the block boundary (4 + 2 nodes)
+            for (int q = threadIdx.x; q < NACC * TX * TY * 2; q += NT) {
+                const int half = q & 1, col = q >> 1;
+                const int f = col / (TX * TY), ab = col % (TX * TY), ta = ab / TY, tb = ab % TY;
+                const int ax = ta >= L::sx, ay = tb >= L::sy;
+                const int slot = s_nbr[ax * 4 + ay * 2 + half];
+                T* dst = a.acc + ((size_t)slot * NACC + f) * L::nodes + L::element(ta - ax * L::sx, tb - ay * L::sy, 0);
+                const T* src = tile + f * TN + (ta * TY + tb) * TZ + half * L::sz;
+                flush_column(dst, src, half ? TZ - L::sz : L::sz);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// grid update
+// ---------------------------------------------------------------------------------------------------
+template <class T>
+__global__ void k_grid(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted_cta(a.st)) return;
+    const uint32_t B = min(a.st->n_blocks, a.b_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_blocks_seen = max(a.st->max_blocks_seen, B);
+    const uint32_t total = B * L::nodes;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ((total + 31) & ~31u); t += gridDim.x * blockDim.x) {
+        T gm = 0;
+        int scene = -1;
+        if (t < total) {
+            const uint32_t b = t / L::nodes, e = t % L::nodes;
+            const uint64_t hk = a.b_key[b];
+            scene = (int)(hk >> 40);
+            const SceneParams<T>& sp = a.scenes[scene];
+            T* A = a.acc + (size_t)b * NACC * L::nodes + e;
+            T m = A[0];
+            T vv[3] = { A[L::nodes], A[2 * L::nodes], A[3 * L::nodes] };
+            T f[3] = { A[4 * L::nodes], A[5 * L::nodes], A[6 * L::nodes] };
+            T pf = A[7 * L::nodes], pfm = A[8 * L::nodes];
+#pragma unroll
+            for (int q = 0; q < NACC; q++) A[q * L::nodes] = (T)0;
+            T* V = a.vel + (size_t)b * NVEL * L::nodes + e;
+            gm = m;
+            if (m != (T)0) {
+                uint32_t bi, bj, bk;
+                L::block_of_page(hk & ((1ULL << 40) - 1), bi, bj, bk);
+                const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
+                const T xi[3] = { (T)(bi * L::sx + lx) * sp.dx, (T)(bj * L::sy + ly) * sp.dx, (T)(bk * L::sz + lz) * sp.dx };
+                const T dt = sp.dt, dt_over_m = dt / m;
+                T vi[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) vi[c] = vv[c] / m + sp.gravity[c] * dt + f[c] * dt_over_m;
+                collide(sp, (T)sp.time, xi, vi);
+                V[0] = vi[0];
+                V[L::nodes] = vi[1];
+                V[2 * L::nodes] = vi[2];
+                V[3 * L::nodes] = pfm != (T)0 ? pf / pfm : (T)0;
+            }
+            else {
+                V[0] = V[L::nodes] = V[2 * L::nodes] = V[3 * L::nodes] = (T)0;
+            }
+        }
+        // grid mass per scene: nodes of one warp share a block (and so a scene) whenever L::nodes >= 32
+        double s = (double)gm;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        int sc0 = __shfl_sync(0xffffffffu, scene, 0);
+        if ((threadIdx.x & 31) == 0 && sc0 >= 0) atomicAdd(&a.grid_mass[sc0], s);
+    }
+    // the hash table is used only by activate and P2G: clear it for the next substep
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= a.h_mask; h += gridDim.x * blockDim.x) a.h_keys[h] = HASH_EMPTY;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// G2P
+// ---------------------------------------------------------------------------------------------------
+template <class T, int NT>
+__global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    __shared__ T sv[8 * NVEL * L::nodes];
+    __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
+    if (aborted_cta(a.st)) return;
+    const uint32_t G = a.st->n_groups;
+    const KeyLayout kl = a.kl;
+    for (;;) {
+        if (threadIdx.x == 0) s_g = (int)atomicAdd(&a.st->work_g2p, 1u);
+        __syncthreads();
+        const int g = s_g;
+        if (g >= (int)G) break;
+        const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
+        if (threadIdx.x < 8) {
+            s_nbr[threadIdx.x] = a.g_nbr[g * 8 + threadIdx.x];
+            if (threadIdx.x == 0) {
+                uint64_t key0 = a.keys_sorted[start];
+                uint32_t bi, bj, bk;
+                L::block_of_page(kl.page(key0), bi, bj, bk);
+                s_scene = (int)kl.scene(key0);
+                s_org[0] = (int)(bi * L::sx);
+                s_org[1] = (int)(bj * L::sy);
+                s_org[2] = (int)(bk * L::sz);
+            }
+        }
+        __syncthreads();
+        // stage the velocities of the 8 neighbouring blocks
+        for (int q = threadIdx.x; q < 8 * NVEL * L::nodes; q += NT) {
+            int d = q / (NVEL * L::nodes), r = q % (NVEL * L::nodes);
+            int slot = s_nbr[d];
+            sv[q] = slot >= 0 ? a.vel[(size_t)slot * NVEL * L::nodes + r] : (T)0;
+        }
+        __syncthreads();
+        const SceneParams<T>& sp = a.scenes[s_scene];
+        const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt, D_inv = sp.D_inv;
+        const T ca = sp.apic_a, cb = sp.apic_b;
+        const bool damage = sp.damage != 0;
+        const T dx2 = dx * dx, half_cfl2 = dx2 * (T)0.25 * (sp.cfl * sp.cfl);
+        const Pool<T>& P = a.pin;
+        const Pool<T>& Q = a.pout;
+        uint32_t flags = 0;
+        for (uint32_t i = start + threadIdx.x; i < end; i += NT) {
+            const uint32_t j = a.vals_sorted[i];
+            T x[3], F[9];
+#pragma unroll
+            for (int c = 0; c < 3; c++) x[c] = P.f[(P_X + c) * P.stride + j];
+            int b[3], l[3];
+            T w[3][3], dw[3][3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T xs = mul_rn(x[c], inv_dx);
+                b[c] = int_floor(sub_rn(xs, (T)0.5));
+                bspline_w(xs, b[c], w[c], dw[c]);
+                l[c] = b[c] - s_org[c];
+            }
+            if (l[0] < 0 || l[0] >= L::sx || l[1] < 0 || l[1] >= L::sy || l[2] < 0 || l[2] >= L::sz) {
+                flags |= FLAG_CAPACITY; // a particle outside its group's block: keys and positions disagree
+                continue;
+            }
+            T pv[3] = { 0, 0, 0 }, Bm[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0;
+            const T ii2 = inv_dx * inv_dx;
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++) {
+                const int tx = l[0] + ii, ax = tx >= L::sx, ex = tx - ax * L::sx;
+                const T xm0 = (T)(b[0] + ii) * dx - x[0];
+                const T ddw = ii == 1 ? (T)-2 : (T)1; // quadratic d2w/dx2 = (1,-2,1)
+#pragma unroll
+                for (int jj = 0; jj < 3; jj++) {
+                    const int ty = l[1] + jj, ay = ty >= L::sy, ey = ty - ay * L::sy;
+                    const T xm1 = (T)(b[1] + jj) * dx - x[1];
+                    const T wij = w[0][ii] * w[1][jj];
+#pragma unroll
+                    for (int kk = 0; kk < 3; kk++) {
+                        const int tz = l[2] + kk, az = tz >= L::sz, ez = tz - az * L::sz;
+                        const T xm2 = (T)(b[2] + kk) * dx - x[2];
+                        const T wk = w[2][kk];
+                        const T wijk = wij * wk;
+                        const T g0 = inv_dx * dw[0][ii] * w[1][jj] * wk;
+                        const T g1 = inv_dx * w[0][ii] * dw[1][jj] * wk;
+                        const T g2 = inv_dx * wij * dw[2][kk];
+                        const T* nv = sv + (ax * 4 + ay * 2 + az) * NVEL * L::nodes + L::element(ex, ey, ez);
+                        const T v0 = nv[0], v1 = nv[L::nodes], v2 = nv[2 * L::nodes];
+                        const T vv[3] = { v0, v1, v2 };
+                        const T xmw[3] = { xm0 * wijk, xm1 * wijk, xm2 * wijk };
+#pragma unroll
+                        for (int r = 0; r < 3; r++) {
+                            pv[r] += wijk * vv[r];
+                            Bm[3 * r] += vv[r] * xmw[0];
+                            Bm[3 * r + 1] += vv[r] * xmw[1];
+                            Bm[3 * r + 2] += vv[r] * xmw[2];
+                            Gv[3 * r] += vv[r] * g0;
+                            Gv[3 * r + 1] += vv[r] * g1;
+                            Gv[3 * r + 2] += vv[r] * g2;
+                        }
+                        if (damage) {
+                            // the reference's 3D Laplacian weights every term with d2w(i) (MpmGrid.h:607-613)
+                            const T Lw = ii2 * ddw * (w[1][jj] * wk + w[0][ii] * wk + w[0][ii] * w[1][jj]);
+                            lap += nv[3 * L::nodes] * Lw;
+                        }
+                    }
+                }
+            }
+            const uint32_t pid = P.pid[j];
+#pragma unroll
+            for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
+            T dd = 0, sc = 0;
+            if (damage) {
+                dd = P.f[P_D * P.stride + j];
+                sc = P.f[P_SC * P.stride + j];
+                const uint32_t mat = pid >> L::index_bits;
+                const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+                if (mt.damage && mt.model == MODEL_NEOHOOKEAN_BORDEN) {
+                    bool fb = false;
+                    dd = damage_update(mt, F, dd, lap, sc, dt, fb);
+                    if (fb) atomicAdd(&a.st->fallback, 1u);
+                }
+            }
+            T Cn[9], Fn[9], A[9];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    Cn[3 * r + c] = (ca * Bm[3 * r + c] + cb * Bm[3 * c + r]) * D_inv;
+                    A[3 * r + c] = (r == c ? (T)1 : (T)0) + dt * Gv[3 * r + c];
+                }
+            mul3(A, F, Fn);
+            T xn[3], inc2 = 0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T inc = dt * pv[c];
+                inc2 += inc * inc;
+                xn[c] = x[c] + inc;
+            }
+            if (inc2 > dx2) flags |= FLAG_CFL;
+            if (inc2 > half_cfl2) flags |= FLAG_CFL_HALF;
+            bool finite = isfinite(inc2) && isfinite(dd);
+#pragma unroll
+            for (int c = 0; c < 9; c++) finite = finite && isfinite(Fn[c]) && isfinite(Cn[c]);
+            if (!finite) flags |= FLAG_NONFINITE;
+            // key of the next substep
+            int nb[3];
+            bool in_dom = true;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                nb[c] = base_node(xn[c], inv_dx);
+                in_dom = in_dom && nb[c] >= 0 && nb[c] < sp.domain_cells - 3;
+            }
+            if (!in_dom) {
+                flags |= FLAG_OUT_OF_DOMAIN;
+                nb[0] = nb[1] = nb[2] = 0;
+            }
+            const uint32_t orig = pid & ((1u << L::index_bits) - 1);
+            a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib) | orig;
+            // particle -> sorted slot i of the other buffer
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Q.f[(P_X + c) * Q.stride + i] = xn[c];
+                Q.f[(P_V + c) * Q.stride + i] = pv[c];
+            }
+#pragma unroll
+            for (int c = 0; c < 9; c++) {
+                Q.f[(P_C + c) * Q.stride + i] = Cn[c];
+                Q.f[(P_F + c) * Q.stride + i] = Fn[c];
+            }
+            Q.f[P_M * Q.stride + i] = P.f[P_M * P.stride + j];
+            Q.f[P_V0 * Q.stride + i] = P.f[P_V0 * P.stride + j];
+            if (damage) {
+                Q.f[P_D * Q.stride + i] = dd;
+                Q.f[P_SC * Q.stride + i] = sc;
+            }
+            Q.pid[i] = pid;
+        }
+        if (flags) raise_flag(a.st, flags);
+        __syncthreads();
+    }
+}
+
+template <class T>
+__global__ void k_step_end(SceneParams<T>* scenes, int n_scenes, DevStatus* st)
+{
+    if (aborted(st)) return;
+    for (int s = threadIdx.x; s < n_scenes; s += blockDim.x) scenes[s].time += (double)scenes[s].dt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->step += 1;
+        st->n_blocks = 0;
+        st->work_p2g = 0;
+        st->work_g2p = 0;
+    }
+}
+
+template <class T>
+__global__ void k_zero_grid_mass(double* gm, int n)
+{
+    for (int s = threadIdx.x; s < n; s += blockDim.x) gm[s] = 0;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// host <-> device field transfer (caller order <-> storage order via the original index)
+// ---------------------------------------------------------------------------------------------------
+template <class T, class O>
+__global__ void k_export(Pool<T> p, int64_t first, int64_t n, int f0, int nc, O* out, int out_stride, int out_off)
+{
+    using L = typename LayoutOf<T>::type;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = first + i;
+        const uint32_t orig = p.pid[s] & ((1u << L::index_bits) - 1);
+        for (int c = 0; c < nc; c++) out[(int64_t)orig * out_stride + out_off + c] = (O)p.f[(f0 + c) * p.stride + s];
+    }
+}
+
+template <class T, class I>
+__global__ void k_import(Pool<T> p, int64_t first, int64_t n, int f0, int nc, const I* in, int in_stride, int in_off)
+{
+    using L = typename LayoutOf<T>::type;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = first + i;
+        const uint32_t orig = p.pid[s] & ((1u << L::index_bits) - 1);
+        for (int c = 0; c < nc; c++) p.f[(f0 + c) * p.stride + s] = (T)in[(int64_t)orig * in_stride + in_off + c];
+    }
+}
+
+// FP64-accumulated particle reductions of one scene: mass, momentum (3), kinetic energy, max speed
+template <class T>
+__global__ void k_reduce(Pool<T> p, int64_t first, int64_t n, double* out)
+{
+    double M = 0, px = 0, py = 0, pz = 0, ke = 0, vmax = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = first + i;
+        double m = p.f[P_M * p.stride + s];
+        double vx = p.f[(P_V + 0) * p.stride + s], vy = p.f[(P_V + 1) * p.stride + s], vz = p.f[(P_V + 2) * p.stride + s];
+        M += m;
+        px += m * vx;
+        py += m * vy;
+        pz += m * vz;
+        double s2 = vx * vx + vy * vy + vz * vz;
+        ke += 0.5 * m * s2;
+        vmax = fmax(vmax, sqrt(s2));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        M += __shfl_down_sync(0xffffffffu, M, o);
+        px += __shfl_down_sync(0xffffffffu, px, o);
+        py += __shfl_down_sync(0xffffffffu, py, o);
+        pz += __shfl_down_sync(0xffffffffu, pz, o);
+        ke += __shfl_down_sync(0xffffffffu, ke, o);
+        vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out + 0, M);
+        atomicAdd(out + 1, px);
+        atomicAdd(out + 2, py);
+        atomicAdd(out + 3, pz);
+        atomicAdd(out + 4, ke);
+        // speeds are non-negative: their IEEE bit patterns order like unsigned integers
+        atomicMax((unsigned long long*)(out + 5), (unsigned long long)__double_as_longlong(vmax));
+    }
+}
+
+template <class T>
+__global__ void k_iota_pid(uint32_t* pid, const uint8_t* mat, int64_t first, int64_t n)
+{
+    using L = typename LayoutOf<T>::type;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        pid[first + i] = (uint32_t)i | ((uint32_t)(mat ? mat[i] : 0) << L::index_bits);
+}
+
+template <class T>
+__global__ void k_iota(uint32_t* v, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
+} // namespace zr

@@ -1,0 +1,461 @@
+// Per-particle and per-node physics of the explicit MPM substep, written for the GPU (also compiles as
+// plain C++ so the same code can be exercised on the host). Matrices are row-major T[9].
+#pragma once
+#include "common.cuh"
+#include <cmath>
+#include <cfloat>
+
+namespace zr {
+
+template <class T>
+struct Eps;
+template <>
+struct Eps<float> {
+    static constexpr float polar_tol = 3e-4f; // Newton stops once a step changes X by less (quadratic phase)
+    static constexpr int polar_iters = 12;
+    static constexpr float polar_kappa = 1e3f; // condition bound above which FP64 takes over
+    static constexpr int jacobi_sweeps = 6;
+};
+template <>
+struct Eps<double> {
+    static constexpr double polar_tol = 1e-8;
+    static constexpr int polar_iters = 16;
+    static constexpr double polar_kappa = 1e7;
+    static constexpr int jacobi_sweeps = 10;
+};
+
+// correctly rounded multiply / subtract with no contraction: the base node must match the
+// reference's floor(x * (1/dx) - 0.5) bit for bit (BSplines.h:16-20, MpmSimulationBase.cpp:1544-1549)
+ZR_HD float mul_rn(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    volatile float r = a * b;
+    return r;
+#endif
+}
+ZR_HD double mul_rn(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __dmul_rn(a, b);
+#else
+    volatile double r = a * b;
+    return r;
+#endif
+}
+ZR_HD float sub_rn(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    volatile float r = a - b;
+    return r;
+#endif
+}
+ZR_HD double sub_rn(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __dsub_rn(a, b);
+#else
+    volatile double r = a - b;
+    return r;
+#endif
+}
+
+// int_floor: truncate, then step down when truncation rounded up (MathTools.h:15-25)
+template <class T>
+ZR_HD int int_floor(T x)
+{
+    int i = (int)x;
+    return i - ((T)i > x);
+}
+
+// base node of a particle coordinate (in metres) along one axis
+template <class T>
+ZR_HD int base_node(T X, T inv_dx)
+{
+    return int_floor(sub_rn(mul_rn(X, inv_dx), (T)0.5));
+}
+
+// quadratic B-spline weights and derivatives of the three nodes base..base+2 (BSplines.h:73-100)
+template <class T>
+ZR_HD void bspline_w(T xs, int base, T w[3], T dw[3])
+{
+    T d0 = xs - (T)base;
+    T z = (T)1.5 - d0;
+    T d1 = d0 - (T)1;
+    T zz = d0 - (T)0.5;
+    w[0] = (T)0.5 * z * z;
+    w[1] = (T)0.75 - d1 * d1;
+    w[2] = (T)0.5 * zz * zz;
+    dw[0] = -z;
+    dw[1] = (T)-2 * d1;
+    dw[2] = zz;
+}
+
+// ------------------------------------------------------------------------------------------------
+// 3x3 helpers
+// ------------------------------------------------------------------------------------------------
+template <class T>
+ZR_HD T det3(const T* F)
+{
+    return F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) + F[2] * (F[3] * F[7] - F[4] * F[6]);
+}
+// J F^{-T} (DenseExt.h:241-252)
+template <class T>
+ZR_HD void cofactor3(const T* F, T* A)
+{
+    A[0] = F[4] * F[8] - F[5] * F[7];
+    A[1] = F[5] * F[6] - F[3] * F[8];
+    A[2] = F[3] * F[7] - F[4] * F[6];
+    A[3] = F[2] * F[7] - F[1] * F[8];
+    A[4] = F[0] * F[8] - F[2] * F[6];
+    A[5] = F[1] * F[6] - F[0] * F[7];
+    A[6] = F[1] * F[5] - F[2] * F[4];
+    A[7] = F[2] * F[3] - F[0] * F[5];
+    A[8] = F[0] * F[4] - F[1] * F[3];
+}
+template <class T>
+ZR_HD void mul3(const T* A, const T* B, T* R)
+{
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) R[3 * r + c] = A[3 * r] * B[c] + A[3 * r + 1] * B[3 + c] + A[3 * r + 2] * B[6 + c];
+}
+template <class T>
+ZR_HD void mul3_bt(const T* A, const T* B, T* R) // A B^T
+{
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) R[3 * r + c] = A[3 * r] * B[3 * c] + A[3 * r + 1] * B[3 * c + 1] + A[3 * r + 2] * B[3 * c + 2];
+}
+
+ZR_HD float rcbrt_(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return rcbrtf(x);
+#else
+    return 1.0f / std::cbrt(x);
+#endif
+}
+ZR_HD double rcbrt_(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return rcbrt(x);
+#else
+    return 1.0 / std::cbrt(x);
+#endif
+}
+
+// ------------------------------------------------------------------------------------------------
+// Robust FP64 SVD by one-sided (Hestenes) Jacobi, with Ziran's sign convention: U and V proper
+// rotations, |s0| >= |s1| >= |s2|, only s2 may be negative (ImplicitQRSVD.h:455-460 contract).
+// Used when the FP32/FP64 Newton polar iteration is not applicable (inverted or ill-conditioned F).
+// ------------------------------------------------------------------------------------------------
+ZR_HD void svd3_jacobi(const double* A, double* U, double* s, double* V)
+{
+    double W[9], Vm[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 };
+    for (int i = 0; i < 9; i++) W[i] = A[i];
+    for (int sweep = 0; sweep < 30; sweep++) {
+        double off = 0;
+        for (int pq = 0; pq < 3; pq++) {
+            int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            double a = 0, b = 0, g = 0;
+            for (int r = 0; r < 3; r++) {
+                a += W[3 * r + p] * W[3 * r + p];
+                b += W[3 * r + q] * W[3 * r + q];
+                g += W[3 * r + p] * W[3 * r + q];
+            }
+            double ab = sqrt(a * b);
+            if (ab == 0 || fabs(g) <= 1e-17 * ab) continue;
+            off = fmax(off, fabs(g) / ab);
+            double zeta = (b - a) / (2 * g);
+            double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+            double c = 1 / sqrt(1 + t * t), sn = c * t;
+            for (int r = 0; r < 3; r++) {
+                double wp = W[3 * r + p], wq = W[3 * r + q];
+                W[3 * r + p] = c * wp - sn * wq;
+                W[3 * r + q] = sn * wp + c * wq;
+                double vp = Vm[3 * r + p], vq = Vm[3 * r + q];
+                Vm[3 * r + p] = c * vp - sn * vq;
+                Vm[3 * r + q] = sn * vp + c * vq;
+            }
+        }
+        if (off < 1e-15) break;
+    }
+    double sg[3];
+    for (int c = 0; c < 3; c++) sg[c] = sqrt(W[c] * W[c] + W[3 + c] * W[3 + c] + W[6 + c] * W[6 + c]);
+    // sort columns by decreasing singular value (swap in W and V together)
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2 - i; j++)
+            if (sg[j] < sg[j + 1]) {
+                double t = sg[j];
+                sg[j] = sg[j + 1];
+                sg[j + 1] = t;
+                for (int r = 0; r < 3; r++) {
+                    t = W[3 * r + j];
+                    W[3 * r + j] = W[3 * r + j + 1];
+                    W[3 * r + j + 1] = t;
+                    t = Vm[3 * r + j];
+                    Vm[3 * r + j] = Vm[3 * r + j + 1];
+                    Vm[3 * r + j + 1] = t;
+                }
+            }
+    if (det3(Vm) < 0) // keep V a proper rotation; negating a column of both W and V leaves A unchanged
+        for (int r = 0; r < 3; r++) {
+            Vm[3 * r + 2] = -Vm[3 * r + 2];
+            W[3 * r + 2] = -W[3 * r + 2];
+        }
+    const double tiny = 1e-150;
+    double Um[9];
+    // first column
+    if (sg[0] > tiny)
+        for (int r = 0; r < 3; r++) Um[3 * r] = W[3 * r] / sg[0];
+    else {
+        Um[0] = 1;
+        Um[3] = 0;
+        Um[6] = 0;
+    }
+    // second column, orthogonal to the first
+    if (sg[1] > tiny * fmax(1.0, sg[0]))
+        for (int r = 0; r < 3; r++) Um[3 * r + 1] = W[3 * r + 1] / sg[1];
+    else {
+        double u0 = Um[0], u1 = Um[3], u2 = Um[6];
+        double px, py, pz;
+        if (fabs(u0) < 0.9) { px = 0; py = -u2; pz = u1; } // u x e0
+        else { px = u2; py = 0; pz = -u0; } // u x e1
+        double nn = sqrt(px * px + py * py + pz * pz);
+        Um[1] = px / nn;
+        Um[4] = py / nn;
+        Um[7] = pz / nn;
+    }
+    // third column completes a right-handed frame; the sign of s2 follows from W
+    double cx = Um[3] * Um[7] - Um[6] * Um[4];
+    double cy = Um[6] * Um[1] - Um[0] * Um[7];
+    double cz = Um[0] * Um[4] - Um[3] * Um[1];
+    double proj = cx * W[2] + cy * W[5] + cz * W[8];
+    Um[2] = cx;
+    Um[5] = cy;
+    Um[8] = cz;
+    sg[2] = proj; // negative when det(A) < 0: the sign sits on the smallest singular value
+    for (int i = 0; i < 9; i++) {
+        U[i] = Um[i];
+        V[i] = Vm[i];
+    }
+    s[0] = sg[0];
+    s[1] = sg[1];
+    s[2] = sg[2];
+}
+
+// Rotation of the polar decomposition F = R S (ImplicitQRSVD.h:546-558: R = U V^T of Ziran's SVD).
+// Determinant-scaled Newton iteration X <- (g X + X^{-T}/g)/2 in T; it converges quadratically to R
+// whenever det F > 0. Inverted, nearly singular or ill-conditioned F goes to the FP64 SVD.
+// Returns true when the FP64 path was taken.
+template <class T>
+ZR_HD bool polar_rotation(const T* F, T* R)
+{
+    T X[9], Cf[9];
+    for (int i = 0; i < 9; i++) X[i] = F[i];
+    bool ok = false;
+    {
+        cofactor3(X, Cf);
+        T J = X[0] * Cf[0] + X[1] * Cf[1] + X[2] * Cf[2];
+        T nf = 0, nc = 0;
+        for (int i = 0; i < 9; i++) {
+            nf += X[i] * X[i];
+            nc += Cf[i] * Cf[i];
+        }
+        // Frobenius condition number ||F|| ||F^-1|| = sqrt(nf nc) / J
+        if (J > 0 && nf * nc < (Eps<T>::polar_kappa * Eps<T>::polar_kappa) * (J * J)) {
+            for (int it = 0; it < Eps<T>::polar_iters; it++) {
+                T g = rcbrt_(J);
+                T a = (T)0.5 * g, b = (T)0.5 / (g * J);
+                T diff = 0;
+                for (int i = 0; i < 9; i++) {
+                    T xn = a * X[i] + b * Cf[i];
+                    T dd = xn - X[i];
+                    diff += dd * dd;
+                    X[i] = xn;
+                }
+                if (diff < Eps<T>::polar_tol * Eps<T>::polar_tol) {
+                    ok = true;
+                    break;
+                }
+                cofactor3(X, Cf);
+                J = X[0] * Cf[0] + X[1] * Cf[1] + X[2] * Cf[2];
+                if (!(J > 0)) break;
+            }
+        }
+    }
+    if (ok) {
+        for (int i = 0; i < 9; i++) R[i] = X[i];
+        return false;
+    }
+    double A[9], U[9], s[3], V[9];
+    for (int i = 0; i < 9; i++) A[i] = (double)F[i];
+    svd3_jacobi(A, U, s, V);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) R[3 * r + c] = (T)(U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + U[3 * r + 2] * V[3 * c + 2]);
+    return true;
+}
+
+// One Jacobi rotation zeroing a_pq of a symmetric 3x3 matrix; a_rp, a_rq are the entries coupling the
+// third index r. Q accumulates the rotations column-wise.
+template <class T>
+ZR_HD void jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T* Q, int p, int q)
+{
+    T x = apq;
+    if (x == (T)0) return;
+    T theta = (aqq - app) / ((T)2 * x);
+    T t = fabs(theta) > (T)1e15 ? (T)0.5 / theta : (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
+    T c = (T)1 / sqrt(t * t + (T)1), s = t * c;
+    app -= t * x;
+    aqq += t * x;
+    apq = (T)0;
+    T rp = arp, rq = arq;
+    arp = c * rp - s * rq;
+    arq = s * rp + c * rq;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        T qp = Q[3 * k + p], qq = Q[3 * k + q];
+        Q[3 * k + p] = c * qp - s * qq;
+        Q[3 * k + q] = s * qp + c * qq;
+    }
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix: S = Q diag(lam) Q^T.
+template <class T>
+ZR_HD void sym_eig3(const T* S, T* lam, T* Q)
+{
+    T a00 = S[0], a11 = S[4], a22 = S[8], a01 = (T)0.5 * (S[1] + S[3]), a02 = (T)0.5 * (S[2] + S[6]), a12 = (T)0.5 * (S[5] + S[7]);
+#pragma unroll
+    for (int i = 0; i < 9; i++) Q[i] = (i % 4 == 0) ? (T)1 : (T)0;
+    for (int sweep = 0; sweep < Eps<T>::jacobi_sweeps; sweep++) {
+        T off = a01 * a01 + a02 * a02 + a12 * a12;
+        T dg = a00 * a00 + a11 * a11 + a22 * a22;
+        if (off <= (T)1e-30 * dg || off == (T)0) break;
+        jacobi_rot(a00, a11, a01, a02, a12, Q, 0, 1);
+        jacobi_rot(a00, a22, a02, a01, a12, Q, 0, 2);
+        jacobi_rot(a11, a22, a12, a01, a02, Q, 1, 2);
+    }
+    lam[0] = a00;
+    lam[1] = a11;
+    lam[2] = a22;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Constitutive models. Both return the Kirchhoff stress tau; FBasedMpmForceHelper multiplies by V0
+// (FBasedMpmForceHelper.cpp:43-63).
+// ------------------------------------------------------------------------------------------------
+// Fixed corotated: P = 2 mu (F - R) + lambda (J-1) J F^{-T}, tau = P F^T
+// (CorotatedElasticity.cpp:56-76, HyperelasticConstitutiveModel.h:75-80)
+template <class T>
+ZR_HD bool tau_corotated(const Material<T>& mt, const T* F, T* tau)
+{
+    T R[9], Cf[9], P[9];
+    bool fb = polar_rotation(F, R);
+    cofactor3(F, Cf);
+    T J = det3(F);
+    T a = (T)2 * mt.mu, b = mt.lambda * (J - (T)1);
+    for (int i = 0; i < 9; i++) P[i] = a * (F[i] - R[i]) + b * Cf[i];
+    mul3_bt(P, F, tau);
+    return fb;
+}
+
+// Neo-Hookean (Borden): tau = g (tau_dev + tau_vol) for J >= 1, g tau_dev + tau_vol otherwise
+// (NeoHookeanBorden.cpp:71-94); kappa = 0.666666 mu + lambda (NeoHookeanBorden.cpp:20)
+template <class T>
+ZR_HD void tau_nhb(const Material<T>& mt, const T* F, T g, T* tau)
+{
+    T B[9];
+    mul3_bt(F, F, B);
+    T J = det3(F);
+    T tr3 = (B[0] + B[4] + B[8]) * ((T)1 / (T)3);
+    T rc = rcbrt_(J);
+    T s = J > (T)0 ? mt.mu * (rc * rc) : (T)NAN; // mu J^{-2/3}; pow() of a negative J is NaN in the reference too
+    T vol = J * (mt.kappa * (T)0.5 * (J - (T)1 / J));
+    bool tension = J >= (T)1;
+    T gd = g * s, gv = tension ? g * vol : vol;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) tau[3 * r + c] = gd * (B[3 * r + c] - (r == c ? tr3 : (T)0)) + (r == c ? gv : (T)0);
+}
+
+// degradation g(d) = (1-d)^2 (1-k) + k (AnisoFractureSimulation.h:279-280)
+template <class T>
+ZR_HD T degradation(T d, T k)
+{
+    return (((T)1 - d) * ((T)1 - d)) * ((T)1 - k) + k;
+}
+
+// Explicit AnisoMPM damage update of one particle (AnisoFractureSimulation.h:210-283, :365-391) with one
+// structural director a0 = e1 rotated by the polar R of F. Returns the new damage.
+template <class T>
+ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, T dt, bool& fallback)
+{
+    T geo = d - mt.l0 * mt.l0 * lap;
+    T tau[9];
+    tau_nhb(mt, F, (T)1, tau);
+    T invJ = (T)1 / det3(F);
+    T S[9], lam[3], Q[9];
+    for (int i = 0; i < 9; i++) S[i] = tau[i] * invJ; // undegraded Cauchy stress
+    sym_eig3(S, lam, Q);
+    T sp[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (int e = 0; e < 3; e++) {
+        T l = lam[e] > (T)0 ? lam[e] : (T)0; // Macaulay bracket of the principal stress
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) sp[3 * r + c] += l * (Q[3 * r + e] * Q[3 * c + e]);
+    }
+    T R[9];
+    fallback = polar_rotation(F, R);
+    T a[3] = { R[0], R[3], R[6] }; // R e1
+    T M[9]; // A sigma+ with A = I + alpha a a^T
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            T as = a[0] * sp[c] + a[1] * sp[3 + c] + a[2] * sp[6 + c];
+            M[3 * r + c] = sp[3 * r + c] + mt.alpha * a[r] * as;
+        }
+    // (A sigma+) : (sigma+ A) = sum_ij M_ij M_ji since sigma+ A = (A sigma+)^T
+    T contraction = 0;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) contraction += M[3 * r + c] * M[3 * c + r];
+    T phi = contraction / (sigma_c * sigma_c);
+    T dtilde = mt.zeta * (phi > (T)1 ? phi - (T)1 : (T)0);
+    T diff = ((T)1 - d) * dtilde - geo;
+    T nd = d + (dt / mt.eta) * (diff > (T)0 ? diff : (T)0);
+    return nd < (T)1 ? nd : (T)1;
+}
+
+// Analytic translating half-spaces at a grid node (CollisionObject.cpp:67-105, :342-406,
+// AnalyticLevelSet.cpp:318-334). Objects apply in order; a STICKY hit ends the loop.
+template <class T>
+ZR_HD void collide(const SceneParams<T>& sp, T time, const T* x, T* v)
+{
+    for (int k = 0; k < sp.n_objects; k++) {
+        const HalfSpaceObj<T>& h = sp.objects[k];
+        T phi = h.normal[0] * (x[0] - h.vel[0] * time - h.origin[0]) + h.normal[1] * (x[1] - h.vel[1] * time - h.origin[1])
+            + h.normal[2] * (x[2] - h.vel[2] * time - h.origin[2]);
+        if (!(phi <= (T)0)) continue;
+        T r[3] = { v[0] - h.vel[0], v[1] - h.vel[1], v[2] - h.vel[2] };
+        if (h.type == OBJ_STICKY) {
+            v[0] = h.vel[0];
+            v[1] = h.vel[1];
+            v[2] = h.vel[2];
+            break;
+        }
+        T dot = r[0] * h.normal[0] + r[1] * h.normal[1] + r[2] * h.normal[2];
+        if (h.type == OBJ_SLIP || dot < (T)0) {
+            for (int a = 0; a < 3; a++) r[a] -= h.normal[a] * dot;
+            if (h.friction != (T)0 && dot < (T)0) {
+                T vn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                if (-dot * h.friction < vn) {
+                    T sc = dot * h.friction / vn;
+                    for (int a = 0; a < 3; a++) r[a] += r[a] * sc;
+                }
+                else
+                    r[0] = r[1] = r[2] = (T)0;
+            }
+        }
+        for (int a = 0; a < 3; a++) v[a] = r[a] + h.vel[a];
+    }
+}
+
+} // namespace zr
