@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
     return ap.parse_args()
 
 
@@ -232,6 +233,12 @@ def run_ours(args, world, rank):
 
     s = zr.Scene(zr.F32)
     s.from_recipe(r)
+    if args.profile_only:
+        s.step(args.warmup)
+        s.step(args.steps)
+        g, b = s.last_grid()
+        print(json.dumps({"profile_only": True, "particles": n, "groups": g, "blocks": b, "ms_per_step": s.last_step_ms / max(1, args.steps)}))
+        return None
     clocks = ClockSampler()
     clocks.start()
     s.step(args.warmup)

@@ -30,7 +30,7 @@ inline int bitlen(uint64_t v)
 template <class T>
 class Engine final : public EngineBase {
     using L = typename LayoutOf<T>::type;
-    static constexpr int NT_P2G = 256;
+    static constexpr int NT_P2G = P2GShape<T>::NT;
     static constexpr int NT_G2P = 256;
     static constexpr int GRAPH_K = 8; // substeps per multi-step graph (even: returns to the same buffer)
 
@@ -198,7 +198,7 @@ public:
         ZR_CUDA(cudaStreamSynchronize(stream_));
         if (hs.flags & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle lies outside its scene's domain");
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
-        int rc = alloc_grid(std::max<uint32_t>(4096, 4 * hs.n_groups + 512));
+        int rc = alloc_grid(std::max<uint32_t>(4096, 8 * hs.n_groups + 1024)); // every group activates at most 8 blocks
         if (rc) return rc;
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
@@ -374,13 +374,21 @@ public:
     {
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
         const int64_t n = N_;
-        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        for (int attempt = 0;; attempt++) {
+            ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+            ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+            StepArgs<T> a = args(cur_);
+            ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
+            ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
+            k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+            ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+            if (!(hst_->flags & FLAG_CAPACITY) || attempt >= 6) break;
+            int rcg = alloc_grid(b_cap_ * 2);
+            if (rcg) return rcg;
+        }
         StepArgs<T> a = args(cur_);
-        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
-        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
-        k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
-        ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
-        ZR_CUDA(cudaStreamSynchronize(stream_));
+        (void)a;
         const uint32_t G = hst_->n_groups, B = std::min(hst_->n_blocks, b_cap_);
         std::vector<uint64_t> sk(n), bk(B);
         std::vector<uint32_t> gs(G);
@@ -481,7 +489,8 @@ private:
             init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
             return;
         }
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p2g_, k_p2g<T, NT_P2G>, NT_P2G, 0);
+        cudaFuncSetAttribute(k_p2g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p2g_, k_p2g<T>, NT_P2G, P2GShape<T>::dyn_bytes);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_, k_g2p<T, NT_G2P>, NT_G2P, 0);
         occ_p2g_ = std::max(1, occ_p2g_);
         occ_g2p_ = std::max(1, occ_g2p_);
@@ -611,7 +620,7 @@ private:
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
-        k_p2g<T, NT_P2G><<<nsm_ * occ_p2g_, NT_P2G, 0, stream_>>>(a);
+        k_p2g<T><<<nsm_ * occ_p2g_, NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
         k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));

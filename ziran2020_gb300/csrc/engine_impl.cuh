@@ -37,7 +37,7 @@
 
 namespace zr {
 
-constexpr int NACC = 9; // m, m v (3), f (3), d w, w
+constexpr int NACC = 6; // m, m v + dt f (3), d w, w
 constexpr int NVEL = 4; // v_new (3), normalised phase field
 constexpr uint64_t HASH_EMPTY = ~0ULL;
 constexpr int HASH_PROBES = 64;
@@ -232,28 +232,65 @@ __device__ inline void flush_column(T* dst, const T* src, int n)
     }
 }
 
-template <class T, int NT>
-__global__ void __launch_bounds__(NT) k_p2g(StepArgs<T> a)
+// P2G with no atomics in the hot loop. For every group (one occupied SPGrid block):
+//   phase 1 (thread per particle): stress and a 26-value payload per particle, staged in shared memory
+//   phase 2 (thread per cell and x-offset of the stencil): the particles of one cell all share the same
+//           27 nodes, so each thread accumulates its 9 nodes x 6 fields in registers over the cell's
+//           particles (deterministic order, no conflicts)
+//   phase 3: one shared add per node and field (distinct nodes within a warp), then vector atomics of
+//           the 6x6x6 node tile into the 8 neighbouring grid blocks
+// Payload: fractional index-space position f = x/dx - base, m, A = m v - dx (m C) f,
+// Bc = dx m C, K = -dt V0 tau / dx, d. With xm = (delta - f) dx for stencil offset delta:
+//   m v + m C xm = A + Bc delta  and  dt f_i = K . (dw_i w_j w_k, w_i dw_j w_k, w_i w_j dw_k),
+// so the node receives m w, w (A + Bc delta) + K grad-hat w, d w and w. The force enters the
+// momentum directly (m v + dt f), which the grid update turns into v + f dt/m + g dt as the reference's
+// gridVelocityExplicitUpdate does (MpmSimulationBase.cpp:1197-1226).
+constexpr int NPAY = 26;
+enum { Y_F = 0, Y_M = 3, Y_A = 4, Y_B = 7, Y_K = 16, Y_D = 25 };
+
+template <class T>
+struct P2GShape {
+    using L = typename LayoutOf<T>::type;
+    static constexpr int NT = 3 * L::nodes; // cells x stencil x-offsets
+    static constexpr int CHUNK = std::is_same<T, float>::value ? 512 : 256;
+    static constexpr int CPAD = CHUNK + CHUNK / 8;
+    static constexpr size_t dyn_bytes = sizeof(T) * NPAY * CPAD;
+};
+
+__device__ __forceinline__ int pay_slot(int q) { return q + (q >> 3); } // bank swizzle: cells hold ~8 particles
+
+template <class T>
+__global__ void __launch_bounds__(P2GShape<T>::NT, 2) k_p2g(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
+    using S = P2GShape<T>;
+    constexpr int NT = S::NT, CHUNK = S::CHUNK, CPAD = S::CPAD, NC = L::nodes;
     constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
+    extern __shared__ __align__(16) unsigned char p2g_dyn[];
+    T* pay = reinterpret_cast<T*>(p2g_dyn);
     __shared__ T tile[NACC * TN];
+    __shared__ uint8_t cellof[CHUNK];
+    __shared__ int16_t cfirst[NC], clast[NC];
     __shared__ int s_g, s_nbr[8], s_scene;
     __shared__ int s_org[3];
     if (aborted_cta(a.st)) return;
     const uint32_t G = a.st->n_groups;
+    const int tid = threadIdx.x;
+    // phase-2 role of this thread: cell c, stencil x-offset ii
+    const int ii = tid / NC, c = tid % NC;
+    const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
     for (;;) {
-        if (threadIdx.x == 0) s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
+        if (tid == 0) s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
         __syncthreads();
         const int g = s_g;
         if (g >= (int)G) break;
         const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
-        if (threadIdx.x < 8) {
+        if (tid < 8) {
             uint64_t key0 = a.keys_sorted[start];
             uint64_t scene = a.kl.scene(key0);
             uint32_t bi, bj, bk;
             L::block_of_page(a.kl.page(key0), bi, bj, bk);
-            int dl = threadIdx.x;
+            int dl = tid;
             uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
             int slot = hash_find(a.h_keys, a.h_vals, a.h_mask, hk);
             if (slot < 0) raise_flag(a.st, FLAG_CAPACITY);
@@ -266,27 +303,34 @@ __global__ void __launch_bounds__(NT) k_p2g(StepArgs<T> a)
                 s_org[2] = (int)(bk * L::sz);
             }
         }
-        for (int q = threadIdx.x; q < NACC * TN; q += NT) tile[q] = (T)0;
+        for (int q = tid; q < NACC * TN; q += NT) tile[q] = (T)0;
         __syncthreads();
         bool bad_slot = false;
         for (int d = 0; d < 8; d++) bad_slot |= s_nbr[d] < 0;
-        if (!bad_slot) {
-            const SceneParams<T>& sp = a.scenes[s_scene];
-            const T dx = sp.dx, inv_dx = sp.inv_dx;
-            const bool damage = sp.damage != 0;
+        const SceneParams<T>& sp = a.scenes[s_scene];
+        const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt;
+        const bool damage = sp.damage != 0;
+        const int nf = damage ? NACC : 4;
+        for (uint32_t c0 = start; c0 < end && !bad_slot; c0 += CHUNK) {
+            const int cnt = (int)min((uint32_t)CHUNK, end - c0);
+            // ---- phase 1: per particle
+            if (tid < NC) {
+                cfirst[tid] = 0;
+                clast[tid] = 0;
+            }
             const Pool<T>& P = a.pin;
-            for (uint32_t i = start + threadIdx.x; i < end; i += NT) {
-                const uint32_t j = a.vals_sorted[i];
+            for (int q = tid; q < cnt; q += NT) {
+                const uint32_t j = a.vals_sorted[c0 + q];
                 T x[3], v[3], Cm[9], F[9];
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    x[c] = P.f[(P_X + c) * P.stride + j];
-                    v[c] = P.f[(P_V + c) * P.stride + j];
+                for (int e = 0; e < 3; e++) {
+                    x[e] = P.f[(P_X + e) * P.stride + j];
+                    v[e] = P.f[(P_V + e) * P.stride + j];
                 }
 #pragma unroll
-                for (int c = 0; c < 9; c++) {
-                    Cm[c] = P.f[(P_C + c) * P.stride + j];
-                    F[c] = P.f[(P_F + c) * P.stride + j];
+                for (int e = 0; e < 9; e++) {
+                    Cm[e] = P.f[(P_C + e) * P.stride + j];
+                    F[e] = P.f[(P_F + e) * P.stride + j];
                 }
                 const T mass = P.f[P_M * P.stride + j], V0 = P.f[P_V0 * P.stride + j];
                 const T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
@@ -298,64 +342,117 @@ __global__ void __launch_bounds__(NT) k_p2g(StepArgs<T> a)
                 }
                 else
                     tau_nhb(mt, F, (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1, tau);
-                // -V0 tau, m C, m v
-                T S[9];
+                T fr[3];
+                int l[3];
 #pragma unroll
-                for (int c = 0; c < 9; c++) {
-                    S[c] = -V0 * tau[c];
-                    Cm[c] *= mass;
+                for (int e = 0; e < 3; e++) {
+                    const T xs = mul_rn(x[e], inv_dx);
+                    const int b = int_floor(sub_rn(xs, (T)0.5));
+                    fr[e] = xs - (T)b;
+                    l[e] = b - s_org[e];
                 }
-                T mom[3] = { mass * v[0], mass * v[1], mass * v[2] };
-                int b[3], l[3];
-                T w[3][3], dw[3][3];
+                const bool inside = l[0] >= 0 && l[0] < L::sx && l[1] >= 0 && l[1] < L::sy && l[2] >= 0 && l[2] < L::sz;
+                if (!inside) raise_flag(a.st, FLAG_CAPACITY); // keys and positions disagree: abort the substep
+                cellof[q] = inside ? (uint8_t)L::element(l[0], l[1], l[2]) : (uint8_t)0xff;
+                T* y = pay + pay_slot(q);
+                const T kf = -dt * V0 * inv_dx;
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    T xs = mul_rn(x[c], inv_dx);
-                    b[c] = int_floor(sub_rn(xs, (T)0.5));
-                    bspline_w(xs, b[c], w[c], dw[c]);
-                    l[c] = b[c] - s_org[c];
-                }
-                if (l[0] < 0 || l[0] >= L::sx || l[1] < 0 || l[1] >= L::sy || l[2] < 0 || l[2] >= L::sz) {
-                    raise_flag(a.st, FLAG_CAPACITY);
-                    continue;
-                }
+                for (int e = 0; e < 3; e++) y[(Y_F + e) * CPAD] = fr[e];
+                y[Y_M * CPAD] = mass;
 #pragma unroll
-                for (int ii = 0; ii < 3; ii++) {
-                    const T xm0 = (T)(b[0] + ii) * dx - x[0];
+                for (int r = 0; r < 3; r++) {
+                    const T m0 = mass * Cm[3 * r], m1 = mass * Cm[3 * r + 1], m2 = mass * Cm[3 * r + 2];
+                    y[(Y_A + r) * CPAD] = mass * v[r] - dx * (m0 * fr[0] + m1 * fr[1] + m2 * fr[2]);
+                    y[(Y_B + 3 * r) * CPAD] = dx * m0;
+                    y[(Y_B + 3 * r + 1) * CPAD] = dx * m1;
+                    y[(Y_B + 3 * r + 2) * CPAD] = dx * m2;
+                    y[(Y_K + 3 * r) * CPAD] = kf * tau[3 * r];
+                    y[(Y_K + 3 * r + 1) * CPAD] = kf * tau[3 * r + 1];
+                    y[(Y_K + 3 * r + 2) * CPAD] = kf * tau[3 * r + 2];
+                }
+                y[Y_D * CPAD] = dd;
+            }
+            __syncthreads();
+            // particles of one cell are contiguous (sorted by cell inside the block)
+            for (int q = tid; q < cnt; q += NT) {
+                const int e = cellof[q];
+                if (e == 0xff) continue;
+                if (q == 0 || cellof[q - 1] != e) cfirst[e] = (int16_t)q;
+                if (q == cnt - 1 || cellof[q + 1] != e) clast[e] = (int16_t)(q + 1);
+            }
+            __syncthreads();
+            // ---- phase 2: per (cell, stencil x-offset), register accumulators of the thread's 9 nodes
+            if (ii < 3) {
+                T acc[9][NACC];
+#pragma unroll
+                for (int n = 0; n < 9; n++)
+#pragma unroll
+                    for (int f = 0; f < NACC; f++) acc[n][f] = (T)0;
+                const int q1 = clast[c];
+                for (int q = cfirst[c]; q < q1; q++) {
+                    const T* y = pay + pay_slot(q);
+                    T w[3][3], dw[3][3];
+#pragma unroll
+                    for (int e = 0; e < 3; e++) {
+                        const T d0 = y[(Y_F + e) * CPAD];
+                        const T z = (T)1.5 - d0, d1 = d0 - (T)1, zz = d0 - (T)0.5;
+                        w[e][0] = (T)0.5 * z * z;
+                        w[e][1] = (T)0.75 - d1 * d1;
+                        w[e][2] = (T)0.5 * zz * zz;
+                        dw[e][0] = -z;
+                        dw[e][1] = (T)-2 * d1;
+                        dw[e][2] = zz;
+                    }
+                    const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
+                    const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
+                    const T mass = y[Y_M * CPAD];
+                    T Ai[3], B1[3], B2[3], K[9];
+#pragma unroll
+                    for (int r = 0; r < 3; r++) {
+                        Ai[r] = y[(Y_A + r) * CPAD] + (T)ii * y[(Y_B + 3 * r) * CPAD];
+                        B1[r] = y[(Y_B + 3 * r + 1) * CPAD];
+                        B2[r] = y[(Y_B + 3 * r + 2) * CPAD];
+                    }
+#pragma unroll
+                    for (int e = 0; e < 9; e++) K[e] = y[(Y_K + e) * CPAD];
+                    const T dd = y[Y_D * CPAD];
 #pragma unroll
                     for (int jj = 0; jj < 3; jj++) {
-                        const T xm1 = (T)(b[1] + jj) * dx - x[1];
-                        const T wij = w[0][ii] * w[1][jj];
+                        const T wxy = wx * w[1][jj], g1xy = wx * dw[1][jj], g0xy = dwx * w[1][jj];
 #pragma unroll
                         for (int kk = 0; kk < 3; kk++) {
-                            const T xm2 = (T)(b[2] + kk) * dx - x[2];
                             const T wk = w[2][kk];
-                            const T wijk = wij * wk;
-                            const T g0 = inv_dx * dw[0][ii] * w[1][jj] * wk;
-                            const T g1 = inv_dx * w[0][ii] * dw[1][jj] * wk;
-                            const T g2 = inv_dx * wij * dw[2][kk];
-                            T* t = tile + ((l[0] + ii) * TY + (l[1] + jj)) * TZ + (l[2] + kk);
-                            atomicAdd(t, wijk * mass);
+                            const T ww = wxy * wk;
+                            const T g0 = g0xy * wk, g1 = g1xy * wk, g2 = wxy * dw[2][kk];
+                            T* ac = acc[jj * 3 + kk];
+                            ac[0] += mass * ww;
 #pragma unroll
-                            for (int r = 0; r < 3; r++) {
-                                T mv = wijk * (mom[r] + Cm[3 * r] * xm0 + Cm[3 * r + 1] * xm1 + Cm[3 * r + 2] * xm2);
-                                T f = S[3 * r] * g0 + S[3 * r + 1] * g1 + S[3 * r + 2] * g2;
-                                atomicAdd(t + (1 + r) * TN, mv);
-                                atomicAdd(t + (4 + r) * TN, f);
-                            }
+                            for (int r = 0; r < 3; r++)
+                                ac[1 + r] += ww * (Ai[r] + (T)jj * B1[r] + (T)kk * B2[r]) + (K[3 * r] * g0 + K[3 * r + 1] * g1 + K[3 * r + 2] * g2);
                             if (damage) {
-                                atomicAdd(t + 7 * TN, wijk * dd);
-                                atomicAdd(t + 8 * TN, wijk);
+                                ac[4] += dd * ww;
+                                ac[5] += ww;
                             }
                         }
                     }
                 }
+                // ---- phase 3: registers -> shared tile (distinct nodes within a warp, so no contention)
+                if (q1 > cfirst[c]) {
+#pragma unroll
+                    for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+                        for (int kk = 0; kk < 3; kk++) {
+                            T* t = tile + ((cx + ii) * TY + (cy + jj)) * TZ + (cz + kk);
+                            const T* ac = acc[jj * 3 + kk];
+                            for (int f = 0; f < nf; f++) atomicAdd(t + f * TN, ac[f]);
+                        }
+                }
             }
+            __syncthreads();
         }
-        __syncthreads();
         if (!bad_slot) {
             // tile -> global: z columns split at the block boundary (4 + 2 nodes)
-            for (int q = threadIdx.x; q < NACC * TX * TY * 2; q += NT) {
+            for (int q = tid; q < nf * TX * TY * 2; q += NT) {
                 const int half = q & 1, col = q >> 1;
                 const int f = col / (TX * TY), ab = col % (TX * TY), ta = ab / TY, tb = ab % TY;
                 const int ax = ta >= L::sx, ay = tb >= L::sy;
@@ -390,9 +487,8 @@ __global__ void k_grid(StepArgs<T> a)
             const SceneParams<T>& sp = a.scenes[scene];
             T* A = a.acc + (size_t)b * NACC * L::nodes + e;
             T m = A[0];
-            T vv[3] = { A[L::nodes], A[2 * L::nodes], A[3 * L::nodes] };
-            T f[3] = { A[4 * L::nodes], A[5 * L::nodes], A[6 * L::nodes] };
-            T pf = A[7 * L::nodes], pfm = A[8 * L::nodes];
+            T P[3] = { A[L::nodes], A[2 * L::nodes], A[3 * L::nodes] };
+            T pf = A[4 * L::nodes], pfm = A[5 * L::nodes];
 #pragma unroll
             for (int q = 0; q < NACC; q++) A[q * L::nodes] = (T)0;
             T* V = a.vel + (size_t)b * NVEL * L::nodes + e;
@@ -402,10 +498,11 @@ __global__ void k_grid(StepArgs<T> a)
                 L::block_of_page(hk & ((1ULL << 40) - 1), bi, bj, bk);
                 const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
                 const T xi[3] = { (T)(bi * L::sx + lx) * sp.dx, (T)(bj * L::sy + ly) * sp.dx, (T)(bk * L::sz + lz) * sp.dx };
-                const T dt = sp.dt, dt_over_m = dt / m;
+                const T dt = sp.dt;
                 T vi[3];
+                // P = m v + dt f: v + g dt + f dt / m (MpmSimulationBase.cpp:1204-1210)
 #pragma unroll
-                for (int c = 0; c < 3; c++) vi[c] = vv[c] / m + sp.gravity[c] * dt + f[c] * dt_over_m;
+                for (int c = 0; c < 3; c++) vi[c] = P[c] / m + sp.gravity[c] * dt;
                 collide(sp, (T)sp.time, xi, vi);
                 V[0] = vi[0];
                 V[L::nodes] = vi[1];
@@ -536,72 +633,70 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
             const uint32_t pid = P.pid[j];
 #pragma unroll
             for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
-            T dd = 0, sc = 0;
+            // finish the transfer first so the gather accumulators die before the damage update
+            {
+                T Fn[9], A[9];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const T cn = (ca * Bm[3 * r + c] + cb * Bm[3 * c + r]) * D_inv;
+                        Q.f[(P_C + 3 * r + c) * Q.stride + i] = cn;
+                        if (!isfinite(cn)) flags |= FLAG_NONFINITE;
+                        A[3 * r + c] = (r == c ? (T)1 : (T)0) + dt * Gv[3 * r + c];
+                    }
+                mul3(A, F, Fn);
+                bool finite = true;
+#pragma unroll
+                for (int c = 0; c < 9; c++) {
+                    finite = finite && isfinite(Fn[c]);
+                    Q.f[(P_F + c) * Q.stride + i] = Fn[c];
+                }
+                T xn[3], inc2 = 0;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    T inc = dt * pv[c];
+                    inc2 += inc * inc;
+                    xn[c] = x[c] + inc;
+                    Q.f[(P_X + c) * Q.stride + i] = xn[c];
+                    Q.f[(P_V + c) * Q.stride + i] = pv[c];
+                }
+                if (inc2 > dx2) flags |= FLAG_CFL;
+                if (inc2 > half_cfl2) flags |= FLAG_CFL_HALF;
+                if (!finite || !isfinite(inc2)) flags |= FLAG_NONFINITE;
+                // key of the next substep
+                int nb[3];
+                bool in_dom = true;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    nb[c] = base_node(xn[c], inv_dx);
+                    in_dom = in_dom && nb[c] >= 0 && nb[c] < sp.domain_cells - 3;
+                }
+                if (!in_dom) {
+                    flags |= FLAG_OUT_OF_DOMAIN;
+                    nb[0] = nb[1] = nb[2] = 0;
+                }
+                const uint32_t orig = pid & ((1u << L::index_bits) - 1);
+                a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib) | orig;
+            }
+            Q.f[P_M * Q.stride + i] = P.f[P_M * P.stride + j];
+            Q.f[P_V0 * Q.stride + i] = P.f[P_V0 * P.stride + j];
+            Q.pid[i] = pid;
             if (damage) {
-                dd = P.f[P_D * P.stride + j];
-                sc = P.f[P_SC * P.stride + j];
+                // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
+                T dd = P.f[P_D * P.stride + j];
+                const T sc = P.f[P_SC * P.stride + j];
                 const uint32_t mat = pid >> L::index_bits;
                 const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
                 if (mt.damage && mt.model == MODEL_NEOHOOKEAN_BORDEN) {
                     bool fb = false;
                     dd = damage_update(mt, F, dd, lap, sc, dt, fb);
                     if (fb) atomicAdd(&a.st->fallback, 1u);
+                    if (!isfinite(dd)) flags |= FLAG_NONFINITE;
                 }
-            }
-            T Cn[9], Fn[9], A[9];
-#pragma unroll
-            for (int r = 0; r < 3; r++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    Cn[3 * r + c] = (ca * Bm[3 * r + c] + cb * Bm[3 * c + r]) * D_inv;
-                    A[3 * r + c] = (r == c ? (T)1 : (T)0) + dt * Gv[3 * r + c];
-                }
-            mul3(A, F, Fn);
-            T xn[3], inc2 = 0;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                T inc = dt * pv[c];
-                inc2 += inc * inc;
-                xn[c] = x[c] + inc;
-            }
-            if (inc2 > dx2) flags |= FLAG_CFL;
-            if (inc2 > half_cfl2) flags |= FLAG_CFL_HALF;
-            bool finite = isfinite(inc2) && isfinite(dd);
-#pragma unroll
-            for (int c = 0; c < 9; c++) finite = finite && isfinite(Fn[c]) && isfinite(Cn[c]);
-            if (!finite) flags |= FLAG_NONFINITE;
-            // key of the next substep
-            int nb[3];
-            bool in_dom = true;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                nb[c] = base_node(xn[c], inv_dx);
-                in_dom = in_dom && nb[c] >= 0 && nb[c] < sp.domain_cells - 3;
-            }
-            if (!in_dom) {
-                flags |= FLAG_OUT_OF_DOMAIN;
-                nb[0] = nb[1] = nb[2] = 0;
-            }
-            const uint32_t orig = pid & ((1u << L::index_bits) - 1);
-            a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib) | orig;
-            // particle -> sorted slot i of the other buffer
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                Q.f[(P_X + c) * Q.stride + i] = xn[c];
-                Q.f[(P_V + c) * Q.stride + i] = pv[c];
-            }
-#pragma unroll
-            for (int c = 0; c < 9; c++) {
-                Q.f[(P_C + c) * Q.stride + i] = Cn[c];
-                Q.f[(P_F + c) * Q.stride + i] = Fn[c];
-            }
-            Q.f[P_M * Q.stride + i] = P.f[P_M * P.stride + j];
-            Q.f[P_V0 * Q.stride + i] = P.f[P_V0 * P.stride + j];
-            if (damage) {
                 Q.f[P_D * Q.stride + i] = dd;
                 Q.f[P_SC * Q.stride + i] = sc;
             }
-            Q.pid[i] = pid;
         }
         if (flags) raise_flag(a.st, flags);
         __syncthreads();
