@@ -406,32 +406,41 @@ __global__ void __launch_bounds__(P2GShape<T>::NT, 2) k_p2g(StepArgs<T> a)
                     const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
                     const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
                     const T mass = y[Y_M * CPAD];
-                    T Ai[3], B1[3], B2[3], K[9];
+                    const T dd = y[Y_D * CPAD];
+                    T Ai[3], B1[3], B2[3], K0[3], K1[3], K2[3];
 #pragma unroll
                     for (int r = 0; r < 3; r++) {
                         Ai[r] = y[(Y_A + r) * CPAD] + (T)ii * y[(Y_B + 3 * r) * CPAD];
                         B1[r] = y[(Y_B + 3 * r + 1) * CPAD];
                         B2[r] = y[(Y_B + 3 * r + 2) * CPAD];
+                        K0[r] = y[(Y_K + 3 * r) * CPAD];
+                        K1[r] = y[(Y_K + 3 * r + 1) * CPAD];
+                        K2[r] = y[(Y_K + 3 * r + 2) * CPAD];
                     }
-#pragma unroll
-                    for (int e = 0; e < 9; e++) K[e] = y[(Y_K + e) * CPAD];
-                    const T dd = y[Y_D * CPAD];
+                    // node (ii, jj, kk) receives, per momentum component r,
+                    //   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
+                    //   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
 #pragma unroll
                     for (int jj = 0; jj < 3; jj++) {
-                        const T wxy = wx * w[1][jj], g1xy = wx * dw[1][jj], g0xy = dwx * w[1][jj];
+                        const T c0 = wx * w[1][jj], gx = dwx * w[1][jj], gy = wx * dw[1][jj];
+                        T al[3], be[3], ga[3];
+#pragma unroll
+                        for (int r = 0; r < 3; r++) {
+                            al[r] = c0 * (jj ? Ai[r] + (T)jj * B1[r] : Ai[r]) + (K0[r] * gx + K1[r] * gy);
+                            be[r] = c0 * B2[r];
+                            ga[r] = c0 * K2[r];
+                        }
+                        const T mc = mass * c0, dc = dd * c0;
 #pragma unroll
                         for (int kk = 0; kk < 3; kk++) {
-                            const T wk = w[2][kk];
-                            const T ww = wxy * wk;
-                            const T g0 = g0xy * wk, g1 = g1xy * wk, g2 = wxy * dw[2][kk];
+                            const T wk = w[2][kk], dwk = dw[2][kk];
                             T* ac = acc[jj * 3 + kk];
-                            ac[0] += mass * ww;
+                            ac[0] += mc * wk;
 #pragma unroll
-                            for (int r = 0; r < 3; r++)
-                                ac[1 + r] += ww * (Ai[r] + (T)jj * B1[r] + (T)kk * B2[r]) + (K[3 * r] * g0 + K[3 * r + 1] * g1 + K[3 * r + 2] * g2);
+                            for (int r = 0; r < 3; r++) ac[1 + r] += wk * al[r] + (kk ? ((T)kk * wk) * be[r] : (T)0) + dwk * ga[r];
                             if (damage) {
-                                ac[4] += dd * ww;
-                                ac[5] += ww;
+                                ac[4] += dc * wk;
+                                ac[5] += c0 * wk;
                             }
                         }
                     }
@@ -575,61 +584,89 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
 #pragma unroll
             for (int c = 0; c < 3; c++) x[c] = P.f[(P_X + c) * P.stride + j];
             int b[3], l[3];
-            T w[3][3], dw[3][3];
+            T w[3][3], dw[3][3], fr[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 T xs = mul_rn(x[c], inv_dx);
                 b[c] = int_floor(sub_rn(xs, (T)0.5));
                 bspline_w(xs, b[c], w[c], dw[c]);
+                fr[c] = xs - (T)b[c];
                 l[c] = b[c] - s_org[c];
             }
             if (l[0] < 0 || l[0] >= L::sx || l[1] < 0 || l[1] >= L::sy || l[2] < 0 || l[2] >= L::sz) {
                 flags |= FLAG_CAPACITY; // a particle outside its group's block: keys and positions disagree
                 continue;
             }
-            T pv[3] = { 0, 0, 0 }, Bm[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0;
-            const T ii2 = inv_dx * inv_dx;
+            // Separable gather: the stencil weight is wx_i wy_j wz_k, so sums over k, then j, then i give
+            //   pv = sum w v,  M_rc = sum w v_r delta_c,  G_rc = sum v_r (grad w)_c dx,
+            // and the APIC moment sum w v (x_i - x_p)^T = dx (M - pv fr^T) because x_i - x_p = (delta - fr) dx.
+            T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0;
 #pragma unroll
             for (int ii = 0; ii < 3; ii++) {
                 const int tx = l[0] + ii, ax = tx >= L::sx, ex = tx - ax * L::sx;
-                const T xm0 = (T)(b[0] + ii) * dx - x[0];
-                const T ddw = ii == 1 ? (T)-2 : (T)1; // quadratic d2w/dx2 = (1,-2,1)
+                T Si[3] = { 0, 0, 0 }, Ji[3] = { 0, 0, 0 }, Ki[3] = { 0, 0, 0 }, Ui[3] = { 0, 0, 0 }, Ti[3] = { 0, 0, 0 };
+                T lA = 0, lB = 0, lC = 0;
 #pragma unroll
                 for (int jj = 0; jj < 3; jj++) {
                     const int ty = l[1] + jj, ay = ty >= L::sy, ey = ty - ay * L::sy;
-                    const T xm1 = (T)(b[1] + jj) * dx - x[1];
-                    const T wij = w[0][ii] * w[1][jj];
+                    T sj[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 }, pz = 0, p1 = 0;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
                         const int tz = l[2] + kk, az = tz >= L::sz, ez = tz - az * L::sz;
-                        const T xm2 = (T)(b[2] + kk) * dx - x[2];
-                        const T wk = w[2][kk];
-                        const T wijk = wij * wk;
-                        const T g0 = inv_dx * dw[0][ii] * w[1][jj] * wk;
-                        const T g1 = inv_dx * w[0][ii] * dw[1][jj] * wk;
-                        const T g2 = inv_dx * wij * dw[2][kk];
                         const T* nv = sv + (ax * 4 + ay * 2 + az) * NVEL * L::nodes + L::element(ex, ey, ez);
-                        const T v0 = nv[0], v1 = nv[L::nodes], v2 = nv[2 * L::nodes];
-                        const T vv[3] = { v0, v1, v2 };
-                        const T xmw[3] = { xm0 * wijk, xm1 * wijk, xm2 * wijk };
+                        const T wk = w[2][kk], dwk = dw[2][kk];
 #pragma unroll
                         for (int r = 0; r < 3; r++) {
-                            pv[r] += wijk * vv[r];
-                            Bm[3 * r] += vv[r] * xmw[0];
-                            Bm[3 * r + 1] += vv[r] * xmw[1];
-                            Bm[3 * r + 2] += vv[r] * xmw[2];
-                            Gv[3 * r] += vv[r] * g0;
-                            Gv[3 * r + 1] += vv[r] * g1;
-                            Gv[3 * r + 2] += vv[r] * g2;
+                            const T vr = nv[r * L::nodes];
+                            sj[r] += wk * vr;
+                            tj[r] += dwk * vr;
+                            if (kk) uj[r] += ((T)kk * wk) * vr;
                         }
                         if (damage) {
-                            // the reference's 3D Laplacian weights every term with d2w(i) (MpmGrid.h:607-613)
-                            const T Lw = ii2 * ddw * (w[1][jj] * wk + w[0][ii] * wk + w[0][ii] * w[1][jj]);
-                            lap += nv[3 * L::nodes] * Lw;
+                            const T pf = nv[3 * L::nodes];
+                            pz += wk * pf;
+                            p1 += pf;
                         }
                     }
+                    const T wj = w[1][jj], dwj = dw[1][jj];
+#pragma unroll
+                    for (int r = 0; r < 3; r++) {
+                        Si[r] += wj * sj[r];
+                        Ui[r] += dwj * sj[r];
+                        Ti[r] += wj * tj[r];
+                        Ki[r] += wj * uj[r];
+                        if (jj) Ji[r] += ((T)jj * wj) * sj[r];
+                    }
+                    if (damage) {
+                        lA += wj * pz;
+                        lB += pz;
+                        lC += wj * p1;
+                    }
                 }
+                const T wi = w[0][ii], dwi = dw[0][ii];
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+                    pv[r] += wi * Si[r];
+                    if (ii) M[3 * r] += ((T)ii * wi) * Si[r];
+                    M[3 * r + 1] += wi * Ji[r];
+                    M[3 * r + 2] += wi * Ki[r];
+                    Gv[3 * r] += dwi * Si[r];
+                    Gv[3 * r + 1] += wi * Ui[r];
+                    Gv[3 * r + 2] += wi * Ti[r];
+                }
+                // the reference's 3D Laplacian weights every term with d2w(i) = (1,-2,1)(i) (MpmGrid.h:607-613):
+                // sum_jk pf * d2w_i (wy_j wz_k + wx_i wz_k + wx_i wy_j)
+                if (damage) lap += (ii == 1 ? (T)-2 : (T)1) * (lA + wi * (lB + lC));
             }
+            lap *= inv_dx * inv_dx;
+            T Bm[9];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    Bm[3 * r + c] = dx * (M[3 * r + c] - fr[c] * pv[r]);
+                    Gv[3 * r + c] *= inv_dx;
+                }
             const uint32_t pid = P.pid[j];
 #pragma unroll
             for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];

@@ -4,6 +4,7 @@
 #include "common.cuh"
 #include <cmath>
 #include <cfloat>
+#include <limits>
 
 namespace zr {
 
@@ -14,14 +15,12 @@ struct Eps<float> {
     static constexpr float polar_tol = 3e-4f; // Newton stops once a step changes X by less (quadratic phase)
     static constexpr int polar_iters = 12;
     static constexpr float polar_kappa = 1e3f; // condition bound above which FP64 takes over
-    static constexpr int jacobi_sweeps = 6;
 };
 template <>
 struct Eps<double> {
     static constexpr double polar_tol = 1e-8;
     static constexpr int polar_iters = 16;
     static constexpr double polar_kappa = 1e7;
-    static constexpr int jacobi_sweeps = 10;
 };
 
 // correctly rounded multiply / subtract with no contraction: the base node must match the
@@ -298,48 +297,90 @@ ZR_HD bool polar_rotation(const T* F, T* R)
     return true;
 }
 
-// One Jacobi rotation zeroing a_pq of a symmetric 3x3 matrix; a_rp, a_rq are the entries coupling the
-// third index r. Q accumulates the rotations column-wise.
+// Tensile part sigma+ = sum_i <lambda_i>_+ q_i q_i^T of a symmetric 3x3 matrix (the quantity
+// AnisoFractureSimulation.h:240-254 builds from an eigen-decomposition). Eigenvalues come from the
+// trigonometric closed form; at most one eigenvector is needed: with one positive eigenvalue
+// sigma+ = l1 q1 q1^T, with two sigma+ = S - l3 q3 q3^T, each eigenvector taken as the largest cross
+// product of two rows of (S - l I). When that eigenvalue is close to another one, it is also close to
+// zero (the other lies on the far side of zero), so the error of its eigenvector is scaled by a small
+// eigenvalue: sigma+ stays accurate.
 template <class T>
-ZR_HD void jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T* Q, int p, int q)
+ZR_HD void eig_vec_of(const T* S, T l, T* q)
 {
-    T x = apq;
-    if (x == (T)0) return;
-    T theta = (aqq - app) / ((T)2 * x);
-    T t = fabs(theta) > (T)1e15 ? (T)0.5 / theta : (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
-    T c = (T)1 / sqrt(t * t + (T)1), s = t * c;
-    app -= t * x;
-    aqq += t * x;
-    apq = (T)0;
-    T rp = arp, rq = arq;
-    arp = c * rp - s * rq;
-    arq = s * rp + c * rq;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        T qp = Q[3 * k + p], qq = Q[3 * k + q];
-        Q[3 * k + p] = c * qp - s * qq;
-        Q[3 * k + q] = s * qp + c * qq;
+    const T r0[3] = { S[0] - l, S[1], S[2] }, r1[3] = { S[3], S[4] - l, S[5] }, r2[3] = { S[6], S[7], S[8] - l };
+    // the three row cross products; keep the longest (selects, no dynamic indexing)
+    const T a0 = r0[1] * r1[2] - r0[2] * r1[1], a1 = r0[2] * r1[0] - r0[0] * r1[2], a2 = r0[0] * r1[1] - r0[1] * r1[0];
+    const T b0 = r0[1] * r2[2] - r0[2] * r2[1], b1 = r0[2] * r2[0] - r0[0] * r2[2], b2 = r0[0] * r2[1] - r0[1] * r2[0];
+    const T e0 = r1[1] * r2[2] - r1[2] * r2[1], e1 = r1[2] * r2[0] - r1[0] * r2[2], e2 = r1[0] * r2[1] - r1[1] * r2[0];
+    const T na = a0 * a0 + a1 * a1 + a2 * a2, nb = b0 * b0 + b1 * b1 + b2 * b2, ne = e0 * e0 + e1 * e1 + e2 * e2;
+    T q0 = a0, q1 = a1, q2 = a2, nk = na;
+    if (nb > nk) {
+        q0 = b0;
+        q1 = b1;
+        q2 = b2;
+        nk = nb;
     }
+    if (ne > nk) {
+        q0 = e0;
+        q1 = e1;
+        q2 = e2;
+        nk = ne;
+    }
+    if (!(nk > (T)0)) {
+        q[0] = (T)1;
+        q[1] = q[2] = (T)0;
+        return;
+    }
+    const T inv = (T)1 / sqrt(nk);
+    q[0] = q0 * inv;
+    q[1] = q1 * inv;
+    q[2] = q2 * inv;
 }
 
-// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix: S = Q diag(lam) Q^T.
 template <class T>
-ZR_HD void sym_eig3(const T* S, T* lam, T* Q)
+ZR_HD void tension_part(const T* S, T* Sp)
 {
-    T a00 = S[0], a11 = S[4], a22 = S[8], a01 = (T)0.5 * (S[1] + S[3]), a02 = (T)0.5 * (S[2] + S[6]), a12 = (T)0.5 * (S[5] + S[7]);
-#pragma unroll
-    for (int i = 0; i < 9; i++) Q[i] = (i % 4 == 0) ? (T)1 : (T)0;
-    for (int sweep = 0; sweep < Eps<T>::jacobi_sweeps; sweep++) {
-        T off = a01 * a01 + a02 * a02 + a12 * a12;
-        T dg = a00 * a00 + a11 * a11 + a22 * a22;
-        if (off <= (T)1e-30 * dg || off == (T)0) break;
-        jacobi_rot(a00, a11, a01, a02, a12, Q, 0, 1);
-        jacobi_rot(a00, a22, a02, a01, a12, Q, 0, 2);
-        jacobi_rot(a11, a22, a12, a01, a02, Q, 1, 2);
+    const T s00 = S[0], s11 = S[4], s22 = S[8];
+    const T s01 = (T)0.5 * (S[1] + S[3]), s02 = (T)0.5 * (S[2] + S[6]), s12 = (T)0.5 * (S[5] + S[7]);
+    const T Ssym[9] = { s00, s01, s02, s01, s11, s12, s02, s12, s22 };
+    const T q = (s00 + s11 + s22) * ((T)1 / (T)3);
+    const T p1 = s01 * s01 + s02 * s02 + s12 * s12;
+    const T a = s00 - q, b = s11 - q, c = s22 - q;
+    const T p2 = a * a + b * b + c * c + (T)2 * p1;
+    T l1, l2, l3;
+    const T p = sqrt(p2 * ((T)1 / (T)6));
+    if (!(p > std::numeric_limits<T>::epsilon() * (fabs(q) + std::numeric_limits<T>::min()))) {
+        l1 = l2 = l3 = q; // a multiple of the identity
     }
-    lam[0] = a00;
-    lam[1] = a11;
-    lam[2] = a22;
+    else {
+        const T ip = (T)1 / p;
+        const T B00 = a * ip, B11 = b * ip, B22 = c * ip, B01 = s01 * ip, B02 = s02 * ip, B12 = s12 * ip;
+        T r = (T)0.5 * (B00 * (B11 * B22 - B12 * B12) - B01 * (B01 * B22 - B12 * B02) + B02 * (B01 * B12 - B11 * B02));
+        r = r < (T)-1 ? (T)-1 : (r > (T)1 ? (T)1 : r);
+        const T phi = acos(r) * ((T)1 / (T)3);
+        l1 = q + (T)2 * p * cos(phi);
+        l3 = q + (T)2 * p * cos(phi + (T)2.0943951023931954923);
+        l2 = (T)3 * q - l1 - l3;
+    }
+    if (l3 >= (T)0) { // all tensile
+        for (int i = 0; i < 9; i++) Sp[i] = Ssym[i];
+        return;
+    }
+    if (l1 <= (T)0) { // all compressive
+        for (int i = 0; i < 9; i++) Sp[i] = (T)0;
+        return;
+    }
+    T v[3];
+    if (l2 <= (T)0) { // one tensile direction
+        eig_vec_of(Ssym, l1, v);
+        for (int r0 = 0; r0 < 3; r0++)
+            for (int c0 = 0; c0 < 3; c0++) Sp[3 * r0 + c0] = l1 * v[r0] * v[c0];
+    }
+    else { // two tensile directions: remove the compressive one
+        eig_vec_of(Ssym, l3, v);
+        for (int r0 = 0; r0 < 3; r0++)
+            for (int c0 = 0; c0 < 3; c0++) Sp[3 * r0 + c0] = Ssym[3 * r0 + c0] - l3 * v[r0] * v[c0];
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -395,15 +436,9 @@ ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, 
     T tau[9];
     tau_nhb(mt, F, (T)1, tau);
     T invJ = (T)1 / det3(F);
-    T S[9], lam[3], Q[9];
+    T S[9], sp[9];
     for (int i = 0; i < 9; i++) S[i] = tau[i] * invJ; // undegraded Cauchy stress
-    sym_eig3(S, lam, Q);
-    T sp[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-    for (int e = 0; e < 3; e++) {
-        T l = lam[e] > (T)0 ? lam[e] : (T)0; // Macaulay bracket of the principal stress
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) sp[3 * r + c] += l * (Q[3 * r + e] * Q[3 * c + e]);
-    }
+    tension_part(S, sp); // sum of Macaulay-bracketed principal stresses times their projectors
     T R[9];
     fallback = polar_rotation(F, R);
     T a[3] = { R[0], R[3], R[6] }; // R e1
