@@ -1,0 +1,35 @@
+"""The C++ shim (include/ziran_gb300.hpp) compiles against the C ABI and links to the in-tree library; on a
+GPU the demo scene runs and conserves momentum up to the gravity impulse."""
+import os
+import subprocess
+
+import pytest
+
+import ziran2020_gb300 as zr
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "shim_demo.cpp")
+
+
+def build_demo(tmp_path):
+    lib = zr.library_path()
+    exe = str(tmp_path / "shim_demo")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe, lib,
+                           "-Wl,-rpath," + os.path.dirname(lib)])
+    return exe
+
+
+def test_shim_compiles_and_links(tmp_path):
+    zr.load_library()
+    assert os.path.exists(build_demo(tmp_path))
+
+
+@pytest.mark.gpu
+def test_shim_demo_runs(tmp_path):
+    exe = build_demo(tmp_path)
+    out = subprocess.check_output([exe], text=True).split()
+    n, t, py = int(out[1]), float(out[3]), float(out[5])
+    assert n == 4096
+    assert abs(t - 20 * 1e-4) < 1e-9
+    m_total = n * 1000 * (1 / 64) ** 3 / 8
+    assert abs(py - m_total * (-1.0 - 9.8 * 20e-4)) < 1e-4 * m_total
