@@ -191,6 +191,25 @@ int zr_batch_stats(zr_batch* b, int64_t* launches_per_step, int64_t* device_byte
 const char* zr_batch_last_error(zr_batch* b);
 double zr_batch_last_step_ms(zr_batch* b);
 
+/* ============================== binning into caller memory, no device allocation ==============================
+ * No counterpart in the reference: it is the binning of MpmSimulationBase::sortParticlesAndPolluteGrid
+ * (MpmSimulationBase.cpp:1531-1573) offered to callers that may not allocate device memory while they
+ * run (a host that reserves one arena at start-up and forbids cudaMalloc afterwards, a loop with a fixed
+ * memory budget, a callback inside another runtime whose device memory is accounted by that runtime).
+ * Inputs and outputs are device pointers owned by the caller: x holds n*3 coordinates of the precision's
+ * type (xyz per particle); sorted_keys receives the n keys in the reference's layout in ascending order,
+ * order the n original indices in that order, group_first the first sorted index of every SPGrid block
+ * (capacity n); *n_groups (host) the number of blocks. All scratch lives in one static device array of
+ * ZR_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; n above ZR_NOALLOC_MAX_PARTICLES is
+ * rejected with ZR_ERR_ARG. The first call on a device resolves that array's address and sizes the
+ * sort (no allocation): make it before any stream capture. Calls share the array, so calls that overlap
+ * on the GPU (different streams or threads) race; serialise them. Returns ZR_ERR_OUT_OF_DOMAIN when a
+ * base node lies outside [0, domain_cells) (0 = the full SPGrid range). The call synchronises `stream`. */
+#define ZR_NOALLOC_MAX_PARTICLES (1 << 20)
+#define ZR_NOALLOC_SCRATCH_BYTES (16u << 20)
+int zr_bin_device_noalloc(int precision, int64_t n, const void* x, double dx, int32_t domain_cells, uint64_t* sorted_keys, int32_t* order,
+    int32_t* group_first, int64_t* n_groups, void* stream);
+
 /* library version string */
 const char* zr_version(void);
 

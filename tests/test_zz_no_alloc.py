@@ -1,0 +1,76 @@
+"""GPU: the binning entry point that allocates no device memory (zr_bin_device_noalloc).
+
+It serves callers that may not allocate device memory while they run (a host that reserved one arena at
+start-up, a loop with a fixed budget, a callback inside another runtime); all its scratch is a static
+device array shared by every call. This file is collected last so that a failure here comes after every
+other test has run. Its output must equal, bit for bit, the binning of the allocating scene API
+(zr_scene_binning) on the same positions, on two consecutive calls (the second smaller than the first,
+so stale scratch from the first call would show up)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import ziran2020_gb300 as zr
+
+pytestmark = pytest.mark.gpu
+
+
+def positions(seed, n_side, dx, origin):
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(n_side)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    x = (g + rng.random(g.shape)) * (dx / 2) + np.asarray(origin)
+    rng.shuffle(x)
+    return x
+
+
+def scene_binning(prec, x, dx):
+    s = zr.Scene(prec)
+    s.set_params(dx, 1e-4)
+    n = len(x)
+    first = s.add_particles(x, np.ones(n), np.ones(n))
+    s.add_corotated(first, n, 1e4, 0.3)
+    return s.binning()
+
+
+def noalloc_binning(prec, x, dx):
+    import torch
+
+    L = zr.load_library()
+    n = len(x)
+    dtype = torch.float32 if prec == zr.F32 else torch.float64
+    xd = torch.tensor(np.ascontiguousarray(x).reshape(-1), dtype=dtype, device="cuda")
+    keys = torch.empty(n, dtype=torch.int64, device="cuda")
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    first = torch.empty(n, dtype=torch.int32, device="cuda")
+    ng = C.c_int64(-1)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = L.zr_bin_device_noalloc(prec, n, C.c_void_p(xd.data_ptr()), dx, 0, C.c_void_p(keys.data_ptr()), C.c_void_p(order.data_ptr()),
+                                 C.c_void_p(first.data_ptr()), C.byref(ng), C.c_void_p(stream))
+    assert rc == zr.ZR_OK, rc
+    return {"sorted": keys.cpu().numpy().view(np.uint64), "order": order.cpu().numpy(), "group_first": first.cpu().numpy()[: ng.value]}
+
+
+@pytest.mark.parametrize("prec", [zr.F32, zr.F64])
+def test_noalloc_binning_equals_scene_binning_on_two_calls(prec):
+    dx = 1 / 128
+    cases = [positions(1, 40, dx, (0.2, 0.3, 0.25)), positions(2, 23, dx, (0.41, 0.22, 0.5))]  # 64000 then 12167 particles
+    for x in cases:
+        if prec == zr.F32:
+            x = x.astype(np.float32).astype(np.float64)  # both paths bin the same float values
+        want = scene_binning(prec, x, dx)
+        got = noalloc_binning(prec, x, dx)
+        assert np.array_equal(got["sorted"], want["sorted"])
+        assert np.array_equal(got["order"], want["order"])
+        assert np.array_equal(got["group_first"], want["group_first"])
+
+
+def test_noalloc_rejects_sizes_beyond_its_static_scratch():
+    import torch
+
+    L = zr.load_library()
+    big = (1 << 20) + 1
+    dummy = torch.empty(16, dtype=torch.float32, device="cuda")
+    p = C.c_void_p(dummy.data_ptr())
+    ng = C.c_int64()
+    assert L.zr_bin_device_noalloc(zr.F32, big, p, 1 / 64, 0, p, p, p, C.byref(ng), None) == zr.ZR_ERR_ARG

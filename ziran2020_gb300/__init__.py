@@ -110,6 +110,7 @@ def load_library(build_if_needed=True):
         "zr_batch_stats": (i32, [vp, P(i64), P(i64), P(i64)]),
         "zr_batch_last_error": (C.c_char_p, [vp]),
         "zr_version": (C.c_char_p, []),
+        "zr_bin_device_noalloc": (i32, [i32, i64, vp, d, C.c_int32, vp, vp, vp, P(i64), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

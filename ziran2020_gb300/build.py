@@ -14,7 +14,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libziran_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-diag-suppress", "20050"]
-SOURCES = ["engine_f32.cu", "engine_f64.cu", "capi.cpp"]
+SOURCES = ["engine_f32.cu", "engine_f64.cu", "capi.cpp", "noalloc.cu"]
 
 
 def _nvcc():
