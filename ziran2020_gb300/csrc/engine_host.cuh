@@ -31,7 +31,7 @@ template <class T>
 class Engine final : public EngineBase {
     using L = typename LayoutOf<T>::type;
     static constexpr int NT_P2G = P2GShape<T>::NT;
-    static constexpr int NT_G2P = 256;
+    static constexpr int NT_G2P = 128;
     static constexpr int GRAPH_K = 8; // substeps per multi-step graph (even: returns to the same buffer)
 
 public:
@@ -115,11 +115,14 @@ public:
             max_domain = std::max(max_domain, dc);
         }
         if (N >= (int64_t)0xffffffffLL) return arg("batch too large");
+        models_ = 0;
+        for (auto& sp : h_scenes_)
+            for (int k = 0; k < sp.n_materials; k++) models_ |= sp.materials[k].model == MODEL_COROTATED ? 1 : 2;
         N_ = (uint32_t)N;
         // key layout
         int cb = bitlen((uint64_t)(max_domain + 2 * std::max(L::sx, std::max(L::sy, L::sz)) - 1));
         uint32_t maxc = (1u << cb) - 1;
-        kl_.ib = std::max(1, bitlen((uint64_t)(max_n - 1)));
+        kl_.ib = 0; // hot-path keys carry no particle index: k_cellfix orders each cell by original index
         kl_.cp = bitlen(L::offset(maxc, maxc, maxc)) - L::data_bits;
         kl_.sb = bitlen((uint64_t)(h_scenes_.size() - 1));
         kl_.block_bits = L::block_bits;
@@ -379,6 +382,7 @@ public:
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
             StepArgs<T> a = args(cur_);
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
+            k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[cur_], N_);
             ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
             k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
             ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
@@ -391,8 +395,10 @@ public:
         (void)a;
         const uint32_t G = hst_->n_groups, B = std::min(hst_->n_blocks, b_cap_);
         std::vector<uint64_t> sk(n), bk(B);
-        std::vector<uint32_t> gs(G);
+        std::vector<uint32_t> gs(G), vs(n), pd(n);
         ZR_CUDA(cudaMemcpy(sk.data(), keys_sorted_, 8 * n, cudaMemcpyDeviceToHost));
+        ZR_CUDA(cudaMemcpy(vs.data(), vals_sorted_, 4 * n, cudaMemcpyDeviceToHost));
+        ZR_CUDA(cudaMemcpy(pd.data(), pid_[cur_], 4 * n, cudaMemcpyDeviceToHost));
         ZR_CUDA(cudaMemcpy(gs.data(), g_start_, 4 * (size_t)G, cudaMemcpyDeviceToHost));
         ZR_CUDA(cudaMemcpy(bk.data(), b_key_, 8 * (size_t)B, cudaMemcpyDeviceToHost));
         // restore a clean grid for the next substep
@@ -405,7 +411,7 @@ public:
         const uint64_t cpmask = (1ULL << kl_.cp) - 1;
         for (int64_t i = 0; i < cnt; i++) {
             uint64_t k = sk[first + i];
-            uint32_t o = kl_.orig(k);
+            uint32_t o = pd[vs[first + i]] & ((1u << L::index_bits) - 1); // original index from the particle id
             keys[i] = (((k >> kl_.ib) & cpmask) << L::index_bits) | o; // the reference's key layout
             order[i] = (int32_t)o;
         }
@@ -461,6 +467,8 @@ private:
     void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
     int occ_p2g_ = 1, occ_g2p_ = 1;
+    int occ_p2g_m_[3] = { 1, 1, 1 };
+    int models_ = 3; // bit 0: a corotated material is present, bit 1: a Neo-Hookean (Borden) material
     bool graphs_on_ = true, timing_ = false;
     cudaGraphExec_t g1_[2] = { nullptr, nullptr }, gk_[2] = { nullptr, nullptr };
     int launches_per_step_ = 0;
@@ -489,8 +497,14 @@ private:
             init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
             return;
         }
-        cudaFuncSetAttribute(k_p2g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p2g_, k_p2g<T>, NT_P2G, P2GShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k_p2g<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k_p2g<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k_p2g<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
+        for (int m = 0; m < 3; m++) {
+            int o = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, m == 0 ? k_p2g<T, 1> : (m == 1 ? k_p2g<T, 2> : k_p2g<T, 3>), NT_P2G, P2GShape<T>::dyn_bytes);
+            occ_p2g_m_[m] = std::max(1, o);
+        }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_, k_g2p<T, NT_G2P>, NT_G2P, 0);
         occ_p2g_ = std::max(1, occ_p2g_);
         occ_g2p_ = std::max(1, occ_g2p_);
@@ -615,12 +629,18 @@ private:
         const int64_t n = N_;
         if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
         ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
+        k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[parity], N_);
         ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
-        k_p2g<T><<<nsm_ * occ_p2g_, NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
+        if (models_ == 1)
+            k_p2g<T, 1><<<nsm_ * occ_p2g_m_[0], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
+        else if (models_ == 2)
+            k_p2g<T, 2><<<nsm_ * occ_p2g_m_[1], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
+        else
+            k_p2g<T, 3><<<nsm_ * occ_p2g_m_[2], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
         k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));

@@ -155,8 +155,36 @@ __global__ void k_keys(Pool<T> p, const SceneParams<T>* scenes, int n_scenes, ui
             raise_flag(st, FLAG_OUT_OF_DOMAIN);
             b[0] = b[1] = b[2] = 0;
         }
-        uint32_t orig = p.pid[i] & ((1u << L::index_bits) - 1);
-        keys[i] = ((uint64_t)lo << (kl.cp + kl.ib)) | ((L::offset(b[0], b[1], b[2]) >> L::data_bits) << kl.ib) | orig;
+        keys[i] = ((uint64_t)lo << (kl.cp + kl.ib)) | ((L::offset(b[0], b[1], b[2]) >> L::data_bits) << kl.ib);
+    }
+}
+
+// The hot-path keys hold (scene, page, cell) only, so the radix sort needs 4 passes instead of 7; a
+// stable sort of storage-ordered input leaves the particles of one cell in their previous order. This pass
+// restores the reference's order inside each cell (ascending original index, the low bits of the
+// reference key, MpmSimulationBase.cpp:1547-1552) with an insertion sort per run of equal keys; runs are
+// short (~8) and nearly sorted (a cell keeps most of its particles from one substep to the next).
+template <class T>
+__global__ void k_cellfix(const uint64_t* ks, uint32_t* vals, const uint32_t* pid, uint32_t n)
+{
+    using L = typename LayoutOf<T>::type;
+    const uint32_t mask = (1u << L::index_bits) - 1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = ks[i];
+        if (i > 0 && ks[i - 1] == k) continue; // not the first of its run
+        uint32_t e = i + 1;
+        while (e < n && ks[e] == k) e++;
+        for (uint32_t q = i + 1; q < e; q++) {
+            const uint32_t v = vals[q], o = pid[v] & mask;
+            uint32_t r = q;
+            while (r > i) {
+                const uint32_t u = vals[r - 1];
+                if ((pid[u] & mask) <= o) break;
+                vals[r] = u;
+                r--;
+            }
+            vals[r] = v;
+        }
     }
 }
 
@@ -259,7 +287,9 @@ struct P2GShape {
 
 __device__ __forceinline__ int pay_slot(int q) { return q + (q >> 3); } // bank swizzle: cells hold ~8 particles
 
-template <class T>
+// MODELS: bit 0 = fixed corotated present in the batch, bit 1 = Neo-Hookean (Borden) present; a batch
+// with one model kind runs a kernel without the other model's code (fewer registers).
+template <class T, int MODELS>
 __global__ void __launch_bounds__(P2GShape<T>::NT, 2) k_p2g(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
@@ -337,7 +367,7 @@ __global__ void __launch_bounds__(P2GShape<T>::NT, 2) k_p2g(StepArgs<T> a)
                 const uint32_t mat = P.pid[j] >> L::index_bits;
                 const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
                 T tau[9];
-                if (mt.model == MODEL_COROTATED) {
+                if (MODELS == 1 || (MODELS == 3 && mt.model == MODEL_COROTATED)) {
                     if (tau_corotated(mt, F, tau)) atomicAdd(&a.st->fallback, 1u);
                 }
                 else
@@ -536,10 +566,10 @@ __global__ void k_grid(StepArgs<T> a)
 // G2P
 // ---------------------------------------------------------------------------------------------------
 template <class T, int NT>
-__global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
+__global__ void __launch_bounds__(NT, 4) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    __shared__ T sv[8 * NVEL * L::nodes];
+    __shared__ __align__(16) T sv[8 * NVEL * L::nodes];
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
     if (aborted_cta(a.st)) return;
     const uint32_t G = a.st->n_groups;
@@ -563,11 +593,15 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
             }
         }
         __syncthreads();
-        // stage the velocities of the 8 neighbouring blocks
-        for (int q = threadIdx.x; q < 8 * NVEL * L::nodes; q += NT) {
-            int d = q / (NVEL * L::nodes), r = q % (NVEL * L::nodes);
-            int slot = s_nbr[d];
-            sv[q] = slot >= 0 ? a.vel[(size_t)slot * NVEL * L::nodes + r] : (T)0;
+        // stage the velocities of the 8 neighbouring blocks (1 KiB contiguous per block, 16-byte loads)
+        {
+            constexpr int V4 = NVEL * L::nodes * (int)sizeof(T) / 16; // 16-byte words per block
+            uint4* dst = reinterpret_cast<uint4*>(sv);
+            for (int q = threadIdx.x; q < 8 * V4; q += NT) {
+                const int d = q / V4, r = q % V4;
+                const int slot = s_nbr[d];
+                dst[q] = slot >= 0 ? reinterpret_cast<const uint4*>(a.vel + (size_t)slot * NVEL * L::nodes)[r] : make_uint4(0, 0, 0, 0);
+            }
         }
         __syncthreads();
         const SceneParams<T>& sp = a.scenes[s_scene];
@@ -580,9 +614,16 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
         uint32_t flags = 0;
         for (uint32_t i = start + threadIdx.x; i < end; i += NT) {
             const uint32_t j = a.vals_sorted[i];
+            // every particle load is issued here, so one memory latency covers them all
             T x[3], F[9];
 #pragma unroll
             for (int c = 0; c < 3; c++) x[c] = P.f[(P_X + c) * P.stride + j];
+#pragma unroll
+            for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
+            const uint32_t pid = P.pid[j];
+            const T pm = P.f[P_M * P.stride + j], pV0 = P.f[P_V0 * P.stride + j];
+            T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
+            const T sc = damage ? P.f[P_SC * P.stride + j] : (T)0;
             int b[3], l[3];
             T w[3][3], dw[3][3], fr[3];
 #pragma unroll
@@ -667,9 +708,6 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
                     Bm[3 * r + c] = dx * (M[3 * r + c] - fr[c] * pv[r]);
                     Gv[3 * r + c] *= inv_dx;
                 }
-            const uint32_t pid = P.pid[j];
-#pragma unroll
-            for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
             // finish the transfer first so the gather accumulators die before the damage update
             {
                 T Fn[9], A[9];
@@ -713,16 +751,13 @@ __global__ void __launch_bounds__(NT) k_g2p(StepArgs<T> a)
                     flags |= FLAG_OUT_OF_DOMAIN;
                     nb[0] = nb[1] = nb[2] = 0;
                 }
-                const uint32_t orig = pid & ((1u << L::index_bits) - 1);
-                a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib) | orig;
+                a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib);
             }
-            Q.f[P_M * Q.stride + i] = P.f[P_M * P.stride + j];
-            Q.f[P_V0 * Q.stride + i] = P.f[P_V0 * P.stride + j];
+            Q.f[P_M * Q.stride + i] = pm;
+            Q.f[P_V0 * Q.stride + i] = pV0;
             Q.pid[i] = pid;
             if (damage) {
                 // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
-                T dd = P.f[P_D * P.stride + j];
-                const T sc = P.f[P_SC * P.stride + j];
                 const uint32_t mat = pid >> L::index_bits;
                 const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
                 if (mt.damage && mt.model == MODEL_NEOHOOKEAN_BORDEN) {
