@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="aniso_slab_dx256", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="aniso_slab_dx256", choices=sorted(WORKLOADS) + ["batch256", "serve"])
+    ap.add_argument("--rates", default="4,16,64", help="serve: Poisson arrival rates (requests/s) to sweep")
+    ap.add_argument("--requests", type=int, default=48, help="serve: requests per arrival rate")
+    ap.add_argument("--tick", type=int, default=25, help="serve: substeps per serving tick")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--fp64-steps", type=int, default=10)
@@ -221,10 +224,130 @@ def _config(args):
             "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{args.gpus}"}
 
 
+def run_batch(args, world, rank):
+    """256 independent elastic boxes (N log-uniform in 5k-400k, E ~ U(5e3, 5e4), centre ~ U[0.3,0.7]^3,
+    v0 ~ U[-1,1]^3; dx = 1/64, dt = 1e-4) advanced together: one launch per kernel for the whole batch."""
+    import ziran2020_gb300 as zr
+    from ziran2020_gb300 import workloads
+
+    recs = workloads.batch_recipes(seed=20200713 + rank)
+    n = workloads.total_particles(recs)
+    b = zr.Batch(zr.F32)
+    for r in recs:
+        b.add_recipe(r)
+    b.commit()
+    clocks = ClockSampler()
+    clocks.start()
+    b.step(args.warmup)
+    barrier(world)
+    b.step(args.steps)
+    ms = b.last_step_ms
+    barrier(world)
+    clock_info = clocks.stop()
+    ms_max = allreduce_max(world, ms)
+    value = allreduce_sum(world, n) * args.steps / (ms_max / 1e3)
+    stats = b.stats()
+    b.set_timing(True)
+    b.step(min(args.steps, 20))
+    phases, ksteps = b.timing()
+    b.set_timing(False)
+    per = {k: v / ksteps for k, v in phases.items()}
+    peak, peak_kind = measured_peaks()
+    blocks = None
+    alg = algorithmic_bytes(4, n, 0, 64, False)  # particle bytes only: the batch reports no block count
+    dom = max(("p2g", "g2p"), key=lambda k: per[k])
+    achieved = alg[dom] / (per[dom] / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "traffic": profiled_traffic(dom, "batch256"),
+            "algorithmic_bytes": alg[dom], "kernel_ms": round(per[dom], 4), "phase_ms_per_substep": {k: round(v, 4) for k, v in per.items()},
+            "note": "algorithmic bytes count particle traffic only (grid nodes excluded)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import pyoracle as po
+        import scenes
+
+        desc = scenes.elastic_box(size=0.25, dx=1 / 64)
+        o = scenes.oracle_scene(desc, 8)
+        ns = len(desc["m"])
+        o.step(1)
+        t0 = time.perf_counter()
+        o.step(20)
+        el = time.perf_counter() - t0
+        cpu = {"value": ns * 20 / el, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
+               "sample": f"one {ns}-particle elastic box of the family (dx=1/64), 20 substeps; the batch would run its scenes one by one"}
+    cfg = {"workload": "batch256", "scenes": len(recs), "particles": int(n), "substeps_timed": args.steps, "precision_path": "fp32",
+           "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{world}"}
+    line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded recipe family)", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "note": "measured on the single-scene workload"},
+            "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
+            "clocks": clock_info, "fp64_fallbacks": stats["fallbacks"]}
+    return line if rank == 0 else None
+
+
+def run_serve(args, world, rank):
+    """Poisson stream of scene-advance requests (elastic or AnisoMPM family, 10k-2M particles log-uniform,
+    50-500 substeps uniform), FP32, state resident on the device, admission by a 60 GB budget; p50/p99
+    request latency (submit -> result on the host) and aggregate particle-substeps/s per arrival rate."""
+    import numpy as np
+
+    import ziran2020_gb300 as zr
+    from ziran2020_gb300 import workloads
+
+    sweep = []
+    for ri, lam in enumerate(float(r) for r in args.rates.split(",")):
+        reqs = workloads.request_stream(seed=4242 + 17 * ri + 1000 * rank, count=args.requests)
+        built = []
+        for r, steps in reqs:
+            sc = zr.Scene(zr.F32)
+            sc.from_recipe(r)  # host-side scene construction happens before the clock starts
+            built.append((sc, steps, zr.recipe_count(r)))
+        arrivals = np.cumsum(np.random.default_rng(99 + ri).exponential(1.0 / lam, len(reqs)))
+        sv = zr.Server(zr.F32, budget_bytes=60e9, tick_substeps=args.tick, max_scenes=256)
+        ids, k = [], 0
+        t0 = time.perf_counter()
+        while True:
+            now = time.perf_counter() - t0
+            while k < len(built) and arrivals[k] <= now:
+                ids.append(sv.submit_scene(built[k][0], built[k][1]))
+                k += 1
+            running, queued, _ = sv.tick()
+            if k == len(built) and running == 0 and queued == 0:
+                break
+            if running == 0 and queued == 0 and k < len(built):
+                time.sleep(max(0.0, arrivals[k] - (time.perf_counter() - t0)))
+        wall = time.perf_counter() - t0
+        lats = np.array([sv.request(i)["latency_s"] for i in ids])
+        st = sv.stats()
+        ps = float(sum(n * steps for _, steps, n in built))
+        sweep.append({"rate_per_s": lam, "requests": len(ids), "p50_latency_s": float(np.percentile(lats, 50)),
+                      "p99_latency_s": float(np.percentile(lats, 99)), "particle_substeps": ps, "makespan_s": wall,
+                      "throughput": ps / wall, "device_throughput": st["particle_substeps"] / (st["device_ms"] / 1e3),
+                      "peak_device_bytes": st["device_bytes"]})
+        del sv, built
+    best = max(sweep, key=lambda e: e["throughput"])
+    cfg = {"workload": "serve", "requests_per_rate": args.requests, "rates_per_s": [e["rate_per_s"] for e in sweep], "budget_bytes": 60e9,
+           "tick_substeps": args.tick, "precision_path": "fp32", "parallelism": f"replicas x{world}"}
+    line = {"metric": "particle-substeps/sec", "value": allreduce_sum(world, best["throughput"]), "unit": "particle-substeps/s",
+            "n_gpus": world, "steps": None, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request stream)", "config": cfg, "serving": sweep,
+            "p50_latency_s": best["p50_latency_s"], "p99_latency_s": best["p99_latency_s"]}
+    return line if rank == 0 else None
+
+
 def run_ours(args, world, rank):
     import numpy as np
 
     import ziran2020_gb300 as zr
+
+    if args.workload == "batch256":
+        return run_batch(args, world, rank)
+    if args.workload == "serve":
+        return run_serve(args, world, rank)
 
     kind, over = WORKLOADS[args.workload]
     r = zr.recipe(kind, seed=12345 + rank, **over)

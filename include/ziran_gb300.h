@@ -191,6 +191,29 @@ int zr_batch_stats(zr_batch* b, int64_t* launches_per_step, int64_t* device_byte
 const char* zr_batch_last_error(zr_batch* b);
 double zr_batch_last_step_ms(zr_batch* b);
 
+/* ================================ serving loop: continuous batching of requests ================================
+ * A request is a scene (a recipe or a built scene description) and a number of substeps. zr_server_tick
+ * admits queued requests in arrival order while the device-memory budget and max_scenes allow, re-forms
+ * the batch (resident scenes keep their state on the device), advances every resident scene by
+ * min(tick_substeps, fewest remaining substeps) in one batched substep sequence and retires finished
+ * requests (their final x, v, C, F, d are copied to the host). No counterpart in the reference, whose
+ * driver runs one scene per process (Projects/anisofracture/anisofracture.cpp:25-139). */
+int zr_server_create(int precision, double budget_bytes, int tick_substeps, int max_scenes, zr_server** out);
+int zr_server_destroy(zr_server* sv);
+int zr_server_submit_recipe(zr_server* sv, const zr_scene_recipe* r, int substeps, int64_t* id);
+/* takes the particles of a scene that has not stepped (the scene handle is left empty) */
+int zr_server_submit_scene(zr_server* sv, zr_scene* s, int substeps, int64_t* id);
+/* *running / *queued: requests resident / waiting after the tick; *finished: requests completed by it */
+int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished);
+/* state: 0 queued, 1 running, 2 done, 3 failed; latency (s) is submit -> completion, -1 before completion */
+int zr_server_request(zr_server* sv, int64_t id, int* state, double* latency_s, int64_t* particles, int* substeps);
+/* final field of a finished request (x, v, C, F or d) in the request's particle order */
+int zr_server_result(zr_server* sv, int64_t id, int field, void* out, int dtype);
+int zr_server_release(zr_server* sv, int64_t id);
+/* particle-substeps advanced, device time of the batched substeps (ms), device bytes held */
+int zr_server_stats(zr_server* sv, double* particle_substeps, double* device_ms, int64_t* device_bytes);
+const char* zr_server_last_error(zr_server* sv);
+
 /* ============================== binning into caller memory, no device allocation ==============================
  * No counterpart in the reference: it is the binning of MpmSimulationBase::sortParticlesAndPolluteGrid
  * (MpmSimulationBase.cpp:1531-1573) offered to callers that may not allocate device memory while they

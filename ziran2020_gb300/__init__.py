@@ -110,6 +110,16 @@ def load_library(build_if_needed=True):
         "zr_batch_stats": (i32, [vp, P(i64), P(i64), P(i64)]),
         "zr_batch_last_error": (C.c_char_p, [vp]),
         "zr_version": (C.c_char_p, []),
+        "zr_server_create": (i32, [i32, d, i32, i32, P(vp)]),
+        "zr_server_destroy": (i32, [vp]),
+        "zr_server_submit_recipe": (i32, [vp, P(Recipe), i32, P(i64)]),
+        "zr_server_submit_scene": (i32, [vp, vp, i32, P(i64)]),
+        "zr_server_tick": (i32, [vp, P(i32), P(i32), P(i32)]),
+        "zr_server_request": (i32, [vp, i64, P(i32), P(d), P(i64), P(i32)]),
+        "zr_server_result": (i32, [vp, i64, i32, vp, i32]),
+        "zr_server_release": (i32, [vp, i64]),
+        "zr_server_stats": (i32, [vp, P(d), P(d), P(i64)]),
+        "zr_server_last_error": (C.c_char_p, [vp]),
         "zr_bin_device_noalloc": (i32, [i32, i64, vp, d, C.c_int32, vp, vp, vp, P(i64), vp]),
     }
     for name, (res, args) in sig.items():
@@ -384,6 +394,71 @@ class Batch:
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self.L.zr_batch_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return {"launches_per_step": a.value, "device_bytes": b.value, "fallbacks": c.value}
+
+
+class Server:
+    """Continuous-batching request loop: requests (scene recipe + substeps) are admitted by a device-memory
+    budget, advanced together with the resident scenes, and retired with their final state on the host."""
+
+    QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, precision=F32, budget_bytes=60e9, tick_substeps=10, max_scenes=256):
+        self.L = load_library()
+        self.h = C.c_void_p()
+        rc = self.L.zr_server_create(precision, float(budget_bytes), tick_substeps, max_scenes, C.byref(self.h))
+        if rc:
+            raise ZrError(rc, "bad server configuration")
+
+    def _check(self, rc):
+        if rc:
+            raise ZrError(rc, self.L.zr_server_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if self.h:
+            self.L.zr_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, r, substeps):
+        rid = C.c_int64()
+        self._check(self.L.zr_server_submit_recipe(self.h, C.byref(r), substeps, C.byref(rid)))
+        return rid.value
+
+    def submit_scene(self, scene, substeps):
+        rid = C.c_int64()
+        self._check(self.L.zr_server_submit_scene(self.h, scene.h, substeps, C.byref(rid)))
+        return rid.value
+
+    def tick(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.zr_server_tick(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def request(self, rid):
+        st, lat, n, k = C.c_int(), C.c_double(), C.c_int64(), C.c_int()
+        self._check(self.L.zr_server_request(self.h, rid, C.byref(st), C.byref(lat), C.byref(n), C.byref(k)))
+        return {"state": st.value, "latency_s": lat.value, "particles": n.value, "substeps": k.value}
+
+    def result(self, rid, name, dtype=np.float64):
+        fid, nc = FIELD[name]
+        n = self.request(rid)["particles"]
+        out = np.zeros((n, nc) if nc > 1 else n, dtype=dtype)
+        self._check(self.L.zr_server_result(self.h, rid, fid, out.ctypes.data_as(C.c_void_p), F64 if dtype == np.float64 else F32))
+        return out
+
+    def release(self, rid):
+        self._check(self.L.zr_server_release(self.h, rid))
+
+    def stats(self):
+        a, b, c = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.L.zr_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"particle_substeps": a.value, "device_ms": b.value, "device_bytes": c.value}
 
 
 def version():

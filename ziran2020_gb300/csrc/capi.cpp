@@ -2,8 +2,12 @@
 #include "../../include/ziran_gb300.h"
 #include "engine.h"
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
 #include <new>
 #include <random>
@@ -762,5 +766,243 @@ int zr_batch_stats(zr_batch* b, int64_t* launches, int64_t* bytes, int64_t* fall
 }
 
 const char* zr_batch_last_error(zr_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+} // extern "C"
+
+// ------------------------------------------------------------------------------------------- serving loop
+// Continuous batching: requests (a scene and a number of substeps) queue on submit; every tick admits
+// queued requests in arrival order while the memory budget and the scene limit allow, re-forms the batch
+// (resident scenes stay on the device), advances all resident scenes together by
+// min(tick_substeps, fewest remaining) substeps and retires the scenes that are done, reading their final
+// state to the host. Latency = completion time - submit time (steady clock).
+struct zr_server {
+    struct Req {
+        SceneDesc desc;
+        int substeps = 0, remaining = 0, state = 0; // 0 queued, 1 running, 2 done, 3 failed
+        double t_submit = 0, t_admit = 0, t_done = 0, bytes = 0;
+        std::vector<double> result; // 25 values per particle at completion
+    };
+    int precision = ZR_F32;
+    double budget = 0;
+    int tick_substeps = 10, max_scenes = 256;
+    std::unique_ptr<EngineBase> eng;
+    std::map<int64_t, Req> reqs;
+    std::deque<int64_t> queue;
+    std::vector<int64_t> resident; // engine slot order
+    bool dirty = false; // resident set changed since the last repack
+    double resident_bytes = 0, particle_substeps = 0, busy_ms = 0;
+    int64_t next_id = 1;
+    std::string err;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+// device bytes a resident scene needs: two particle copies, sort buffers, and the grid blocks of about
+// n / 256 occupied blocks plus their neighbours (8 per occupied block at most)
+double scene_bytes(int precision, int64_t n)
+{
+    const double s = precision == ZR_F64 ? 8 : 4, nodes = precision == ZR_F64 ? 32 : 64;
+    const double per_particle = 2 * (28 * s + 4) + 8 + 8 + 4 + 4 + 4;
+    const double groups = (double)n / (nodes * 4) + 64;
+    return n * per_particle + 8 * groups * (10 * nodes * s + 64);
+}
+} // namespace
+
+extern "C" {
+
+int zr_server_create(int precision, double budget_bytes, int tick_substeps, int max_scenes, zr_server** out)
+{
+    if (!out || (precision != ZR_F32 && precision != ZR_F64) || !(budget_bytes > 0) || tick_substeps <= 0 || max_scenes <= 0 || max_scenes > 4096)
+        return ZR_ERR_ARG;
+    zr_server* sv = new (std::nothrow) zr_server();
+    if (!sv) return ZR_ERR_ARG;
+    sv->precision = precision;
+    sv->budget = budget_bytes;
+    sv->tick_substeps = tick_substeps;
+    sv->max_scenes = max_scenes;
+    *out = sv;
+    return ZR_OK;
+}
+
+int zr_server_destroy(zr_server* sv)
+{
+    delete sv;
+    return ZR_OK;
+}
+
+static int server_enqueue(zr_server* sv, SceneDesc&& d, int substeps, int64_t* id)
+{
+    if (substeps <= 0) return set_err(sv->err, ZR_ERR_ARG, "substeps must be positive");
+    const double bytes = scene_bytes(sv->precision, d.n);
+    if (bytes > sv->budget) return set_err(sv->err, ZR_ERR_BUDGET, "the request alone exceeds the memory budget");
+    const int64_t rid = sv->next_id++;
+    zr_server::Req& r = sv->reqs[rid];
+    r.desc = std::move(d);
+    r.substeps = r.remaining = substeps;
+    r.t_submit = sv->now();
+    r.bytes = bytes;
+    sv->queue.push_back(rid);
+    if (id) *id = rid;
+    return ZR_OK;
+}
+
+int zr_server_submit_recipe(zr_server* sv, const zr_scene_recipe* rcp, int substeps, int64_t* id)
+{
+    if (!sv || !rcp) return ZR_ERR_ARG;
+    SceneDesc d;
+    int rc = desc_from_recipe(d, rcp, sv->err);
+    if (rc) return rc;
+    return server_enqueue(sv, std::move(d), substeps, id);
+}
+
+int zr_server_submit_scene(zr_server* sv, zr_scene* s, int substeps, int64_t* id)
+{
+    if (!sv || !s) return ZR_ERR_ARG;
+    if (s->desc.n <= 0 || s->desc.materials.empty()) return set_err(sv->err, ZR_ERR_ARG, "scene has no particles or no model");
+    if (s->committed) return set_err(sv->err, ZR_ERR_STATE, "submit a scene before it has stepped");
+    SceneDesc d = std::move(s->desc); // the server takes the particles; the scene handle is left empty
+    s->desc = SceneDesc();
+    return server_enqueue(sv, std::move(d), substeps, id);
+}
+
+int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished)
+{
+    if (!sv) return ZR_ERR_ARG;
+    int done_now = 0;
+    // admit in arrival order while the budget and the scene limit allow
+    std::vector<int64_t> add_ids;
+    double bytes = sv->resident_bytes;
+    while (!sv->queue.empty() && (int)(sv->resident.size() + add_ids.size()) < sv->max_scenes) {
+        zr_server::Req& r = sv->reqs[sv->queue.front()];
+        if (bytes + r.bytes > sv->budget) break;
+        bytes += r.bytes;
+        add_ids.push_back(sv->queue.front());
+        sv->queue.pop_front();
+    }
+    if (!add_ids.empty() || sv->dirty) {
+        std::vector<int> keep;
+        for (size_t k = 0; k < sv->resident.size(); k++) keep.push_back((int)k);
+        std::vector<const SceneDesc*> add;
+        for (int64_t rid : add_ids) add.push_back(&sv->reqs[rid].desc);
+        if (keep.empty() && add.empty()) {
+            sv->eng.reset();
+        }
+        else {
+            if (!sv->eng) sv->eng = make_engine(sv->precision);
+            int rc = keep.empty() ? sv->eng->load(add) : sv->eng->repack(keep, add);
+            if (rc) return set_err(sv->err, rc, sv->eng->last_error());
+        }
+        const double t = sv->now();
+        for (int64_t rid : add_ids) {
+            zr_server::Req& r = sv->reqs[rid];
+            r.state = 1;
+            r.t_admit = t;
+            sv->resident.push_back(rid);
+            r.desc.x.clear(); // the device holds the state now
+            r.desc.v.clear();
+            r.desc.C.clear();
+            r.desc.F.clear();
+            r.desc.d.clear();
+        }
+        sv->resident_bytes = bytes;
+        sv->dirty = false;
+    }
+    if (!sv->resident.empty()) {
+        int k = sv->tick_substeps;
+        for (int64_t rid : sv->resident) k = std::min(k, sv->reqs[rid].remaining);
+        StepReport rep;
+        int rc = sv->eng->step(k, &rep);
+        sv->busy_ms += rep.device_ms;
+        if (rc) {
+            for (int64_t rid : sv->resident) sv->reqs[rid].state = 3;
+            return set_err(sv->err, rc, sv->eng->last_error());
+        }
+        std::vector<int64_t> still;
+        const double t = sv->now();
+        for (size_t slot = 0; slot < sv->resident.size(); slot++) {
+            const int64_t rid = sv->resident[slot];
+            zr_server::Req& r = sv->reqs[rid];
+            r.remaining -= k;
+            sv->particle_substeps += (double)r.desc.n * k;
+            if (r.remaining > 0) {
+                still.push_back(rid);
+                continue;
+            }
+            r.result.resize((size_t)r.desc.n * 25);
+            int rc2 = sv->eng->get_state((int)slot, r.result.data(), 0);
+            if (rc2) return set_err(sv->err, rc2, sv->eng->last_error());
+            r.state = 2;
+            r.t_done = t;
+            sv->resident_bytes -= r.bytes;
+            sv->dirty = true;
+            done_now++;
+        }
+        sv->resident.swap(still);
+    }
+    if (running) *running = (int)sv->resident.size();
+    if (queued) *queued = (int)sv->queue.size();
+    if (finished) *finished = done_now;
+    return ZR_OK;
+}
+
+int zr_server_request(zr_server* sv, int64_t id, int* state, double* latency_s, int64_t* particles, int* substeps)
+{
+    if (!sv) return ZR_ERR_ARG;
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return set_err(sv->err, ZR_ERR_ARG, "unknown request");
+    const zr_server::Req& r = it->second;
+    if (state) *state = r.state;
+    if (latency_s) *latency_s = r.state == 2 ? r.t_done - r.t_submit : -1.0;
+    if (particles) *particles = r.desc.n;
+    if (substeps) *substeps = r.substeps;
+    return ZR_OK;
+}
+
+int zr_server_result(zr_server* sv, int64_t id, int field, void* out, int dtype)
+{
+    if (!sv || !out || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end() || it->second.state != 2) return set_err(sv->err, ZR_ERR_STATE, "request not finished");
+    const zr_server::Req& r = it->second;
+    int off, nc;
+    switch (field) {
+    case ZR_FIELD_X: off = 0; nc = 3; break;
+    case ZR_FIELD_V: off = 3; nc = 3; break;
+    case ZR_FIELD_C: off = 6; nc = 9; break;
+    case ZR_FIELD_F: off = 15; nc = 9; break;
+    case ZR_FIELD_D: off = 24; nc = 1; break;
+    default: return set_err(sv->err, ZR_ERR_ARG, "results hold x, v, C, F and d");
+    }
+    for (int64_t p = 0; p < r.desc.n; p++)
+        for (int c = 0; c < nc; c++) {
+            const double v = r.result[(size_t)p * 25 + off + c];
+            if (dtype == ZR_F64)
+                ((double*)out)[p * nc + c] = v;
+            else
+                ((float*)out)[p * nc + c] = (float)v;
+        }
+    return ZR_OK;
+}
+
+int zr_server_release(zr_server* sv, int64_t id)
+{
+    if (!sv) return ZR_ERR_ARG;
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end() || (it->second.state != 2 && it->second.state != 3)) return set_err(sv->err, ZR_ERR_STATE, "request not finished");
+    sv->reqs.erase(it);
+    return ZR_OK;
+}
+
+int zr_server_stats(zr_server* sv, double* particle_substeps, double* device_ms, int64_t* device_bytes)
+{
+    if (!sv) return ZR_ERR_ARG;
+    if (particle_substeps) *particle_substeps = sv->particle_substeps;
+    if (device_ms) *device_ms = sv->busy_ms;
+    if (device_bytes) *device_bytes = sv->eng ? sv->eng->device_bytes() : 0;
+    return ZR_OK;
+}
+
+const char* zr_server_last_error(zr_server* sv) { return sv ? sv->err.c_str() : "null server"; }
 
 } // extern "C"

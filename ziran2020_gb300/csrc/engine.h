@@ -69,6 +69,9 @@ public:
     virtual int precision() const = 0;
     // Build device state for the given scenes (replaces any previous batch).
     virtual int load(const std::vector<const SceneDesc*>& scenes) = 0;
+    // Re-form the batch: keep the listed scene slots (device state, in that order) and append new scenes.
+    // Slots are renumbered: kept scenes first, then the new ones.
+    virtual int repack(const std::vector<int>& keep, const std::vector<const SceneDesc*>& add) = 0;
     // Advance every scene of the batch by nsteps substeps. Returns 0 or a ZR_ERR code; rep gets details.
     virtual int step(int nsteps, StepReport* rep) = 0;
     // Copy one field of one scene, in the caller's particle order, into out (float64 or float32).

@@ -49,160 +49,164 @@ public:
         if (init_err_) return init_err_;
         release_batch();
         if (scenes.empty()) return arg("empty batch");
-        h_scenes_.clear();
-        int64_t N = 0, max_n = 1;
-        int max_domain = 0;
-        for (auto* sd : scenes) {
-            if (!sd || sd->n <= 0) return arg("scene without particles");
-            if (sd->n >= (int64_t)(1u << L::index_bits)) return arg("too many particles in one scene for the SPGrid key (limit 2^" + std::to_string(L::index_bits) + ")");
-            if ((int)sd->materials.size() > MAX_MATERIALS || sd->materials.empty()) return arg("a scene needs 1.." + std::to_string(MAX_MATERIALS) + " materials");
-            if ((int)sd->objects.size() > MAX_OBJECTS) return arg("at most " + std::to_string(MAX_OBJECTS) + " collision objects per scene");
-            if (!(sd->dx > 0) || !(sd->dt > 0)) return arg("dx and dt must be positive");
-            int dc = sd->domain_cells > 0 ? sd->domain_cells : 4096 - 8;
-            if (dc > 4096 - 8 || dc < 8) return arg("domain_cells must be in [8, 4088]");
+        return repack({}, scenes);
+    }
+
+    // Re-form the batch: keep the listed scenes (device state, in the given order) and append new ones.
+    // Kept scenes move device-to-device into the other particle buffer (or into larger buffers when the
+    // capacity grows); their time, materials and collision objects stay as they are on the device.
+    int repack(const std::vector<int>& keep, const std::vector<const SceneDesc*>& add) override
+    {
+        if (init_err_) return init_err_;
+        if (keep.empty() && add.empty()) return arg("empty batch");
+        std::vector<SceneParams<T>> np;
+        std::vector<int64_t> src_first;
+        int64_t N = 0;
+        if (!keep.empty()) {
+            std::vector<SceneParams<T>> curp(h_scenes_.size());
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+            ZR_CUDA(cudaMemcpy(curp.data(), d_scenes_, sizeof(SceneParams<T>) * curp.size(), cudaMemcpyDeviceToHost));
+            for (int k : keep) {
+                if (k < 0 || k >= (int)curp.size()) return arg("repack: kept scene out of range");
+                SceneParams<T> sp = curp[k];
+                src_first.push_back(sp.first);
+                sp.first = N;
+                N += sp.count;
+                np.push_back(sp);
+            }
+        }
+        int64_t max_add = 1;
+        for (auto* sd : add) {
+            if (!sd) return arg("null scene");
             SceneParams<T> sp;
-            std::memset(&sp, 0, sizeof sp);
-            sp.dx = (T)sd->dx;
-            sp.inv_dx = (T)1 / sp.dx; // BSplineWeights one_over_dx(1 / dx) (MpmGrid.h:69)
-            sp.dt = (T)sd->dt;
-            T dx2 = sp.dx * sp.dx;
-            sp.D_inv = (T)4 / dx2;
-            for (int c = 0; c < 3; c++) sp.gravity[c] = (T)sd->gravity[c];
-            T r = (T)sd->apic_rpic_ratio;
-            sp.apic_a = (r + 1) * (T)0.5;
-            sp.apic_b = (r - 1) * (T)0.5;
-            sp.cfl = (T)sd->cfl;
-            sp.time = sd->time;
+            int rc = params_from_desc(*sd, sp);
+            if (rc) return rc;
             sp.first = N;
-            sp.count = sd->n;
-            sp.domain_cells = dc;
-            sp.n_objects = (int)sd->objects.size();
-            sp.n_materials = (int)sd->materials.size();
-            sp.damage = 0;
-            for (int k = 0; k < sp.n_materials; k++) {
-                const auto& m = sd->materials[k];
-                Material<T>& mt = sp.materials[k];
-                T E = (T)m.E, nu = (T)m.nu;
-                mt.model = m.model;
-                mt.damage = m.damage;
-                mt.lambda = E * nu / (((T)1 + nu) * ((T)1 - (T)2 * nu)); // CorotatedElasticity.cpp:16-21
-                mt.mu = E / ((T)2 * ((T)1 + nu));
-                mt.kappa = (T).666666 * mt.mu + mt.lambda; // NeoHookeanBorden.cpp:20
-                mt.alpha = (T)m.alpha;
-                mt.l0 = (T)m.l0;
-                mt.eta = (T)m.eta;
-                mt.zeta = (T)m.zeta;
-                mt.residual = (T)m.residual;
-                if (m.damage) sp.damage = 1;
-            }
-            for (int k = 0; k < sp.n_objects; k++) {
-                const auto& o = sd->objects[k];
-                double nn = std::sqrt(o.normal[0] * o.normal[0] + o.normal[1] * o.normal[1] + o.normal[2] * o.normal[2]);
-                if (!(nn > 0)) return arg("half-space normal must be non-zero");
-                if (o.type < 1 || o.type > 3) return arg("collision type must be STICKY(1), SLIP(2) or SEPARATE(3)");
-                HalfSpaceObj<T>& h = sp.objects[k];
-                for (int c = 0; c < 3; c++) {
-                    h.origin[c] = (T)o.origin[c];
-                    h.normal[c] = (T)(o.normal[c] / nn); // AnalyticLevelSet.cpp:318-323 normalises
-                    h.vel[c] = (T)o.vel[c];
-                }
-                h.friction = (T)o.friction;
-                h.type = o.type;
-            }
-            h_scenes_.push_back(sp);
             N += sd->n;
-            max_n = std::max<int64_t>(max_n, sd->n);
-            max_domain = std::max(max_domain, dc);
+            max_add = std::max<int64_t>(max_add, sd->n);
+            np.push_back(sp);
         }
         if (N >= (int64_t)0xffffffffLL) return arg("batch too large");
+        // key layout of the new batch
+        int max_domain = 0;
+        for (auto& sp : np) max_domain = std::max(max_domain, sp.domain_cells);
+        KeyLayout kl;
+        const int cb = bitlen((uint64_t)(max_domain + 2 * std::max(L::sx, std::max(L::sy, L::sz)) - 1));
+        const uint32_t maxc = (1u << cb) - 1;
+        kl.ib = 0; // hot-path keys carry no particle index: k_cellfix orders each cell by original index
+        kl.cp = bitlen(L::offset(maxc, maxc, maxc)) - L::data_bits;
+        kl.sb = bitlen((uint64_t)(np.size() - 1));
+        kl.block_bits = L::block_bits;
+        if (kl.total() > 64) return arg("batch too large for 64-bit keys: reduce the number of scenes or their domain");
+        drop_graphs();
+        // particle buffers: the free half of the current pair, or a larger pair
+        int dst;
+        T* old_pool = pool_[cur_];
+        uint32_t* old_pid = pid_[cur_];
+        const int64_t old_cap = cap_;
+        T* grown_pool[2] = { nullptr, nullptr };
+        uint32_t* grown_pid[2] = { nullptr, nullptr };
+        if ((uint64_t)N > cap_) {
+            const int64_t cap = std::max<int64_t>(N, 2 * (int64_t)cap_);
+            if (alloc((void**)&grown_pool[0], sizeof(T) * P_NF * cap) || alloc((void**)&grown_pool[1], sizeof(T) * P_NF * cap)
+                || alloc((void**)&grown_pid[0], 4 * cap) || alloc((void**)&grown_pid[1], 4 * cap))
+                return ZR_ERR_CUDA_;
+            ZR_CUDA(cudaMemsetAsync(grown_pool[0], 0, sizeof(T) * P_NF * cap, stream_));
+            ZR_CUDA(cudaMemsetAsync(grown_pool[1], 0, sizeof(T) * P_NF * cap, stream_));
+            for (size_t q = 0; q < np.size() - add.size(); q++) {
+                for (int f = 0; f < P_NF; f++)
+                    ZR_CUDA(cudaMemcpyAsync(grown_pool[0] + (size_t)f * cap + np[q].first, old_pool + (size_t)f * old_cap + src_first[q],
+                        sizeof(T) * np[q].count, cudaMemcpyDeviceToDevice, stream_));
+                ZR_CUDA(cudaMemcpyAsync(grown_pid[0] + np[q].first, old_pid + src_first[q], 4 * np[q].count, cudaMemcpyDeviceToDevice, stream_));
+            }
+            ZR_CUDA(cudaStreamSynchronize(stream_));
+            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_ };
+            for (void* p : olds)
+                if (p) cudaFree(p);
+            pool_[0] = grown_pool[0];
+            pool_[1] = grown_pool[1];
+            pid_[0] = grown_pid[0];
+            pid_[1] = grown_pid[1];
+            cap_ = (uint64_t)cap;
+            if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
+                || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap))
+                return ZR_ERR_CUDA_;
+            k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
+            size_t sb = 0, se = 0;
+            ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, cap, 0, 64, stream_));
+            ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, (uint32_t*)nullptr, cap,
+                GroupHead{ keys_sorted_, kl }, stream_));
+            sort_bytes_ = sb;
+            sel_bytes_ = se;
+            if (alloc(&sort_tmp_, sort_bytes_) || alloc(&sel_tmp_, sel_bytes_)) return ZR_ERR_CUDA_;
+            dst = 0;
+        }
+        else {
+            dst = cur_ ^ 1;
+            for (size_t q = 0; q < np.size() - add.size(); q++) {
+                for (int f = 0; f < P_NF; f++)
+                    ZR_CUDA(cudaMemcpyAsync(pool_[dst] + (size_t)f * cap_ + np[q].first, pool_[cur_] + (size_t)f * cap_ + src_first[q],
+                        sizeof(T) * np[q].count, cudaMemcpyDeviceToDevice, stream_));
+                ZR_CUDA(cudaMemcpyAsync(pid_[dst] + np[q].first, pid_[cur_] + src_first[q], 4 * np[q].count, cudaMemcpyDeviceToDevice, stream_));
+            }
+        }
+        // per-scene device arrays
+        if (np.size() > scene_cap_) {
+            void* p1 = d_scenes_;
+            dfree(p1);
+            void* p2 = grid_mass_;
+            dfree(p2);
+            d_scenes_ = nullptr;
+            grid_mass_ = nullptr;
+            scene_cap_ = std::max<size_t>(np.size(), 2 * scene_cap_);
+            if (alloc((void**)&d_scenes_, sizeof(SceneParams<T>) * scene_cap_) || alloc((void**)&grid_mass_, 8 * scene_cap_)) return ZR_ERR_CUDA_;
+        }
+        if (!st_ && alloc((void**)&st_, sizeof(DevStatus))) return ZR_ERR_CUDA_;
+        h_scenes_ = np;
+        N_ = (uint32_t)N;
+        kl_ = kl;
+        cur_ = dst;
         models_ = 0;
         for (auto& sp : h_scenes_)
             for (int k = 0; k < sp.n_materials; k++) models_ |= sp.materials[k].model == MODEL_COROTATED ? 1 : 2;
-        N_ = (uint32_t)N;
-        // key layout
-        int cb = bitlen((uint64_t)(max_domain + 2 * std::max(L::sx, std::max(L::sy, L::sz)) - 1));
-        uint32_t maxc = (1u << cb) - 1;
-        kl_.ib = 0; // hot-path keys carry no particle index: k_cellfix orders each cell by original index
-        kl_.cp = bitlen(L::offset(maxc, maxc, maxc)) - L::data_bits;
-        kl_.sb = bitlen((uint64_t)(h_scenes_.size() - 1));
-        kl_.block_bits = L::block_bits;
-        if (kl_.total() > 64) return arg("batch too large for 64-bit keys: reduce the number of scenes or their domain");
-        // device buffers
-        const int64_t n = N_;
-        if (alloc((void**)&pool_[0], sizeof(T) * P_NF * n) || alloc((void**)&pool_[1], sizeof(T) * P_NF * n) || alloc((void**)&pid_[0], 4 * n)
-            || alloc((void**)&pid_[1], 4 * n) || alloc((void**)&keys_in_, 8 * n) || alloc((void**)&keys_sorted_, 8 * n) || alloc((void**)&iota_, 4 * n)
-            || alloc((void**)&vals_sorted_, 4 * n) || alloc((void**)&g_start_, 4 * n) || alloc((void**)&d_scenes_, sizeof(SceneParams<T>) * h_scenes_.size())
-            || alloc((void**)&grid_mass_, 8 * h_scenes_.size()) || alloc((void**)&st_, sizeof(DevStatus)))
-            return ZR_ERR_CUDA_;
-        ZR_CUDA(cudaMemsetAsync(pool_[0], 0, sizeof(T) * P_NF * n, stream_));
-        ZR_CUDA(cudaMemsetAsync(pool_[1], 0, sizeof(T) * P_NF * n, stream_));
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
-        ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * h_scenes_.size(), stream_));
+        ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * scene_cap_, stream_));
         ZR_CUDA(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), sizeof(SceneParams<T>) * h_scenes_.size(), cudaMemcpyHostToDevice, stream_));
-        k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, N_);
-        // CUB scratch
-        size_t sb = 0, se = 0;
-        ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)n, 0, kl_.total(), stream_));
-        GroupHead gh{ keys_sorted_, kl_ };
-        ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)n, gh, stream_));
-        sort_bytes_ = sb;
-        sel_bytes_ = se;
-        if (alloc(&sort_tmp_, sort_bytes_) || alloc(&sel_tmp_, sel_bytes_)) return ZR_ERR_CUDA_;
-        // particles
-        cur_ = 0;
-        std::vector<T> buf;
+        // new scenes: host -> device
+        const size_t first_new = np.size() - add.size();
         uint8_t* d_mat = nullptr;
-        if (alloc((void**)&d_mat, (size_t)max_n)) return ZR_ERR_CUDA_;
-        for (size_t s = 0; s < scenes.size(); s++) {
-            const SceneDesc& sd = *scenes[s];
-            const int64_t first = h_scenes_[s].first, cnt = sd.n;
-            auto put = [&](int f0, int nc, const std::vector<double>& src, double dflt_diag, double dflt) -> int {
-                buf.resize(cnt);
-                for (int c = 0; c < nc; c++) {
-                    for (int64_t i = 0; i < cnt; i++) {
-                        if (!src.empty())
-                            buf[i] = (T)src[(size_t)i * nc + c];
-                        else
-                            buf[i] = (T)((nc == 9 && (c % 4) == 0) ? dflt_diag : dflt);
-                    }
-                    ZR_CUDA(cudaMemcpy(pool_[0] + (size_t)(f0 + c) * n + first, buf.data(), sizeof(T) * cnt, cudaMemcpyHostToDevice));
-                }
-                return 0;
-            };
-            if ((int64_t)sd.x.size() != 3 * cnt || (int64_t)sd.m.size() != cnt || (int64_t)sd.V0.size() != cnt) return arg("x, m, V0 are required");
-            if (!sd.v.empty() && (int64_t)sd.v.size() != 3 * cnt) return arg("v must have 3n values");
-            if (!sd.F.empty() && (int64_t)sd.F.size() != 9 * cnt) return arg("F must have 9n values");
-            if (!sd.C.empty() && (int64_t)sd.C.size() != 9 * cnt) return arg("C must have 9n values");
-            if (!sd.d.empty() && (int64_t)sd.d.size() != cnt) return arg("d must have n values");
-            if (!sd.sigma_c.empty() && (int64_t)sd.sigma_c.size() != cnt) return arg("sigma_c must have n values");
-            int rc;
-            if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
-                || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1)))
+        if (!add.empty() && alloc((void**)&d_mat, (size_t)max_add)) return ZR_ERR_CUDA_;
+        std::vector<T> buf;
+        for (size_t q = 0; q < add.size(); q++) {
+            int rc = upload_scene(*add[q], h_scenes_[first_new + q].first, dst, d_mat, buf);
+            if (rc) {
+                cudaFree(d_mat);
                 return rc;
-            const uint8_t* mp = nullptr;
-            if (!sd.material.empty()) {
-                if ((int64_t)sd.material.size() != cnt) return arg("material must have n values");
-                for (auto mm : sd.material)
-                    if ((int)mm >= (int)sd.materials.size()) return arg("material index out of range");
-                ZR_CUDA(cudaMemcpy(d_mat, sd.material.data(), cnt, cudaMemcpyHostToDevice));
-                mp = d_mat;
             }
-            k_iota_pid<T><<<nsm_ * 4, 256, 0, stream_>>>(pid_[0], mp, first, cnt);
-            ZR_CUDA(cudaStreamSynchronize(stream_));
         }
-        cudaFree(d_mat);
-        dev_bytes_ -= (int64_t)max_n;
-        // first binning pass sizes the grid: groups G0 -> capacity for 4 G0 active blocks (at least 4096)
-        k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(0), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
-        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)n, 0, kl_.total(), stream_));
-        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)n, gh, stream_));
+        if (d_mat) {
+            cudaFree(d_mat);
+            dev_bytes_ -= (int64_t)max_add;
+        }
+        // keys, and a first binning pass that sizes the grid (every group activates at most 8 blocks)
+        k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
+        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)N_, 0, kl_.total(), stream_));
+        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)N_,
+            GroupHead{ keys_sorted_, kl_ }, stream_));
         DevStatus hs;
         ZR_CUDA(cudaMemcpyAsync(&hs, st_, sizeof hs, cudaMemcpyDeviceToHost, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
         if (hs.flags & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle lies outside its scene's domain");
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
-        int rc = alloc_grid(std::max<uint32_t>(4096, 8 * hs.n_groups + 1024)); // every group activates at most 8 blocks
-        if (rc) return rc;
+        const uint32_t need = std::max<uint32_t>(4096, 8 * hs.n_groups + 1024);
+        if (need > b_cap_) {
+            int rc = alloc_grid(std::max(need, b_cap_ * 2));
+            if (rc) return rc;
+        }
+        else {
+            ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
+            ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+        }
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
     }
@@ -449,6 +453,8 @@ private:
     std::vector<SceneParams<T>> h_scenes_;
     SceneParams<T>* d_scenes_ = nullptr;
     uint32_t N_ = 0;
+    uint64_t cap_ = 0; // particle capacity of the buffers (the pool's field stride)
+    size_t scene_cap_ = 0;
     KeyLayout kl_{};
     T* pool_[2] = { nullptr, nullptr };
     uint32_t* pid_[2] = { nullptr, nullptr };
@@ -477,7 +483,103 @@ private:
     KernelTimes kt_;
     int64_t dev_bytes_ = 0;
 
-    Pool<T> pool(int which) const { return Pool<T>{ pool_[which], pid_[which], (int64_t)N_ }; }
+    Pool<T> pool(int which) const { return Pool<T>{ pool_[which], pid_[which], (int64_t)cap_ }; }
+
+    int params_from_desc(const SceneDesc& sdr, SceneParams<T>& sp)
+    {
+        const SceneDesc* sd = &sdr;
+        if (sd->n <= 0) return arg("scene without particles");
+        if (sd->n >= (int64_t)(1u << L::index_bits)) return arg("too many particles in one scene for the SPGrid key (limit 2^" + std::to_string(L::index_bits) + ")");
+        if ((int)sd->materials.size() > MAX_MATERIALS || sd->materials.empty()) return arg("a scene needs 1.." + std::to_string(MAX_MATERIALS) + " materials");
+        if ((int)sd->objects.size() > MAX_OBJECTS) return arg("at most " + std::to_string(MAX_OBJECTS) + " collision objects per scene");
+        if (!(sd->dx > 0) || !(sd->dt > 0)) return arg("dx and dt must be positive");
+        int dc = sd->domain_cells > 0 ? sd->domain_cells : 4096 - 8;
+        if (dc > 4096 - 8 || dc < 8) return arg("domain_cells must be in [8, 4088]");
+        std::memset(&sp, 0, sizeof sp);
+        sp.dx = (T)sd->dx;
+        sp.inv_dx = (T)1 / sp.dx; // BSplineWeights one_over_dx(1 / dx) (MpmGrid.h:69)
+        sp.dt = (T)sd->dt;
+        T dx2 = sp.dx * sp.dx;
+        sp.D_inv = (T)4 / dx2;
+        for (int c = 0; c < 3; c++) sp.gravity[c] = (T)sd->gravity[c];
+        T r = (T)sd->apic_rpic_ratio;
+        sp.apic_a = (r + 1) * (T)0.5;
+        sp.apic_b = (r - 1) * (T)0.5;
+        sp.cfl = (T)sd->cfl;
+        sp.time = sd->time;
+        sp.count = sd->n;
+        sp.domain_cells = dc;
+        sp.n_objects = (int)sd->objects.size();
+        sp.n_materials = (int)sd->materials.size();
+        sp.damage = 0;
+        for (int k = 0; k < sp.n_materials; k++) {
+            const auto& m = sd->materials[k];
+            Material<T>& mt = sp.materials[k];
+            T E = (T)m.E, nu = (T)m.nu;
+            mt.model = m.model;
+            mt.damage = m.damage;
+            mt.lambda = E * nu / (((T)1 + nu) * ((T)1 - (T)2 * nu)); // CorotatedElasticity.cpp:16-21
+            mt.mu = E / ((T)2 * ((T)1 + nu));
+            mt.kappa = (T).666666 * mt.mu + mt.lambda; // NeoHookeanBorden.cpp:20
+            mt.alpha = (T)m.alpha;
+            mt.l0 = (T)m.l0;
+            mt.eta = (T)m.eta;
+            mt.zeta = (T)m.zeta;
+            mt.residual = (T)m.residual;
+            if (m.damage) sp.damage = 1;
+        }
+        for (int k = 0; k < sp.n_objects; k++) {
+            const auto& o = sd->objects[k];
+            double nn = std::sqrt(o.normal[0] * o.normal[0] + o.normal[1] * o.normal[1] + o.normal[2] * o.normal[2]);
+            if (!(nn > 0)) return arg("half-space normal must be non-zero");
+            if (o.type < 1 || o.type > 3) return arg("collision type must be STICKY(1), SLIP(2) or SEPARATE(3)");
+            HalfSpaceObj<T>& h = sp.objects[k];
+            for (int c = 0; c < 3; c++) {
+                h.origin[c] = (T)o.origin[c];
+                h.normal[c] = (T)(o.normal[c] / nn); // AnalyticLevelSet.cpp:318-323 normalises
+                h.vel[c] = (T)o.vel[c];
+            }
+            h.friction = (T)o.friction;
+            h.type = o.type;
+        }
+        return 0;
+    }
+
+    // host arrays of one scene -> storage slots [first, first + n) of particle buffer `which`
+    int upload_scene(const SceneDesc& sd, int64_t first, int which, uint8_t* d_mat, std::vector<T>& buf)
+    {
+        const int64_t cnt = sd.n, stride = (int64_t)cap_;
+        if ((int64_t)sd.x.size() != 3 * cnt || (int64_t)sd.m.size() != cnt || (int64_t)sd.V0.size() != cnt) return arg("x, m, V0 are required");
+        if (!sd.v.empty() && (int64_t)sd.v.size() != 3 * cnt) return arg("v must have 3n values");
+        if (!sd.F.empty() && (int64_t)sd.F.size() != 9 * cnt) return arg("F must have 9n values");
+        if (!sd.C.empty() && (int64_t)sd.C.size() != 9 * cnt) return arg("C must have 9n values");
+        if (!sd.d.empty() && (int64_t)sd.d.size() != cnt) return arg("d must have n values");
+        if (!sd.sigma_c.empty() && (int64_t)sd.sigma_c.size() != cnt) return arg("sigma_c must have n values");
+        auto put = [&](int f0, int nc, const std::vector<double>& src, double dflt_diag, double dflt) -> int {
+            buf.resize(cnt);
+            for (int c = 0; c < nc; c++) {
+                for (int64_t i = 0; i < cnt; i++)
+                    buf[i] = !src.empty() ? (T)src[(size_t)i * nc + c] : (T)((nc == 9 && (c % 4) == 0) ? dflt_diag : dflt);
+                ZR_CUDA(cudaMemcpy(pool_[which] + (size_t)(f0 + c) * stride + first, buf.data(), sizeof(T) * cnt, cudaMemcpyHostToDevice));
+            }
+            return 0;
+        };
+        int rc;
+        if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
+            || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1)))
+            return rc;
+        const uint8_t* mp = nullptr;
+        if (!sd.material.empty()) {
+            if ((int64_t)sd.material.size() != cnt) return arg("material must have n values");
+            for (auto mm : sd.material)
+                if ((int)mm >= (int)sd.materials.size()) return arg("material index out of range");
+            ZR_CUDA(cudaMemcpy(d_mat, sd.material.data(), cnt, cudaMemcpyHostToDevice));
+            mp = d_mat;
+        }
+        k_iota_pid<T><<<nsm_ * 4, 256, 0, stream_>>>(pid_[which], mp, first, cnt);
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
 
     int arg(const std::string& m) { return fail(ZR_ERR_ARG_, m); }
     int fail(int code, const std::string& m)
@@ -774,6 +876,8 @@ private:
         sort_tmp_ = sel_tmp_ = stage_ = nullptr;
         stage_bytes_ = 0;
         N_ = 0;
+        cap_ = 0;
+        scene_cap_ = 0;
         b_cap_ = 0;
         dev_bytes_ = 0;
         h_scenes_.clear();
