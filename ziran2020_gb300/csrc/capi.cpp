@@ -788,7 +788,8 @@ struct zr_server {
     std::unique_ptr<EngineBase> eng;
     std::map<int64_t, Req> reqs;
     std::deque<int64_t> queue;
-    std::vector<int64_t> resident; // engine slot order
+    std::vector<int64_t> resident; // requests on the device
+    std::vector<int> slot; // engine slot of each resident request (slots of retired requests are dropped at the next repack)
     bool dirty = false; // resident set changed since the last repack
     double resident_bytes = 0, particle_substeps = 0, busy_ms = 0;
     int64_t next_id = 1;
@@ -881,8 +882,7 @@ int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished)
         sv->queue.pop_front();
     }
     if (!add_ids.empty() || sv->dirty) {
-        std::vector<int> keep;
-        for (size_t k = 0; k < sv->resident.size(); k++) keep.push_back((int)k);
+        std::vector<int> keep = sv->slot; // the engine slots of the requests that are still resident
         std::vector<const SceneDesc*> add;
         for (int64_t rid : add_ids) add.push_back(&sv->reqs[rid].desc);
         if (keep.empty() && add.empty()) {
@@ -891,13 +891,27 @@ int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished)
         else {
             if (!sv->eng) sv->eng = make_engine(sv->precision);
             int rc = keep.empty() ? sv->eng->load(add) : sv->eng->repack(keep, add);
-            if (rc) return set_err(sv->err, rc, sv->eng->last_error());
+            if (rc) {
+                // the batch could not be formed: fail the requests involved and start from an empty device
+                set_err(sv->err, rc, sv->eng->last_error());
+                for (int64_t rid : add_ids) sv->reqs[rid].state = 3;
+                for (int64_t rid : sv->resident) sv->reqs[rid].state = 3;
+                sv->resident.clear();
+                sv->slot.clear();
+                sv->resident_bytes = 0;
+                sv->dirty = false;
+                sv->eng.reset();
+                return rc;
+            }
         }
+        // the engine renumbered its slots: kept scenes first, in order, then the admitted ones
+        for (size_t k = 0; k < sv->slot.size(); k++) sv->slot[k] = (int)k;
         const double t = sv->now();
         for (int64_t rid : add_ids) {
             zr_server::Req& r = sv->reqs[rid];
             r.state = 1;
             r.t_admit = t;
+            sv->slot.push_back((int)sv->resident.size());
             sv->resident.push_back(rid);
             r.desc.x.clear(); // the device holds the state now
             r.desc.v.clear();
@@ -915,22 +929,32 @@ int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished)
         int rc = sv->eng->step(k, &rep);
         sv->busy_ms += rep.device_ms;
         if (rc) {
+            set_err(sv->err, rc, sv->eng->last_error());
             for (int64_t rid : sv->resident) sv->reqs[rid].state = 3;
-            return set_err(sv->err, rc, sv->eng->last_error());
+            sv->resident.clear();
+            sv->slot.clear();
+            sv->resident_bytes = 0;
+            sv->dirty = false;
+            sv->eng.reset();
+            return rc;
         }
         std::vector<int64_t> still;
+        std::vector<int> still_slot;
         const double t = sv->now();
-        for (size_t slot = 0; slot < sv->resident.size(); slot++) {
-            const int64_t rid = sv->resident[slot];
+        for (size_t k2 = 0; k2 < sv->resident.size(); k2++) {
+            const int64_t rid = sv->resident[k2];
+            const int slot = sv->slot[k2];
             zr_server::Req& r = sv->reqs[rid];
             r.remaining -= k;
             sv->particle_substeps += (double)r.desc.n * k;
             if (r.remaining > 0) {
                 still.push_back(rid);
+                still_slot.push_back(slot);
                 continue;
             }
+            if (sv->eng->count(slot) != r.desc.n) return set_err(sv->err, ZR_ERR_STATE, "server slot bookkeeping does not match the engine");
             r.result.resize((size_t)r.desc.n * 25);
-            int rc2 = sv->eng->get_state((int)slot, r.result.data(), 0);
+            int rc2 = sv->eng->get_state(slot, r.result.data(), 0);
             if (rc2) return set_err(sv->err, rc2, sv->eng->last_error());
             r.state = 2;
             r.t_done = t;
@@ -939,6 +963,7 @@ int zr_server_tick(zr_server* sv, int* running, int* queued, int* finished)
             done_now++;
         }
         sv->resident.swap(still);
+        sv->slot.swap(still_slot);
     }
     if (running) *running = (int)sv->resident.size();
     if (queued) *queued = (int)sv->queue.size();
