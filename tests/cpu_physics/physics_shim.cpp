@@ -1,0 +1,73 @@
+// Test shim: exposes the GPU physics routines (ziran2020_gb300/csrc/physics.cuh, compiled here as host
+// C++) to the CPU tests, which compare them with the oracle and with numpy.
+#include "../../ziran2020_gb300/csrc/physics.cuh"
+
+using namespace zr;
+
+template <class T>
+static Material<T> mat(int model, double E, double nu)
+{
+    Material<T> m{};
+    m.model = model;
+    T Et = (T)E, nut = (T)nu;
+    m.lambda = Et * nut / (((T)1 + nut) * ((T)1 - (T)2 * nut));
+    m.mu = Et / ((T)2 * ((T)1 + nut));
+    m.kappa = (T).666666 * m.mu + m.lambda;
+    return m;
+}
+
+extern "C" {
+// returns 1 when the FP64 SVD path was taken
+int shim_polar(int prec, const double* F, double* R)
+{
+    if (prec == 4) {
+        float f[9], r[9];
+        for (int i = 0; i < 9; i++) f[i] = (float)F[i];
+        bool fb = polar_rotation(f, r);
+        for (int i = 0; i < 9; i++) R[i] = r[i];
+        return fb;
+    }
+    double r[9];
+    bool fb = polar_rotation(F, r);
+    for (int i = 0; i < 9; i++) R[i] = r[i];
+    return fb;
+}
+void shim_svd_jacobi(const double* A, double* U, double* s, double* V) { svd3_jacobi(A, U, s, V); }
+void shim_tension(int prec, const double* S, double* Sp)
+{
+    if (prec == 4) {
+        float a[9], b[9];
+        for (int i = 0; i < 9; i++) a[i] = (float)S[i];
+        tension_part(a, b);
+        for (int i = 0; i < 9; i++) Sp[i] = b[i];
+        return;
+    }
+    tension_part(S, Sp);
+}
+void shim_tau(int model, double E, double nu, const double* F, double g, double* tau)
+{
+    Material<double> m = mat<double>(model, E, nu);
+    if (model == MODEL_COROTATED)
+        tau_corotated(m, F, tau);
+    else
+        tau_nhb(m, F, g, tau);
+}
+double shim_damage(double E, double nu, double alpha, double l0, double eta, double zeta, double k, const double* F, double d, double lap, double sc,
+    double dt)
+{
+    Material<double> m = mat<double>(MODEL_NEOHOOKEAN_BORDEN, E, nu);
+    m.damage = 1;
+    m.alpha = alpha;
+    m.l0 = l0;
+    m.eta = eta;
+    m.zeta = zeta;
+    m.residual = k;
+    bool fb = false;
+    return damage_update(m, F, d, lap, sc, dt, fb);
+}
+int shim_key(int prec, int i, int j, int k, unsigned id, unsigned long long* key)
+{
+    *key = prec == 4 ? SpLayout<6>::key(i, j, k, id) : SpLayout<7>::key(i, j, k, id);
+    return 0;
+}
+}

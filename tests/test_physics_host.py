@@ -1,0 +1,166 @@
+"""CPU: the GPU physics routines (physics.cuh compiled as host C++ through tests/cpu_physics) against the
+oracle's restatement and numpy: polar decomposition incl. inverted and singular F (FP64 SVD fallback),
+the tensile stress split, both constitutive models, the damage update and the SPGrid key."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpu_physics", "physics_shim.cpp")
+
+
+@pytest.fixture(scope="module")
+def shim(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("shim") / "libphysics_shim.so")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", SRC, "-o", so])
+    L = C.CDLL(so)
+    pd = C.POINTER(C.c_double)
+    L.shim_polar.argtypes = [C.c_int, pd, pd]
+    L.shim_svd_jacobi.argtypes = [pd, pd, pd, pd]
+    L.shim_tension.argtypes = [C.c_int, pd, pd]
+    L.shim_tau.argtypes = [C.c_int, C.c_double, C.c_double, pd, C.c_double, pd]
+    L.shim_damage.restype = C.c_double
+    L.shim_damage.argtypes = [C.c_double] * 7 + [pd] + [C.c_double] * 4
+    L.shim_key.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint, C.POINTER(C.c_ulonglong)]
+    return L
+
+
+def p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def oracle_R(prec, F):
+    U, s, V = po.svd3(prec, F)
+    return U @ V.T
+
+
+def test_polar_matches_oracle_svd(shim):
+    rng = np.random.default_rng(1)
+    fallbacks = 0
+    for t in range(400):
+        if t % 4 == 0:
+            F = np.eye(3) + 0.02 * rng.normal(size=(3, 3))  # small strain
+        elif t % 4 == 1:
+            F = rng.normal(size=(3, 3))  # generic, often inverted
+        elif t % 4 == 2:
+            Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            F = Q * np.array([1.0, 1.0, 1.0])  # a pure rotation / reflection: degenerate singular values
+        else:
+            F = np.diag([1.5, 0.7, 1e-9]) @ np.linalg.qr(rng.normal(size=(3, 3)))[0]  # nearly singular
+        F = np.ascontiguousarray(F)
+        R = np.zeros(9)
+        fallbacks += shim.shim_polar(8, p(F), p(R))
+        R = R.reshape(3, 3)
+        assert abs(np.linalg.det(R) - 1) < 1e-9 and np.abs(R @ R.T - np.eye(3)).max() < 1e-9
+        s = np.linalg.svd(F, compute_uv=False)
+        if s[1] + s[2] > 1e-6:  # the polar rotation is unique: it must equal the reference's U V^T
+            assert np.abs(R - oracle_R(8, F)).max() < 1e-8 / (s[1] + s[2]), t
+    assert fallbacks > 50  # the inverted and singular cases took the FP64 SVD path
+
+
+def test_polar_fp32_accuracy(shim):
+    rng = np.random.default_rng(2)
+    for t in range(200):
+        F = np.ascontiguousarray(np.eye(3) + 0.3 * rng.normal(size=(3, 3)))
+        R = np.zeros(9)
+        shim.shim_polar(4, p(F), p(R))
+        assert np.abs(R.reshape(3, 3) - oracle_R(8, F)).max() < 2e-5
+
+
+def test_svd_jacobi_sign_convention(shim):
+    rng = np.random.default_rng(3)
+    for t in range(200):
+        A = np.ascontiguousarray(rng.normal(size=(3, 3)))
+        U, s, V = np.zeros(9), np.zeros(3), np.zeros(9)
+        shim.shim_svd_jacobi(p(A), p(U), p(s), p(V))
+        U, V = U.reshape(3, 3), V.reshape(3, 3)
+        assert np.abs(U @ np.diag(s) @ V.T - A).max() < 1e-12
+        assert abs(np.linalg.det(U) - 1) < 1e-12 and abs(np.linalg.det(V) - 1) < 1e-12
+        assert s[0] >= s[1] >= abs(s[2]) and s[1] >= 0
+        assert np.sign(s[2]) == np.sign(np.linalg.det(A)) or abs(s[2]) < 1e-12
+
+
+def test_tension_part(shim):
+    rng = np.random.default_rng(4)
+    for t in range(500):
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        lam = rng.normal(size=3) * 100
+        if t % 5 == 0:
+            lam[1] = lam[0]  # repeated eigenvalue
+        if t % 7 == 0:
+            lam[:] = lam[0]  # multiple of the identity
+        S = np.ascontiguousarray(Q @ np.diag(lam) @ Q.T)
+        want = Q @ np.diag(np.maximum(lam, 0)) @ Q.T
+        got = np.zeros(9)
+        shim.shim_tension(8, p(S), p(got))
+        assert np.abs(got.reshape(3, 3) - want).max() < 1e-9 * max(1, np.abs(lam).max()), t
+        shim.shim_tension(4, p(S), p(got))
+        assert np.abs(got.reshape(3, 3) - want).max() < 2e-4 * max(1, np.abs(lam).max()), t
+
+
+def tau_reference(model, E, nu, F, g):
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    mu = E / (2 * (1 + nu))
+    J = np.linalg.det(F)
+    if model == 0:
+        R = oracle_R(8, F)
+        P = 2 * mu * (F - R) + lam * (J - 1) * J * np.linalg.inv(F).T
+        return P @ F.T
+    kappa = 0.666666 * mu + lam
+    B = F @ F.T
+    dev = mu * J ** (-2 / 3) * (B - np.trace(B) / 3 * np.eye(3))
+    vol = J * kappa / 2 * (J - 1 / J) * np.eye(3)
+    return g * (dev + vol) if J >= 1 else g * dev + vol
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_stress_models(shim, model):
+    rng = np.random.default_rng(5)
+    for t in range(100):
+        F = np.ascontiguousarray(np.eye(3) + 0.2 * rng.normal(size=(3, 3)))
+        if np.linalg.det(F) <= 0.1:
+            continue
+        g = rng.uniform(0.01, 1)
+        tau = np.zeros(9)
+        shim.shim_tau(model, 5e4, 0.25, p(F), g, p(tau))
+        want = tau_reference(model, 5e4, 0.25, F, g)
+        assert np.abs(tau.reshape(3, 3) - want).max() < 1e-8 * 5e4
+
+
+def test_damage_update_matches_reference_formula(shim):
+    rng = np.random.default_rng(6)
+    E, nu, alpha, l0, eta, zeta, k = 5e4, 0.25, -1.0, 0.002, 0.1, 1.0, 0.01
+    for t in range(200):
+        F = np.ascontiguousarray(np.eye(3) + 0.05 * rng.normal(size=(3, 3)))
+        d, lap, sc, dt = rng.uniform(0, 0.5), rng.normal() * 100, rng.uniform(50, 500), 5e-5
+        got = shim.shim_damage(E, nu, alpha, l0, eta, zeta, k, p(F), d, lap, sc, dt)
+        # AnisoFractureSimulation.h:219-281 with numpy's symmetric eigen-decomposition
+        J = np.linalg.det(F)
+        S = tau_reference(1, E, nu, F, 1.0) / J
+        w, Q = np.linalg.eigh((S + S.T) / 2)
+        sp = Q @ np.diag(np.maximum(w, 0)) @ Q.T
+        a = oracle_R(8, F)[:, 0]
+        A = np.eye(3) + alpha * np.outer(a, a)
+        phi = np.sum((A @ sp) * (sp @ A)) / sc ** 2
+        dtil = zeta * max(phi - 1, 0)
+        want = min(d + dt / eta * max((1 - d) * dtil - (d - l0 * l0 * lap), 0), 1)
+        assert abs(got - want) < 1e-10, t
+
+
+def test_gpu_key_function_matches_oracle_layout(shim):
+    rng = np.random.default_rng(7)
+    for prec in (4, 8):
+        for t in range(300):
+            i, j, k = (int(v) for v in rng.integers(0, 4000, 3))
+            key = C.c_ulonglong()
+            idx = int(rng.integers(0, 1 << 20))
+            shim.shim_key(prec, i, j, k, idx, C.byref(key))
+            bb = 6 if prec == 4 else 5
+            data_bits = 6 if prec == 4 else 7
+            want = ((po.linear_offset(prec, i, j, k) >> data_bits) << (32 - bb)) + idx
+            assert key.value == want
