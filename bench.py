@@ -47,11 +47,14 @@ def parse():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per arrival rate")
     ap.add_argument("--tick", type=int, default=25, help="serve: substeps per serving tick")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--accuracy-steps", default="100,500", help="substeps at which FP32 is compared with the FP64 path")
+    ap.add_argument("--oracle-steps", type=int, default=200, help="substeps of the elastic-cube check against the FP64 oracle")
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
+    ap.add_argument("--schedule", default="auto",
+                    help="auto (the autotuner), or fused:CTAS:G2P or split:CHUNK:BUFFERS:CTAS:G2P (a fixed launch schedule)")
     return ap.parse_args()
 
 
@@ -212,11 +215,54 @@ def run_reference(args, world, rank):
             "e2e": {"value": val, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def error_vs_oracle(steps):
+    """Max and RMS error of x, v, F, d of the FP32 and FP64 GPU paths against the FP64 oracle (host cores)
+    after `steps` substeps of the elastic cube: side 0.25 centred at (0.5, 0.6, 0.5), dx = 1/64, 8 particles
+    per cell (32,768), E = 1e4, nu = 0.3, rho = 1000, v0 = (0, -1, 0), gravity, sticky ground at y = 0.05,
+    dt = 1e-4."""
+    import numpy as np
+
+    import ziran2020_gb300 as zr
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes
+
+    desc = scenes.elastic_box(size=0.25, dx=1 / 64, seed=20200)
+    o = scenes.oracle_scene(desc, 8)
+    t0 = time.perf_counter()
+    o.step(steps)
+    ref = o.state()
+    out = {"scene": f"elastic cube, {len(desc['m'])} particles, dx=1/64, {steps} substeps", "oracle_seconds": round(time.perf_counter() - t0, 2),
+           "x_unit": "metres in a unit domain (domain-relative)"}
+    for prec, name in ((zr.F32, "fp32"), (zr.F64, "fp64")):
+        g = scenes.gpu_scene(desc, prec)
+        g.step(steps)
+        st = scenes.gpu_state(g)
+        out[name] = {}
+        for f in ("x", "v", "F", "d"):
+            e = np.abs(np.asarray(st[f], dtype=np.float64) - np.asarray(ref[f], dtype=np.float64))
+            out[name][f] = {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
+        del g
+    return out
+
+
 def _desc_for(kind, over, scenes):
     if kind == 1:
         dx = over.get("dx", 1 / 128)
         return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345)
     return scenes.elastic_box(size=over.get("size", 0.25), dx=over.get("dx", 1 / 64), seed=12345)
+
+
+def apply_schedule(obj, spec):
+    """Fix the launch schedule of a scene from --schedule (the autotuner otherwise picks it)."""
+    if spec == "auto":
+        return
+    f = spec.split(":")
+    if f[0] == "fused":
+        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused=True)
+    else:
+        obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]))
 
 
 def _config(args):
@@ -278,14 +324,24 @@ def run_batch(args, world, rank):
         cpu = {"value": ns * 20 / el, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
                "sample": f"one {ns}-particle elastic box of the family (dx=1/64), 20 substeps; the batch would run its scenes one by one"}
     cfg = {"workload": "batch256", "scenes": len(recs), "particles": int(n), "substeps_timed": args.steps, "precision_path": "fp32",
-           "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{world}"}
+           "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{world}", "schedule": b.schedule()}
+    del b
+    # the plain FP64 GPU path on the same batch
+    b64 = zr.Batch(zr.F64)
+    for r in recs:
+        b64.add_recipe(r)
+    b64.step(2)
+    b64.step(args.fp64_steps)
+    fp64_value = n * args.fp64_steps / (b64.last_step_ms / 1e3)
+    del b64
     line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded recipe family)", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "measured on the single-scene workload"},
             "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
-            "clocks": clock_info, "fp64_fallbacks": stats["fallbacks"]}
+            "clocks": clock_info, "fp64_fallbacks": stats["fallbacks"],
+            "fp64_path": {"value": fp64_value, "unit": "particle-substeps/s", "fp32_over_fp64": value / world / fp64_value}}
     return line if rank == 0 else None
 
 
@@ -356,6 +412,7 @@ def run_ours(args, world, rank):
 
     s = zr.Scene(zr.F32)
     s.from_recipe(r)
+    apply_schedule(s, args.schedule)
     if args.profile_only:
         s.step(args.warmup)
         s.step(args.steps)
@@ -375,6 +432,7 @@ def run_ours(args, world, rank):
     value = n_total * args.steps / (ms_max / 1e3)
     stats = s.stats()
     groups, blocks = s.last_grid()
+    schedule = s.schedule()
 
     # per-phase kernel durations (CUDA events on the engine's stream, substeps run without graphs)
     kt_steps = min(args.steps, 20)
@@ -426,20 +484,32 @@ def run_ours(args, world, rank):
     fp64_value = n * args.fp64_steps / (s64.last_step_ms / 1e3)
     del s64
 
-    # FP32 vs FP64 after the same number of substeps from the same seeded inputs
+    # FP32 vs FP64 after the same numbers of substeps from the same seeded inputs (the FP64 GPU path is
+    # pinned to the FP64 oracle by tests/test_gpu_parity.py; a full-size oracle run would take hours)
     acc = None
-    if args.accuracy_steps > 0 and rank == 0:
+    marks = sorted({int(v) for v in str(args.accuracy_steps).split(",") if v.strip() and int(v) > 0})
+    if marks and rank == 0:
         a32, a64 = zr.Scene(zr.F32), zr.Scene(zr.F64)
         a32.from_recipe(r)
         a64.from_recipe(r)
-        a32.step(args.accuracy_steps)
-        a64.step(args.accuracy_steps)
-        acc = {"substeps": args.accuracy_steps, "reference": "FP64 GPU path (pinned to the FP64 oracle by tests/test_gpu_parity.py)"}
-        for f in ("x", "v", "F", "d"):
-            e = np.abs(a32.get(f) - a64.get(f))
-            acc[f] = {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
-        acc["x"]["note"] = "metres in a unit domain (domain-relative)"
+        acc = {"reference": "FP64 GPU path", "x_unit": "metres in a unit domain (domain-relative)", "at": []}
+        done = 0
+        for mk in marks:
+            a32.step(mk - done)
+            a64.step(mk - done)
+            done = mk
+            row = {"substeps": mk}
+            for f in ("x", "v", "F", "d"):
+                e = np.abs(a32.get(f) - a64.get(f))
+                row[f] = {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
+            acc["at"].append(row)
         del a32, a64
+
+    # FP32 and FP64 GPU paths against the FP64 oracle on the elastic cube (32,768 particles, dx = 1/64,
+    # corotated E = 1e4, sticky ground), the scene the 1e-4 position bound is stated on
+    vs_oracle = None
+    if rank == 0 and not args.no_cpu and args.oracle_steps > 0:
+        vs_oracle = error_vs_oracle(args.oracle_steps)
 
     # CPU baseline: the oracle restatement on a bounded sample of the same workload, all host threads
     cpu = None
@@ -466,12 +536,13 @@ def run_ours(args, world, rank):
     cfg["particles"] = int(n)
     cfg["active_blocks"] = int(blocks)
     cfg["particle_groups"] = int(groups)
+    cfg["schedule"] = schedule
     line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded recipe)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
             "clocks": clock_info, "fp64_path": {"value": fp64_value, "unit": "particle-substeps/s", "fp32_over_fp64": value / world / fp64_value},
-            "fp32_vs_fp64_error": acc, "fp64_fallbacks": stats["fallbacks"]}
+            "fp32_vs_fp64_error": acc, "error_vs_fp64_oracle": vs_oracle, "fp64_fallbacks": stats["fallbacks"]}
     return line if rank == 0 else None
 
 

@@ -129,6 +129,21 @@ int zr_scene_binning(zr_scene* s, uint64_t* sorted_keys, int32_t* order, int32_t
  * g2p; and the number of timed substeps. Timing runs the substeps without CUDA graphs. */
 int zr_scene_set_timing(zr_scene* s, int on);
 int zr_scene_get_timing(zr_scene* s, double out5[5], int64_t* steps);
+/* Launch schedule of the substep: the P2G form (fused: one kernel that evaluates the stress; split: a
+ * stress kernel writing a per-particle payload that a scatter kernel streams into shared memory with bulk
+ * asynchronous copies), the particles staged per P2G chunk and the staging buffers of the split form, the
+ * P2G CTAs per SM and the G2P threads per CTA (particles per warp pass over a block). No reference
+ * counterpart: Ziran's CPU loops are scheduled by TBB (MpmSimulationBase.cpp:669-855, 1269-1515).
+ * mode 0 = a fixed default schedule, 1 = autotuned: measured with trial substeps on the scene's own state
+ * when it first steps (the trials are rolled back) and cached per workload class in the process,
+ * 2 = autotuned, re-measured per batch. Schedules differ only in the order of floating-point sums.
+ * get: out6 = fused, chunk, buffers, CTAs per SM, G2P threads, 1 if measured. set: in5 = fused (1 or 0),
+ * (chunk, buffers) one of (512, 1), (512, 2), (256, 2) in FP32 or (256, 1), (256, 2), (128, 2) in FP64
+ * (ignored when fused), CTAs per SM, G2P threads (64, 128 or 256); an explicit schedule disables the
+ * autotuner for the scene. */
+int zr_scene_set_autotune(zr_scene* s, int mode);
+int zr_scene_set_schedule(zr_scene* s, const int32_t in5[5]);
+int zr_scene_get_schedule(zr_scene* s, int32_t out6[6]);
 /* kernels launched per substep (CUDA-graph node count) and device bytes held by the scene. */
 int zr_scene_stats(zr_scene* s, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
 
@@ -186,6 +201,8 @@ int zr_batch_get_field(zr_batch* b, int slot, int field, void* out, int dtype);
 int zr_batch_reductions(zr_batch* b, int slot, double out[7]);
 int64_t zr_batch_count(zr_batch* b, int slot);
 int zr_batch_set_timing(zr_batch* b, int on);
+int zr_batch_set_autotune(zr_batch* b, int mode);
+int zr_batch_get_schedule(zr_batch* b, int32_t out6[6]);
 int zr_batch_get_timing(zr_batch* b, double out5[5], int64_t* steps);
 int zr_batch_stats(zr_batch* b, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
 const char* zr_batch_last_error(zr_batch* b);

@@ -21,9 +21,11 @@ def test_batch_matches_single_scenes(prec):
         singles.append(sc)
     b.commit()
     b.step(25)
-    # batch and single runs differ only in the order of the atomic grid sums. In FP32 that rounding
-    # reaches the damage update, whose threshold (phi > 1) amplifies it: d (in [0,1]) is held to 1e-4.
-    tol = {"x": 1e-11, "v": 1e-11, "F": 1e-11, "d": 1e-11} if prec == 8 else {"x": 2e-6, "v": 2e-6, "F": 2e-6, "d": 1e-4}
+    # batch and single runs differ only in the order of the floating-point grid sums (atomics, and the P2G
+    # form the autotuner picks for each: a batch and a lone scene are tuned separately). In FP32 that is a
+    # few ulps of v ~ 1 m/s per substep; the damage update's threshold (phi > 1) amplifies it: d (in [0,1])
+    # is held to 1e-4.
+    tol = {"x": 1e-11, "v": 1e-11, "F": 1e-11, "d": 1e-11} if prec == 8 else {"x": 1e-5, "v": 1e-5, "F": 1e-5, "d": 1e-4}
     for k, sc in enumerate(singles):
         sc.step(25)
         for f in ("x", "v", "F", "d"):

@@ -40,6 +40,24 @@ def test_elastic_box_fp32_within_1e4_of_fp64_oracle():
     assert e["F"][0] < 1e-3, e
 
 
+def test_elastic_cube_200_substeps_against_fp64_oracle():
+    """The plain FP64 scene the position bound is stated on: a 0.25 m corotated cube at dx = 1/64
+    (32,768 particles, E = 1e4, nu = 0.3, rho = 1000, v0 = (0, -1, 0), gravity, sticky ground at y = 0.05,
+    dt = 1e-4), 200 substeps. FP32: max position error <= 1e-4 of the unit domain; FP64: <= 1e-11."""
+    d = scenes.elastic_box(size=0.25)
+    assert len(d["m"]) == 32768
+    o = scenes.oracle_scene(d, 8)
+    o.step(200)
+    r = o.state()
+    for prec, xtol, ftol in ((zr.F32, 1e-4, 1e-3), (zr.F64, 1e-11, 1e-8)):
+        s = scenes.gpu_scene(d, prec)
+        s.step(200)
+        e = scenes.errors(scenes.gpu_state(s), r)
+        assert e["x"][0] <= xtol, (prec, e)
+        assert e["F"][0] <= ftol, (prec, e)
+    assert d["x"][:, 1].min() - r["x"][:, 1].min() > 0.015  # the cube fell ~2 cm (1 m/s for 0.02 s plus gravity)
+
+
 @pytest.mark.parametrize("steps", [1, 30])
 def test_aniso_slab_fp64_matches_oracle(steps):
     d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0)

@@ -89,6 +89,9 @@ def load_library(build_if_needed=True):
         "zr_scene_binning": (i32, [vp, P(C.c_uint64), P(C.c_int32), P(C.c_int32), P(i64), P(C.c_uint64), P(i64)]),
         "zr_scene_set_timing": (i32, [vp, i32]),
         "zr_scene_get_timing": (i32, [vp, pd, P(i64)]),
+        "zr_scene_set_autotune": (i32, [vp, i32]),
+        "zr_scene_set_schedule": (i32, [vp, P(i32)]),
+        "zr_scene_get_schedule": (i32, [vp, P(i32)]),
         "zr_scene_stats": (i32, [vp, P(i64), P(i64), P(i64)]),
         "zr_recipe_default": (i32, [i32, P(Recipe)]),
         "zr_recipe_count": (i64, [P(Recipe)]),
@@ -107,6 +110,8 @@ def load_library(build_if_needed=True):
         "zr_batch_count": (i64, [vp, i32]),
         "zr_batch_set_timing": (i32, [vp, i32]),
         "zr_batch_get_timing": (i32, [vp, pd, P(i64)]),
+        "zr_batch_set_autotune": (i32, [vp, i32]),
+        "zr_batch_get_schedule": (i32, [vp, P(i32)]),
         "zr_batch_stats": (i32, [vp, P(i64), P(i64), P(i64)]),
         "zr_batch_last_error": (C.c_char_p, [vp]),
         "zr_version": (C.c_char_p, []),
@@ -312,6 +317,20 @@ class Scene:
         self._check(self.L.zr_scene_get_timing(self.h, _dp(out), C.byref(steps)))
         return dict(zip(("sort", "activate", "p2g", "grid", "g2p"), out)), steps.value
 
+    def set_autotune(self, mode):
+        """0 fixed default schedule, 1 autotuned and cached per workload class, 2 re-measured per batch."""
+        self._check(self.L.zr_scene_set_autotune(self.h, int(mode)))
+
+    def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=False):
+        """chunk/buffers select the split P2G form's staging; fused=True selects the one-kernel P2G."""
+        arr = (C.c_int32 * 5)(int(fused), chunk, buffers, p2g_ctas_per_sm, g2p_threads)
+        self._check(self.L.zr_scene_set_schedule(self.h, arr))
+
+    def schedule(self):
+        rc, out = _schedule(self.L.zr_scene_get_schedule, self.h)
+        self._check(rc)
+        return out
+
     def stats(self):
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self.L.zr_scene_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
@@ -390,10 +409,25 @@ class Batch:
         self._check(self.L.zr_batch_get_timing(self.h, _dp(out), C.byref(steps)))
         return dict(zip(("sort", "activate", "p2g", "grid", "g2p"), out)), steps.value
 
+    def set_autotune(self, mode):
+        self._check(self.L.zr_batch_set_autotune(self.h, int(mode)))
+
+    def schedule(self):
+        rc, out = _schedule(self.L.zr_batch_get_schedule, self.h)
+        self._check(rc)
+        return out
+
     def stats(self):
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self.L.zr_batch_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return {"launches_per_step": a.value, "device_bytes": b.value, "fallbacks": c.value}
+
+
+def _schedule(fn, h):
+    out = (C.c_int32 * 6)()
+    rc = fn(h, out)
+    return rc, {"fused": bool(out[0]), "chunk": out[1], "buffers": out[2], "p2g_ctas_per_sm": out[3], "g2p_threads": out[4], "tuned": bool(out[5])}
+
 
 
 class Server:

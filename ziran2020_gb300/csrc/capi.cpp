@@ -17,6 +17,9 @@
 using namespace zr;
 
 struct zr_scene {
+    int autotune = -1; // -1: the engine's default
+    bool has_schedule = false;
+    zr::Schedule schedule;
     double last_ms = 0;
     int64_t last_groups = 0, last_blocks = 0;
     int precision = ZR_F32;
@@ -28,6 +31,7 @@ struct zr_scene {
 };
 
 struct zr_batch {
+    int autotune = -1;
     double last_ms = 0;
     int precision = ZR_F32;
     std::vector<std::unique_ptr<SceneDesc>> descs;
@@ -375,6 +379,12 @@ static int commit(zr_scene* s)
     if (s->desc.materials.empty()) return set_err(s->err, ZR_ERR_STATE, "no constitutive model attached");
     // particles without an explicit model take the first one
     s->eng = make_engine(s->precision);
+    if (s->autotune >= 0) s->eng->set_autotune(s->autotune);
+    if (s->has_schedule && s->eng->set_schedule(s->schedule)) {
+        s->err = s->eng->last_error();
+        s->eng.reset();
+        return ZR_ERR_ARG;
+    }
     std::vector<const SceneDesc*> v{ &s->desc };
     int rc = s->eng->load(v);
     if (rc) {
@@ -511,6 +521,51 @@ int zr_scene_set_timing(zr_scene* s, int on)
     NEED_ENGINE(s);
     s->eng->set_timing(on != 0);
     s->eng->reset_timing();
+    return ZR_OK;
+}
+
+int zr_scene_set_autotune(zr_scene* s, int mode)
+{
+    if (!s || mode < 0 || mode > 2) return ZR_ERR_ARG;
+    s->autotune = mode;
+    if (s->eng) s->eng->set_autotune(mode);
+    return ZR_OK;
+}
+
+int zr_scene_set_schedule(zr_scene* s, const int32_t in5[5])
+{
+    if (!s || !in5) return ZR_ERR_ARG;
+    zr::Schedule sc;
+    sc.fused = in5[0];
+    sc.chunk = in5[1];
+    sc.buffers = in5[2];
+    sc.scatter_ctas_per_sm = in5[3];
+    sc.g2p_threads = in5[4];
+    if (s->eng) {
+        int rc = s->eng->set_schedule(sc);
+        if (rc) s->err = s->eng->last_error();
+        return rc;
+    }
+    s->schedule = sc;
+    s->has_schedule = true;
+    return ZR_OK;
+}
+
+static void schedule_out(const zr::Schedule& sc, int32_t out6[6])
+{
+    out6[0] = sc.fused;
+    out6[1] = sc.chunk;
+    out6[2] = sc.buffers;
+    out6[3] = sc.scatter_ctas_per_sm;
+    out6[4] = sc.g2p_threads;
+    out6[5] = sc.tuned;
+}
+
+int zr_scene_get_schedule(zr_scene* s, int32_t out6[6])
+{
+    NEED_ENGINE(s);
+    if (!out6) return ZR_ERR_ARG;
+    schedule_out(s->eng->schedule(), out6);
     return ZR_OK;
 }
 
@@ -657,6 +712,7 @@ int zr_batch_commit(zr_batch* b)
     if (b->committed) return ZR_OK;
     if (b->descs.empty()) return set_err(b->err, ZR_ERR_STATE, "empty batch");
     b->eng = make_engine(b->precision);
+    if (b->autotune >= 0) b->eng->set_autotune(b->autotune);
     std::vector<const SceneDesc*> v;
     for (auto& d : b->descs) v.push_back(d.get());
     int rc = b->eng->load(v);
@@ -741,6 +797,22 @@ int zr_batch_set_timing(zr_batch* b, int on)
     return ZR_OK;
 }
 
+int zr_batch_set_autotune(zr_batch* b, int mode)
+{
+    if (!b || mode < 0 || mode > 2) return ZR_ERR_ARG;
+    b->autotune = mode;
+    if (b->eng) b->eng->set_autotune(mode);
+    return ZR_OK;
+}
+
+int zr_batch_get_schedule(zr_batch* b, int32_t out6[6])
+{
+    NEED_BATCH(b);
+    if (!out6) return ZR_ERR_ARG;
+    schedule_out(b->eng->schedule(), out6);
+    return ZR_OK;
+}
+
 int zr_batch_get_timing(zr_batch* b, double out5[5], int64_t* steps)
 {
     NEED_BATCH(b);
@@ -804,7 +876,8 @@ namespace {
 double scene_bytes(int precision, int64_t n)
 {
     const double s = precision == ZR_F64 ? 8 : 4, nodes = precision == ZR_F64 ? 32 : 64;
-    const double per_particle = 2 * (28 * s + 4) + 8 + 8 + 4 + 4 + 4;
+    // two pool copies, keys (in, sorted), sort values, iota, group starts, and the P2G payload (27 fields at 9/8 density)
+    const double per_particle = 2 * (28 * s + 4) + 8 + 8 + 4 + 4 + 4 + 27 * s * 9 / 8;
     const double groups = (double)n / (nodes * 4) + 64;
     return n * per_particle + 8 * groups * (10 * nodes * s + 64);
 }

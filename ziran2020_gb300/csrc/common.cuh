@@ -110,9 +110,10 @@ enum : uint32_t {
     FLAG_OUT_OF_DOMAIN = 1u << 3, // a base node left the scene's domain
     FLAG_CAPACITY = 1u << 4, // active-block table or grid storage full
     FLAG_TIMEOUT = 1u << 5, // a bounded wait on a copy barrier gave up
+    FLAG_CHECK = 1u << 6, // an internal consistency check failed (status.check_code says which); the access was skipped
     FLAG_ABORT = 1u << 31, // processing stopped at status.abort_step; later substeps were no-ops
 };
-constexpr uint32_t ABORTING = FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_CAPACITY | FLAG_TIMEOUT;
+constexpr uint32_t ABORTING = FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_CAPACITY | FLAG_TIMEOUT | FLAG_CHECK;
 
 struct DevStatus {
     uint32_t flags;
@@ -125,7 +126,9 @@ struct DevStatus {
     uint32_t fallback; // polar decompositions that took the FP64 SVD path (cumulative)
     uint32_t max_blocks_seen;
     uint32_t max_groups_seen;
-    uint32_t pad[6];
+    uint32_t check_code; // first failed internal check (0 = none)
+    uint32_t check_count;
+    uint32_t pad[4];
 };
 
 constexpr int MAX_OBJECTS = 8;

@@ -57,6 +57,18 @@ struct StepReport {
     uint32_t n_groups = 0, n_blocks = 0, fallback = 0;
 };
 
+// Launch schedule of the substep (what the autotuner picks). None of these changes the arithmetic beyond
+// the order of floating-point sums.
+struct Schedule {
+    int fused = 0; // P2G: 1 = one kernel evaluating the stress itself; 0 = a stress kernel writing a payload that a
+                   // scatter kernel streams into shared memory with bulk asynchronous copies
+    int chunk = 0; // P2G: particles per chunk staged in shared memory by one bulk copy per payload field
+    int buffers = 1; // P2G: staging buffers (2: the next chunk's copy overlaps the whole current chunk)
+    int scatter_ctas_per_sm = 0; // P2G scatter: persistent CTAs per SM
+    int g2p_threads = 0; // G2P: threads per CTA, i.e. particles per pass over a group
+    int tuned = 0; // 1 when chosen by the autotuner's measurements
+};
+
 struct KernelTimes {
     // milliseconds accumulated per phase while timing is enabled
     double sort = 0, blocks = 0, p2g = 0, grid = 0, g2p = 0;
@@ -99,6 +111,10 @@ public:
     virtual int64_t device_bytes() const = 0;
     virtual int use_graph(bool on) = 0;
     virtual int kernel_launches_per_step() const = 0;
+    // autotuner: 0 off (default schedule), 1 on with a process-wide cache, 2 on and re-measured per batch
+    virtual int set_autotune(int mode) = 0;
+    virtual Schedule schedule() const = 0;
+    virtual int set_schedule(const Schedule& s) = 0;
     virtual std::string last_error() const = 0;
 };
 

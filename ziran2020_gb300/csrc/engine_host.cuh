@@ -3,6 +3,10 @@
 #pragma once
 #include "engine_impl.cuh"
 
+#include <cstdlib>
+#include <map>
+#include <mutex>
+
 #define ZR_CUDA(call)                                                                                      \
     do {                                                                                                   \
         cudaError_t e_ = (call);                                                                           \
@@ -30,9 +34,13 @@ inline int bitlen(uint64_t v)
 template <class T>
 class Engine final : public EngineBase {
     using L = typename LayoutOf<T>::type;
-    static constexpr int NT_P2G = P2GShape<T>::NT;
-    static constexpr int NT_G2P = 128;
     static constexpr int GRAPH_K = 8; // substeps per multi-step graph (even: returns to the same buffer)
+    // compiled schedule variants. P2G scatter: (particles per staged chunk, staging buffers); the large chunk
+    // holds a whole occupied block of 8 particles per cell. G2P: threads per CTA.
+    static constexpr int CH_BIG = sizeof(T) == 4 ? 512 : 256;
+    static constexpr int VAR_CHUNK[3] = { CH_BIG, CH_BIG, CH_BIG / 2 };
+    static constexpr int VAR_NBUF[3] = { 1, 2, 2 };
+    static constexpr int G2P_NT[3] = { 64, 128, 256 };
 
 public:
     Engine() { init_device(); }
@@ -120,7 +128,7 @@ public:
                 ZR_CUDA(cudaMemcpyAsync(grown_pid[0] + np[q].first, old_pid + src_first[q], 4 * np[q].count, cudaMemcpyDeviceToDevice, stream_));
             }
             ZR_CUDA(cudaStreamSynchronize(stream_));
-            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_ };
+            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_, pay_ };
             for (void* p : olds)
                 if (p) cudaFree(p);
             pool_[0] = grown_pool[0];
@@ -128,9 +136,13 @@ public:
             pid_[0] = grown_pid[0];
             pid_[1] = grown_pid[1];
             cap_ = (uint64_t)cap;
+            pay_ = nullptr;
+            // P2G payload: NPAY fields of sorted particles at q + q/8, plus the copy granularity at the end
+            pstride_ = (int64_t)((pay_pos((uint64_t)cap) + 64 + 63) & ~(uint64_t)63);
             if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
-                || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap))
+                || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_))
                 return ZR_ERR_CUDA_;
+            ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
             k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
             size_t sb = 0, se = 0;
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, cap, 0, 64, stream_));
@@ -167,8 +179,13 @@ public:
         kl_ = kl;
         cur_ = dst;
         models_ = 0;
-        for (auto& sp : h_scenes_)
+        any_damage_ = false;
+        for (auto& sp : h_scenes_) {
             for (int k = 0; k < sp.n_materials; k++) models_ |= sp.materials[k].model == MODEL_COROTATED ? 1 : 2;
+            any_damage_ = any_damage_ || sp.damage;
+        }
+        tuned_ = false;
+        sorted_storage_ = false;
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * scene_cap_, stream_));
         ZR_CUDA(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), sizeof(SceneParams<T>) * h_scenes_.size(), cudaMemcpyHostToDevice, stream_));
@@ -218,11 +235,28 @@ public:
         if (nsteps < 0) return arg("nsteps must be >= 0");
         int done = 0;
         StepReport r;
+        int rc = 0;
+        if (nsteps > 0 && !tuned_ && !fixed_schedule_ && !autotune_cached()) {
+            // the trials must see the particles in sorted storage order, which one substep of G2P produces
+            if (!sorted_storage_) rc = run_steps(1, r, done);
+            if (!rc && done < nsteps) rc = autotune_trials();
+        }
+        if (!rc) rc = run_steps(nsteps - done, r, done);
+        r.steps_done = done;
+        if (rep) *rep = r;
+        return rc;
+    }
+
+    // Advance nsteps substeps with the current schedule; r accumulates the report, done counts finished substeps.
+    // An aborted substep is retried after growing the grid (capacity) or reported with the state left at its start.
+    int run_steps(int nsteps, StepReport& r, int& done)
+    {
+        const int target = done + nsteps;
         int grow_rounds = 0;
-        while (done < nsteps) {
+        while (done < target) {
             ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
             const int cur0 = cur_;
-            int todo = nsteps - done;
+            int todo = target - done;
             if (!timing_ && graphs_on_) {
                 int rcg = prepare_graphs(todo);
                 if (rcg) return rcg;
@@ -244,11 +278,13 @@ public:
             if (!(hst_->flags & FLAG_ABORT)) {
                 cur_ = (cur0 + todo) & 1;
                 done += todo;
+                sorted_storage_ = true;
                 break;
             }
             const int k = hst_->abort_step;
             done += k;
             cur_ = (cur0 + k) & 1;
+            if (k > 0) sorted_storage_ = true;
             // the aborted substep may have left partial grid sums, hash entries or next keys behind
             ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
@@ -256,22 +292,21 @@ public:
             k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
             ZR_CUDA(cudaStreamSynchronize(stream_));
             const uint32_t f = hst_->flags;
-            if ((f & FLAG_CAPACITY) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT)) && grow_rounds < 6) {
+            if ((f & FLAG_CAPACITY) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK)) && grow_rounds < 6) {
                 grow_rounds++;
                 int rc2 = alloc_grid(b_cap_ * 2);
                 if (rc2) return rc2;
                 continue; // retry the aborted substep with a larger grid
             }
-            r.steps_done = done;
-            if (rep) *rep = r;
             if (f & FLAG_NONFINITE) return fail(ZR_ERR_NONFINITE_, "non-finite particle state at substep " + std::to_string(done));
             if (f & FLAG_OUT_OF_DOMAIN) return fail(ZR_ERR_OUT_OF_DOMAIN_, "a particle left its scene's domain at substep " + std::to_string(done));
             if (f & FLAG_CFL) return fail(ZR_ERR_CFL_, "a particle moved more than one cell at substep " + std::to_string(done) + " (reduce dt)");
             if (f & FLAG_TIMEOUT) return fail(ZR_ERR_TIMEOUT_, "bounded wait expired at substep " + std::to_string(done));
+            if (f & FLAG_CHECK)
+                return fail(ZR_ERR_STATE_, "internal consistency check " + std::to_string(hst_->check_code) + " failed " + std::to_string(hst_->check_count) +
+                        " times at substep " + std::to_string(done));
             return fail(ZR_ERR_CAPACITY_, "active-block capacity exhausted");
         }
-        r.steps_done = done;
-        if (rep) *rep = r;
         return 0;
     }
 
@@ -445,6 +480,36 @@ public:
     }
     int kernel_launches_per_step() const override { return launches_per_step_; }
 
+    // Schedule autotuner. The tunable launch shapes change no arithmetic beyond the order of floating-point
+    // sums: P2G particles per staged chunk and P2G CTAs per SM, G2P threads per CTA (particles per warp
+    // per pass over a group). Each candidate runs single trial substeps on the current state, timed with
+    // CUDA events on the engine's stream; the state is rolled back after each trial (the trial writes only
+    // the other particle buffer, the next-substep keys and the scene clocks, which are restored). The
+    // choice is cached per (precision, models, damage, particle-count and scene-count magnitude).
+    int set_autotune(int mode) override
+    {
+        autotune_mode_ = mode;
+        fixed_schedule_ = false;
+        tuned_ = false;
+        return 0;
+    }
+    Schedule schedule() const override { return sched_; }
+    int set_schedule(const Schedule& sc) override
+    {
+        if ((!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0 || sc.scatter_ctas_per_sm < 1
+            || sc.scatter_ctas_per_sm > 8)
+            return arg("schedule: unknown (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
+        sched_ = sc;
+        if (sc.fused) {
+            sched_.chunk = FusedShape<T>::CHUNK;
+            sched_.buffers = 0;
+        }
+        sched_.tuned = 0;
+        fixed_schedule_ = true; // explicit schedules are not overridden by the autotuner
+        drop_graphs();
+        return 0;
+    }
+
 private:
     int dev_ = 0, nsm_ = 0;
     cudaStream_t stream_ = nullptr;
@@ -472,9 +537,18 @@ private:
     DevStatus* hst_ = nullptr;
     void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
-    int occ_p2g_ = 1, occ_g2p_ = 1;
-    int occ_p2g_m_[3] = { 1, 1, 1 };
+    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[3] = { 1, 1, 1 }, occ_fused_[3] = { 1, 1, 1 };
     int models_ = 3; // bit 0: a corotated material is present, bit 1: a Neo-Hookean (Borden) material
+    bool any_damage_ = false;
+    T* pay_ = nullptr;
+    int64_t pstride_ = 0;
+    Schedule sched_{ 0, VAR_CHUNK[0], VAR_NBUF[0], 2, 128, 0 };
+    int autotune_mode_ = 1; // 0 off (defaults), 1 on (cached), 2 always re-tune on a new batch
+    bool tuned_ = false;
+    bool fixed_schedule_ = false;
+    bool sorted_storage_ = false; // particles sit in the sorted order of their last substep (after one G2P)
+    void* scenes_backup_ = nullptr;
+    size_t scenes_backup_bytes_ = 0;
     bool graphs_on_ = true, timing_ = false;
     cudaGraphExec_t g1_[2] = { nullptr, nullptr }, gk_[2] = { nullptr, nullptr };
     int launches_per_step_ = 0;
@@ -599,17 +673,24 @@ private:
             init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
             return;
         }
-        cudaFuncSetAttribute(k_p2g<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
-        cudaFuncSetAttribute(k_p2g<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
-        cudaFuncSetAttribute(k_p2g<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2GShape<T>::dyn_bytes);
-        for (int m = 0; m < 3; m++) {
-            int o = 1;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, m == 0 ? k_p2g<T, 1> : (m == 1 ? k_p2g<T, 2> : k_p2g<T, 3>), NT_P2G, P2GShape<T>::dyn_bytes);
-            occ_p2g_m_[m] = std::max(1, o);
-        }
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_, k_g2p<T, NT_G2P>, NT_G2P, 0);
-        occ_p2g_ = std::max(1, occ_p2g_);
-        occ_g2p_ = std::max(1, occ_g2p_);
+        scatter_setup<0>();
+        scatter_setup<1>();
+        scatter_setup<2>();
+        fused_setup<1>(0);
+        fused_setup<2>(1);
+        fused_setup<3>(2);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[0], k_stress<T, 1>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 3>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[0], k_g2p<T, G2P_NT[0]>, G2P_NT[0], 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[1], k_g2p<T, G2P_NT[1]>, G2P_NT[1], 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[2], k_g2p<T, G2P_NT[2]>, G2P_NT[2], 0);
+        for (int& o : occ_scatter_) o = std::max(1, o);
+        for (int& o : occ_stress_) o = std::max(1, o);
+        for (int& o : occ_g2p_) o = std::max(1, o);
+        sched_.scatter_ctas_per_sm = occ_scatter_[0];
+        sched_.tuned = 0;
+        if (const char* e = std::getenv("ZR_AUTOTUNE")) autotune_mode_ = std::atoi(e);
     }
 
     int alloc(void** p, size_t bytes)
@@ -675,6 +756,7 @@ private:
 
     int rekey()
     {
+        sorted_storage_ = false; // new positions: the storage order may no longer follow the cells
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
         ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
@@ -708,6 +790,8 @@ private:
         a.pout = pool(parity ^ 1);
         a.g_start = g_start_;
         a.g_nbr = g_nbr_;
+        a.pay = pay_;
+        a.pstride = pstride_;
         a.b_key = b_key_;
         a.acc = acc_;
         a.vel = vel_;
@@ -736,17 +820,43 @@ private:
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+        k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
-        if (models_ == 1)
-            k_p2g<T, 1><<<nsm_ * occ_p2g_m_[0], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
-        else if (models_ == 2)
-            k_p2g<T, 2><<<nsm_ * occ_p2g_m_[1], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
-        else
-            k_p2g<T, 3><<<nsm_ * occ_p2g_m_[2], NT_P2G, P2GShape<T>::dyn_bytes, stream_>>>(a);
+        if (sched_.fused) {
+            const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[models_slot()]);
+            if (models_ == 1)
+                k_p2g_fused<T, 1><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            else if (models_ == 2)
+                k_p2g_fused<T, 2><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            else
+                k_p2g_fused<T, 3><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+        }
+        else {
+            if (models_ == 1)
+                k_stress<T, 1><<<nsm_ * occ_stress_[0], 256, 0, stream_>>>(a);
+            else if (models_ == 2)
+                k_stress<T, 2><<<nsm_ * occ_stress_[1], 256, 0, stream_>>>(a);
+            else
+                k_stress<T, 3><<<nsm_ * occ_stress_[2], 256, 0, stream_>>>(a);
+            const int vi = std::max(0, variant_index(sched_.chunk, sched_.buffers));
+            const int sctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_scatter_[vi]);
+            if (vi == 0)
+                launch_scatter<0>(a, sctas);
+            else if (vi == 1)
+                launch_scatter<1>(a, sctas);
+            else
+                launch_scatter<2>(a, sctas);
+        }
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
         k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));
-        k_g2p<T, NT_G2P><<<nsm_ * occ_g2p_, NT_G2P, 0, stream_>>>(a);
+        const int gi = std::max(0, g2p_index(sched_.g2p_threads));
+        if (gi == 0)
+            k_g2p<T, G2P_NT[0]><<<nsm_ * occ_g2p_[0], G2P_NT[0], 0, stream_>>>(a);
+        else if (gi == 1)
+            k_g2p<T, G2P_NT[1]><<<nsm_ * occ_g2p_[1], G2P_NT[1], 0, stream_>>>(a);
+        else
+            k_g2p<T, G2P_NT[2]><<<nsm_ * occ_g2p_[2], G2P_NT[2], 0, stream_>>>(a);
         k_step_end<T><<<1, 256, 0, stream_>>>(d_scenes_, n_scenes(), st_);
         if (ev) ZR_CUDA(cudaEventRecord(ev[5], stream_));
         ZR_CUDA(cudaGetLastError());
@@ -840,6 +950,178 @@ private:
         return 0;
     }
 
+    static int variant_index(int chunk, int buffers)
+    {
+        for (int v = 0; v < 3; v++)
+            if (VAR_CHUNK[v] == chunk && VAR_NBUF[v] == buffers) return v;
+        return -1;
+    }
+    template <int V>
+    void scatter_setup()
+    {
+        using S = ScatterShape<T, VAR_CHUNK[V], VAR_NBUF[V]>;
+        auto k = k_scatter<T, VAR_CHUNK[V], VAR_NBUF[V]>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::dyn_bytes);
+        // the staging buffers are the point: ask for the largest shared-memory carveout
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_scatter_[V], k, S::NT, S::dyn_bytes);
+    }
+    template <int M>
+    void fused_setup(int slot)
+    {
+        cudaFuncSetAttribute(k_p2g_fused<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k_p2g_fused<T, M>, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[slot], k_p2g_fused<T, M>, FusedShape<T>::NT, FusedShape<T>::dyn_bytes);
+        occ_fused_[slot] = std::max(1, occ_fused_[slot]);
+    }
+    int models_slot() const { return models_ == 1 ? 0 : (models_ == 2 ? 1 : 2); }
+    template <int V>
+    void launch_scatter(const StepArgs<T>& a, int ctas)
+    {
+        using S = ScatterShape<T, VAR_CHUNK[V], VAR_NBUF[V]>;
+        k_scatter<T, VAR_CHUNK[V], VAR_NBUF[V]><<<ctas, S::NT, S::dyn_bytes, stream_>>>(a);
+    }
+    static int g2p_index(int nt) { return nt == G2P_NT[0] ? 0 : (nt == G2P_NT[1] ? 1 : (nt == G2P_NT[2] ? 2 : -1)); }
+
+    static std::map<uint64_t, Schedule>& tune_cache()
+    {
+        static std::map<uint64_t, Schedule> c;
+        return c;
+    }
+    static std::mutex& tune_mutex()
+    {
+        static std::mutex m;
+        return m;
+    }
+    uint64_t tune_key() const
+    {
+        return (uint64_t)sizeof(T) | ((uint64_t)models_ << 4) | ((uint64_t)any_damage_ << 6) | ((uint64_t)bitlen(N_) << 8)
+            | ((uint64_t)bitlen((uint64_t)n_scenes()) << 16) | ((uint64_t)nsm_ << 24);
+    }
+
+    // one trial substep with schedule sc on the current state; p2g / g2p milliseconds; state rolled back
+    int trial(const Schedule& sc, float& p2g_ms, float& g2p_ms, bool& aborted_out)
+    {
+        sched_ = sc;
+        if ((int)ev_.size() < 6) {
+            size_t old = ev_.size();
+            ev_.resize(6);
+            for (size_t i = old; i < ev_.size(); i++) ZR_CUDA(cudaEventCreate(&ev_[i]));
+        }
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        int rc = enqueue_step(cur_, ev_.data());
+        if (rc) return rc;
+        ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        ZR_CUDA(cudaEventElapsedTime(&p2g_ms, ev_[2], ev_[3]));
+        ZR_CUDA(cudaEventElapsedTime(&g2p_ms, ev_[4], ev_[5]));
+        aborted_out = (hst_->flags & FLAG_ABORT) != 0;
+        // roll back: scene clocks, a clean grid after an aborted trial, the keys of the current buffer
+        ZR_CUDA(cudaMemcpyAsync(d_scenes_, scenes_backup_, sizeof(SceneParams<T>) * h_scenes_.size(), cudaMemcpyDeviceToDevice, stream_));
+        if (aborted_out) {
+            ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
+            ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+        }
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
+        ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    // A schedule without measuring: the fixed default (mode 0) or a cached choice (mode 1). False when trials are needed.
+    bool autotune_cached()
+    {
+        if (autotune_mode_ == 0) {
+            sched_ = default_schedule();
+            tuned_ = true;
+            drop_graphs();
+            return true;
+        }
+        if (autotune_mode_ == 1) {
+            std::lock_guard<std::mutex> lk(tune_mutex());
+            auto it = tune_cache().find(tune_key());
+            if (it != tune_cache().end()) {
+                sched_ = it->second;
+                tuned_ = true;
+                drop_graphs();
+                return true;
+            }
+        }
+        return false;
+    }
+
+    Schedule default_schedule() const { return Schedule{ 0, VAR_CHUNK[0], VAR_NBUF[0], occ_scatter_[0], G2P_NT[1], 0 }; }
+
+    int autotune_trials()
+    {
+        tuned_ = true;
+        const size_t sb = sizeof(SceneParams<T>) * h_scenes_.size();
+        if (sb > scenes_backup_bytes_) {
+            dfree(scenes_backup_);
+            scenes_backup_bytes_ = 0;
+            if (alloc(&scenes_backup_, sb)) return ZR_ERR_CUDA_;
+            scenes_backup_bytes_ = sb;
+        }
+        ZR_CUDA(cudaMemcpyAsync(scenes_backup_, d_scenes_, sb, cudaMemcpyDeviceToDevice, stream_));
+        // P2G candidates with the default G2P, then G2P candidates with the chosen P2G
+        std::vector<Schedule> p2g_c;
+        for (int vi = 0; vi < 3; vi++)
+            for (int c = occ_scatter_[vi]; c >= std::max(1, occ_scatter_[vi] - 1); c--)
+                p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 1 });
+        const int of = occ_fused_[models_slot()];
+        for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 1 });
+        constexpr int REPS = 2; // the first run of a candidate warms caches and instruction memory
+        Schedule best = p2g_c[0];
+        float best_p2g = 1e30f, best_g2p = 1e30f;
+        for (const Schedule& sc : p2g_c) {
+            float mp = 1e30f;
+            for (int r = 0; r < REPS; r++) {
+                float p = 0, g = 0;
+                bool ab = false;
+                int rc = trial(sc, p, g, ab);
+                if (rc) return rc;
+                if (ab) { // the state cannot step (CFL, out of domain, capacity): keep defaults, the step reports it
+                    sched_ = default_schedule();
+                    drop_graphs();
+                    return 0;
+                }
+                mp = std::min(mp, p);
+            }
+            if (mp < best_p2g) {
+                best_p2g = mp;
+                best = sc;
+            }
+        }
+        for (int gi = 0; gi < 3; gi++) {
+            Schedule sc = best;
+            sc.g2p_threads = G2P_NT[gi];
+            float mg = 1e30f;
+            for (int r = 0; r < REPS; r++) {
+                float p = 0, g = 0;
+                bool ab = false;
+                int rc = trial(sc, p, g, ab);
+                if (rc) return rc;
+                if (ab) {
+                    sched_ = default_schedule();
+                    drop_graphs();
+                    return 0;
+                }
+                mg = std::min(mg, g);
+            }
+            if (mg < best_g2p) {
+                best_g2p = mg;
+                best.g2p_threads = sc.g2p_threads;
+            }
+        }
+        best.tuned = 1;
+        sched_ = best;
+        drop_graphs();
+        std::lock_guard<std::mutex> lk(tune_mutex());
+        tune_cache()[tune_key()] = best;
+        return 0;
+    }
+
     void collect_timing(int nsteps)
     {
         for (int s = 0; s < nsteps; s++) {
@@ -858,7 +1140,7 @@ private:
     {
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
-            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_ };
+            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -875,6 +1157,11 @@ private:
         st_ = nullptr;
         sort_tmp_ = sel_tmp_ = stage_ = nullptr;
         stage_bytes_ = 0;
+        pay_ = nullptr;
+        pstride_ = 0;
+        scenes_backup_ = nullptr;
+        scenes_backup_bytes_ = 0;
+        tuned_ = false;
         N_ = 0;
         cap_ = 0;
         scene_cap_ = 0;

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "engine.h"
 #include "physics.cuh"
+#include "tma.cuh"
 
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
@@ -72,6 +73,8 @@ struct StepArgs {
     Pool<T> pin, pout;
     const uint32_t* g_start;
     int32_t* g_nbr;
+    T* pay; // P2G payload, NPAY fields of pstride elements
+    int64_t pstride;
     uint64_t* b_key;
     T* acc;
     T* vel;
@@ -100,6 +103,14 @@ __device__ inline void raise_flag(DevStatus* st, uint32_t f)
 {
     uint32_t old = atomicOr(&st->flags, f | ((f & ABORTING) ? FLAG_ABORT : 0u));
     if ((f & ABORTING) && !(old & FLAG_ABORT)) atomicExch(&st->abort_step, (int32_t)st->step);
+}
+
+// an internal consistency check failed: record the first check's code, count, abort the substep
+__device__ inline void check_failed(DevStatus* st, uint32_t code)
+{
+    atomicCAS(&st->check_code, 0u, code);
+    atomicAdd(&st->check_count, 1u);
+    raise_flag(st, FLAG_CHECK);
 }
 
 __device__ inline bool aborted(const DevStatus* st) { return (*(volatile const uint32_t*)&st->flags & FLAG_ABORT) != 0; }
@@ -239,8 +250,140 @@ __global__ void k_activate(StepArgs<T> a)
 }
 
 // ---------------------------------------------------------------------------------------------------
-// P2G
+// neighbour slots: the grid slots of every group's block and its 7 neighbours at +1 block (read by the
+// P2G scatter and by G2P). A separate pass after activation, so that every slot is final when read.
 // ---------------------------------------------------------------------------------------------------
+template <class T>
+__global__ void k_nbr(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const uint32_t G = a.st->n_groups;
+    if (G > a.b_cap) return; // activation already raised FLAG_CAPACITY
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
+        const uint32_t g = t >> 3, dl = t & 7;
+        const uint64_t key0 = a.keys_sorted[a.g_start[g]];
+        uint32_t bi, bj, bk;
+        L::block_of_page(a.kl.page(key0), bi, bj, bk);
+        const uint64_t scene = a.kl.scene(key0);
+        const uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
+        const int slot = hash_find(a.h_keys, a.h_vals, a.h_mask, hk);
+        if (slot < 0) raise_flag(a.st, FLAG_CAPACITY);
+        a.g_nbr[t] = slot;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// P2G, in two kernels.
+//
+// k_stress (thread per sorted particle): stress V0 tau(F, g(d)) (FBasedMpmForceHelper.cpp:43-63) and a
+// 27-value payload per particle, written in sorted order: fractional index-space position
+// f = x/dx - base, m, A = m v - dx (m C) f, Bc = dx m C, K = -dt V0 tau / dx, d, and the particle's
+// cell inside its block. With xm = (delta - f) dx for stencil offset delta,
+//   m v + m C xm = A + Bc delta   and   dt f_i = K . (dw_i w_j w_k, w_i dw_j w_k, w_i w_j dw_k),
+// so a node receives m w, w (A + Bc delta) + K grad-hat w, d w and w. The force enters the momentum
+// directly (m v + dt f), which the grid update turns into v + f dt/m + g dt as the reference's
+// gridVelocityExplicitUpdate does (MpmSimulationBase.cpp:1197-1226).
+//
+// k_scatter (CTA per group, persistent): a producer warp streams each chunk of a group's payload from
+// HBM into shared memory with bulk asynchronous copies (double-buffered, mbarrier-synchronised); the
+// consumer threads, one per (cell, stencil x-offset), accumulate the 9 nodes x 6 fields of their cell's
+// particles in registers (all particles of a cell share the same 27 nodes), add them into a shared
+// 6x6x6 node tile, and after the group's last chunk the tile goes to the 8 neighbouring grid blocks as
+// vector atomics (MpmSimulationBase.cpp:669-855, AnisoFractureSimulation.h:161-176).
+//
+// Payload storage: field k of sorted particle q at pay[k * pstride + q + q/8]. The gap after every 8
+// particles carries over into shared memory with the copy and staggers the shared-memory banks of the
+// consumer lanes (one lane per cell, ~8 particles per cell).
+// ---------------------------------------------------------------------------------------------------
+constexpr int NPAY = 27;
+enum { Y_F = 0, Y_M = 3, Y_A = 4, Y_B = 7, Y_K = 16, Y_D = 25, Y_CELL = 26 };
+
+__host__ __device__ __forceinline__ uint64_t pay_pos(uint64_t q) { return q + (q >> 3); }
+
+// Stress and payload of one particle (storage slot j of pool P): fields Y_F..Y_D at y[f * S]; b gets the
+// base node. V0 tau(F) of the particle's model (FBasedMpmForceHelper.cpp:43-63) with the degradation g(d).
+template <class T, int MODELS>
+__device__ __forceinline__ void particle_payload(const Pool<T>& P, uint32_t j, const SceneParams<T>& sp, T* y, int64_t S, int (&b)[3],
+    uint32_t& fallbacks)
+{
+    using L = typename LayoutOf<T>::type;
+    T x[3], v[3], Cm[9], F[9];
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        x[e] = P.f[(P_X + e) * P.stride + j];
+        v[e] = P.f[(P_V + e) * P.stride + j];
+    }
+#pragma unroll
+    for (int e = 0; e < 9; e++) {
+        Cm[e] = P.f[(P_C + e) * P.stride + j];
+        F[e] = P.f[(P_F + e) * P.stride + j];
+    }
+    const T mass = P.f[P_M * P.stride + j], V0 = P.f[P_V0 * P.stride + j];
+    const bool damage = sp.damage != 0;
+    const T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
+    const uint32_t mat = P.pid[j] >> L::index_bits;
+    const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+    T tau[9];
+    if (MODELS == 1 || (MODELS == 3 && mt.model == MODEL_COROTATED)) {
+        if (tau_corotated(mt, F, tau)) fallbacks++;
+    }
+    else
+        tau_nhb(mt, F, (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1, tau);
+    const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt;
+    T fr[3];
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        const T xs = mul_rn(x[e], inv_dx);
+        b[e] = int_floor(sub_rn(xs, (T)0.5));
+        fr[e] = xs - (T)b[e];
+    }
+    const T kf = -dt * V0 * inv_dx;
+#pragma unroll
+    for (int e = 0; e < 3; e++) y[(Y_F + e) * S] = fr[e];
+    y[Y_M * S] = mass;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const T m0 = mass * Cm[3 * r], m1 = mass * Cm[3 * r + 1], m2 = mass * Cm[3 * r + 2];
+        y[(Y_A + r) * S] = mass * v[r] - dx * (m0 * fr[0] + m1 * fr[1] + m2 * fr[2]);
+        y[(Y_B + 3 * r) * S] = dx * m0;
+        y[(Y_B + 3 * r + 1) * S] = dx * m1;
+        y[(Y_B + 3 * r + 2) * S] = dx * m2;
+        y[(Y_K + 3 * r) * S] = kf * tau[3 * r];
+        y[(Y_K + 3 * r + 1) * S] = kf * tau[3 * r + 1];
+        y[(Y_K + 3 * r + 2) * S] = kf * tau[3 * r + 2];
+    }
+    y[Y_D * S] = dd;
+}
+
+template <class T, int MODELS>
+__global__ void __launch_bounds__(256) k_stress(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const KeyLayout kl = a.kl;
+    const uint64_t cmask = (1ULL << kl.cp) - 1;
+    const int64_t S = a.pstride;
+    uint32_t flags = 0, fallbacks = 0;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
+        const uint64_t key = a.keys_sorted[q];
+        T* y = a.pay + pay_pos(q);
+        int b[3];
+        particle_payload<T, MODELS>(a.pin, a.vals_sorted[q], a.scenes[kl.scene(key)], y, S, b, fallbacks);
+        // the key was computed from this position by the previous G2P (or k_keys): they must agree
+        const uint64_t want = (key >> kl.ib) & cmask;
+        const bool ok = b[0] >= 0 && b[1] >= 0 && b[2] >= 0 && (L::offset(b[0], b[1], b[2]) >> L::data_bits) == want;
+        if (!ok) flags |= FLAG_CAPACITY;
+        y[Y_CELL * S] = ok ? (T)(int)(want & (L::nodes - 1)) : (T)255;
+        if ((q & 7) == 7) { // the gap slot after every 8th particle: writing it keeps every 32-byte sector whole
+#pragma unroll
+            for (int f = 0; f < NPAY; f++) y[f * S + 1] = (T)0;
+        }
+    }
+    if (flags) raise_flag(a.st, flags);
+    if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
+}
+
 template <class T>
 __device__ inline void flush_column(T* dst, const T* src, int n)
 {
@@ -260,249 +403,427 @@ __device__ inline void flush_column(T* dst, const T* src, int n)
     }
 }
 
-// P2G with no atomics in the hot loop. For every group (one occupied SPGrid block):
-//   phase 1 (thread per particle): stress and a 26-value payload per particle, staged in shared memory
-//   phase 2 (thread per cell and x-offset of the stencil): the particles of one cell all share the same
-//           27 nodes, so each thread accumulates its 9 nodes x 6 fields in registers over the cell's
-//           particles (deterministic order, no conflicts)
-//   phase 3: one shared add per node and field (distinct nodes within a warp), then vector atomics of
-//           the 6x6x6 node tile into the 8 neighbouring grid blocks
-// Payload: fractional index-space position f = x/dx - base, m, A = m v - dx (m C) f,
-// Bc = dx m C, K = -dt V0 tau / dx, d. With xm = (delta - f) dx for stencil offset delta:
-//   m v + m C xm = A + Bc delta  and  dt f_i = K . (dw_i w_j w_k, w_i dw_j w_k, w_i w_j dw_k),
-// so the node receives m w, w (A + Bc delta) + K grad-hat w, d w and w. The force enters the
-// momentum directly (m v + dt f), which the grid update turns into v + f dt/m + g dt as the reference's
-// gridVelocityExplicitUpdate does (MpmSimulationBase.cpp:1197-1226).
-constexpr int NPAY = 26;
-enum { Y_F = 0, Y_M = 3, Y_A = 4, Y_B = 7, Y_K = 16, Y_D = 25 };
-
 template <class T>
-struct P2GShape {
+__device__ __forceinline__ void zero_acc(T (&acc)[9][NACC])
+{
+#pragma unroll
+    for (int n = 0; n < 9; n++)
+#pragma unroll
+        for (int f = 0; f < NACC; f++) acc[n][f] = (T)0;
+}
+
+// One particle's contribution to the 9 nodes (ii, jj, kk) of a (cell, stencil x-offset ii) thread; y points
+// at the particle's payload, fields STRIDE apart. Weights from the fractional position (BSplines.h:73-100).
+// Node (ii, jj, kk) receives, per momentum component r,
+//   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
+//   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
+template <class T, int STRIDE>
+__device__ __forceinline__ void accumulate_particle(T (&acc)[9][NACC], const T* y, int ii, bool damage)
+{
+    T w[3][3], dw[3][3];
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        const T d0 = y[(Y_F + e) * STRIDE];
+        const T z = (T)1.5 - d0, d1 = d0 - (T)1, zz = d0 - (T)0.5;
+        w[e][0] = (T)0.5 * z * z;
+        w[e][1] = (T)0.75 - d1 * d1;
+        w[e][2] = (T)0.5 * zz * zz;
+        dw[e][0] = -z;
+        dw[e][1] = (T)-2 * d1;
+        dw[e][2] = zz;
+    }
+    const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
+    const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
+    const T mass = y[Y_M * STRIDE];
+    const T dd = y[Y_D * STRIDE];
+    T Ai[3], B1[3], B2[3], K0[3], K1[3], K2[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        Ai[r] = y[(Y_A + r) * STRIDE] + (T)ii * y[(Y_B + 3 * r) * STRIDE];
+        B1[r] = y[(Y_B + 3 * r + 1) * STRIDE];
+        B2[r] = y[(Y_B + 3 * r + 2) * STRIDE];
+        K0[r] = y[(Y_K + 3 * r) * STRIDE];
+        K1[r] = y[(Y_K + 3 * r + 1) * STRIDE];
+        K2[r] = y[(Y_K + 3 * r + 2) * STRIDE];
+    }
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++) {
+        const T c0 = wx * w[1][jj], gx = dwx * w[1][jj], gy = wx * dw[1][jj];
+        T al[3], be[3], ga[3];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            al[r] = c0 * (jj ? Ai[r] + (T)jj * B1[r] : Ai[r]) + (K0[r] * gx + K1[r] * gy);
+            be[r] = c0 * B2[r];
+            ga[r] = c0 * K2[r];
+        }
+        const T mc = mass * c0, dc = dd * c0;
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            const T wk = w[2][kk], dwk = dw[2][kk];
+            T* ac = acc[jj * 3 + kk];
+            ac[0] += mc * wk;
+#pragma unroll
+            for (int r = 0; r < 3; r++) ac[1 + r] += wk * al[r] + (kk ? ((T)kk * wk) * be[r] : (T)0) + dwk * ga[r];
+            if (damage) {
+                ac[4] += dc * wk;
+                ac[5] += c0 * wk;
+            }
+        }
+    }
+}
+
+// registers -> shared node tile of the block plus its +2 halo (distinct nodes within a warp: no contention)
+template <class T, class L>
+__device__ __forceinline__ void add_to_tile(const T (&acc)[9][NACC], T* tile, int cx, int cy, int cz, int ii, int nf)
+{
+    constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            T* t = tile + ((cx + ii) * TY + (cy + jj)) * TZ + (cz + kk);
+            const T* ac = acc[jj * 3 + kk];
+#pragma unroll
+            for (int f = 0; f < NACC; f++)
+                if (f < nf) atomicAdd(t + f * TN, ac[f]);
+        }
+}
+
+// tile -> the 8 neighbouring grid blocks: z columns split at the block boundary (4 + 2 nodes), vector atomics;
+// the tile is cleared behind the flush. nbr: grid slots of the block and its +1 neighbours (x*4 + y*2 + z).
+template <class T, class L>
+__device__ __forceinline__ void flush_tile(const StepArgs<T>& a, T* tile, const int32_t* nbr, int nf, int tid, int nthreads)
+{
+    constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
+    for (int q = tid; q < nf * TX * TY * 2; q += nthreads) {
+        const int half = q & 1, col = q >> 1;
+        const int f = col / (TX * TY), ab = col % (TX * TY), ta = ab / TY, tb = ab % TY;
+        const int ax = ta >= L::sx, ay = tb >= L::sy;
+        const int slot = nbr[ax * 4 + ay * 2 + half];
+        if ((uint32_t)slot >= a.b_cap) {
+            check_failed(a.st, 5);
+            continue;
+        }
+        T* dst = a.acc + ((size_t)slot * NACC + f) * L::nodes + L::element(ta - ax * L::sx, tb - ay * L::sy, 0);
+        T* src = tile + f * TN + (ta * TY + tb) * TZ + half * L::sz;
+        const int n = half ? TZ - L::sz : L::sz;
+        flush_column(dst, src, n);
+        for (int z = 0; z < n; z++) src[z] = (T)0;
+    }
+}
+
+// CHUNK: particles staged per copy (the tile of particles); the scatter CTA is the consumer threads
+// (cell x stencil x-offset) plus one producer warp
+// NBUF: staging buffers (1: the next chunk's copy overlaps the tile accumulation and flush of the current
+// one; 2: it overlaps the whole chunk)
+template <class T, int CHUNK, int NBUF>
+struct ScatterShape {
     using L = typename LayoutOf<T>::type;
-    static constexpr int NT = 3 * L::nodes; // cells x stencil x-offsets
-    static constexpr int CHUNK = std::is_same<T, float>::value ? 512 : 256;
-    static constexpr int CPAD = CHUNK + CHUNK / 8;
-    static constexpr size_t dyn_bytes = sizeof(T) * NPAY * CPAD;
+    static constexpr int NCONS = 3 * L::nodes;
+    static constexpr int NT = NCONS + 32;
+    static constexpr int VEC = 16 / (int)sizeof(T); // elements per 16 bytes: copy granularity
+    static constexpr int WIN = CHUNK + CHUNK / 8 + 8; // payload window per field, >= the span of CHUNK particles
+    static constexpr size_t buf_bytes = sizeof(T) * NPAY * WIN;
+    static constexpr size_t dyn_bytes = NBUF * buf_bytes;
+    static constexpr int MIN_CTAS = sizeof(T) == 4 ? 2 : 1;
+    static_assert(CHUNK % 32 == 0 && (WIN * sizeof(T)) % 16 == 0 && (NBUF == 1 || NBUF == 2), "copy alignment, buffers");
 };
 
-__device__ __forceinline__ int pay_slot(int q) { return q + (q >> 3); } // bank swizzle: cells hold ~8 particles
+enum : uint32_t { ITEM_LAST = 1, ITEM_DONE = 2, ITEM_BAD = 4 };
 
-// MODELS: bit 0 = fixed corotated present in the batch, bit 1 = Neo-Hookean (Borden) present; a batch
-// with one model kind runs a kernel without the other model's code (fewer registers).
-template <class T, int MODELS>
-__global__ void __launch_bounds__(P2GShape<T>::NT, 2) k_p2g(StepArgs<T> a)
+struct ScatterItem {
+    uint32_t q0, q1; // sorted particle range of the chunk
+    uint32_t base; // payload position of element 0 of the staged window
+    uint32_t flags;
+    int32_t nf; // accumulator fields in use (4 without damage)
+    int32_t nbr[8]; // grid slots of the group's block and its +1 neighbours
+};
+
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull; // 2 s: far beyond any copy; only a broken pipeline waits this long
+
+// the producer: claims groups, cuts them into chunks and issues one bulk copy per payload field and chunk
+template <class T, int CHUNK, int NBUF>
+__device__ void scatter_producer(const StepArgs<T>& a, unsigned char* dyn, uint64_t* full, uint64_t* empty, ScatterItem* item)
+{
+    using S = ScatterShape<T, CHUNK, NBUF>;
+    constexpr int WIN = S::WIN, VEC = S::VEC;
+    const uint32_t G = a.st->n_groups;
+    uint32_t ph_empty = 3u; // parity bit per buffer; a fresh barrier counts as released
+    uint32_t issues0 = 0, issues1 = 0;
+    int b = 0;
+    bool stop = false;
+    while (!stop) {
+        const uint32_t g = atomicAdd(&a.st->work_p2g, 1u);
+        uint32_t qs = 0, qe = 0, flags = 0;
+        int nf = 4;
+        int32_t nbr[8];
+        if (g < G) {
+            qs = a.g_start[g];
+            qe = (g + 1 < G) ? a.g_start[g + 1] : a.n_total;
+            nf = a.scenes[a.kl.scene(a.keys_sorted[qs])].damage ? NACC : 4;
+#pragma unroll
+            for (int d = 0; d < 8; d++) {
+                nbr[d] = a.g_nbr[g * 8 + d];
+                if (nbr[d] < 0) flags |= ITEM_BAD; // the lookup failed and raised FLAG_CAPACITY
+                else if ((uint32_t)nbr[d] >= a.b_cap) {
+                    check_failed(a.st, 4);
+                    flags |= ITEM_BAD;
+                }
+            }
+            if (qe <= qs || qe > a.n_total) {
+                check_failed(a.st, 1);
+                flags |= ITEM_BAD;
+                qe = qs + 1 <= a.n_total ? qs + 1 : qs; // keep the pipeline moving with an in-bounds chunk
+            }
+        }
+        else
+            flags = ITEM_DONE;
+        uint32_t q0 = qs;
+        do {
+            if (!mbar_wait(&empty[b], (ph_empty >> b) & 1u, WAIT_LIMIT_NS)) {
+                raise_flag(a.st, FLAG_TIMEOUT);
+                stop = true;
+                break;
+            }
+            ph_empty ^= 1u << b;
+            ScatterItem& it = item[b];
+            if (b) issues1++;
+            else issues0++;
+            if (flags & ITEM_DONE) {
+                it.flags = ITEM_DONE;
+                mbar_arrive(&full[b]);
+                stop = true;
+                break;
+            }
+            const uint32_t q1 = min(q0 + (uint32_t)CHUNK, qe);
+            const uint64_t p0 = pay_pos(q0) & ~(uint64_t)(VEC - 1);
+            const uint64_t p1 = (pay_pos(q1 - 1) + VEC) & ~(uint64_t)(VEC - 1);
+            uint32_t bytes = (uint32_t)(p1 - p0) * (uint32_t)sizeof(T);
+            uint64_t src0 = p0;
+            if (p1 > (uint64_t)a.pstride || bytes > (uint32_t)(WIN * sizeof(T))) { // never expected: record it, copy 16 in-bounds bytes
+                check_failed(a.st, 2);
+                flags |= ITEM_BAD;
+                bytes = 16;
+                src0 = 0;
+            }
+            it.q0 = q0;
+            it.q1 = q1;
+            it.base = (uint32_t)p0;
+            it.flags = flags | (q1 == qe ? ITEM_LAST : 0u);
+            it.nf = nf;
+#pragma unroll
+            for (int d = 0; d < 8; d++) it.nbr[d] = nbr[d];
+            T* dst = reinterpret_cast<T*>(dyn + b * S::buf_bytes);
+            fence_async_smem();
+            mbar_arrive_expect_tx(&full[b], bytes * NPAY);
+            for (int f = 0; f < NPAY; f++) bulk_load(dst + f * WIN, a.pay + f * a.pstride + src0, bytes, &full[b]);
+            b = NBUF == 2 ? b ^ 1 : 0;
+            q0 = q1;
+        } while (q0 < qe);
+    }
+    // leave no copy in flight behind: wait (bounded) for the last phase issued on each buffer
+    if (issues0) mbar_wait(&full[0], (issues0 - 1) & 1u, WAIT_LIMIT_NS);
+    if (issues1) mbar_wait(&full[1], (issues1 - 1) & 1u, WAIT_LIMIT_NS);
+}
+
+template <class T, int CHUNK, int NBUF, int MIN_CTAS = ScatterShape<T, CHUNK, NBUF>::MIN_CTAS>
+__global__ void __launch_bounds__(ScatterShape<T, CHUNK, NBUF>::NT, MIN_CTAS) k_scatter(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    using S = P2GShape<T>;
-    constexpr int NT = S::NT, CHUNK = S::CHUNK, CPAD = S::CPAD, NC = L::nodes;
+    using S = ScatterShape<T, CHUNK, NBUF>;
+    constexpr int NCONS = S::NCONS, WIN = S::WIN, NC = L::nodes;
     constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
-    extern __shared__ __align__(16) unsigned char p2g_dyn[];
-    T* pay = reinterpret_cast<T*>(p2g_dyn);
+    extern __shared__ __align__(128) unsigned char scat_dyn[];
+    __shared__ T tile[NACC * TN];
+    __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ ScatterItem item[2];
+    __shared__ int16_t cfirst[2][NC], clast[2][NC];
+    __shared__ uint32_t ctag[2][NC];
+    __shared__ int32_t s_nbr[8]; // the grid slots of the group being flushed (the item is released before the flush)
+    __shared__ int s_stop;
+    if (aborted_cta(a.st)) return;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], NCONS / 32); // one arrival per consumer warp
+        mbar_init(&empty[1], NCONS / 32);
+        mbar_init_fence();
+        s_stop = 0;
+    }
+    for (int q = tid; q < NACC * TN; q += S::NT) tile[q] = (T)0;
+    for (int q = tid; q < 2 * NC; q += S::NT) (&ctag[0][0])[q] = 0xffffffffu;
+    __syncthreads();
+    if (tid >= NCONS) { // the producer warp (one lane works); no CTA-wide barrier follows this point
+        if (tid == NCONS) scatter_producer<T, CHUNK, NBUF>(a, scat_dyn, full, empty, item);
+        return;
+    }
+    // consumer role: cell c, stencil x-offset ii
+    const int ii = tid / NC, c = tid % NC;
+    const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    uint32_t ph_full = 0; // parity bit per buffer
+    int b = 0;
+    for (uint32_t seq = 0;; seq++) {
+        const bool ready = mbar_wait(&full[b], (ph_full >> b) & 1u, WAIT_LIMIT_NS);
+        ph_full ^= 1u << b;
+        const T* buf = reinterpret_cast<const T*>(scat_dyn + b * S::buf_bytes);
+        const ScatterItem& it = item[b];
+        uint32_t fl = ITEM_DONE;
+        uint32_t q0 = 0, base = 0;
+        if (!ready) {
+            s_stop = 1;
+            raise_flag(a.st, FLAG_TIMEOUT);
+        }
+        else {
+            fl = it.flags;
+            q0 = it.q0;
+            base = it.base;
+            if (!(fl & (ITEM_DONE | ITEM_BAD)) && (it.q1 <= q0 || it.q1 - q0 > (uint32_t)CHUNK || pay_pos(it.q1 - 1) - base >= (uint64_t)WIN)) {
+                check_failed(a.st, 6); // an item that does not fit its window: skip it
+                fl |= ITEM_BAD;
+            }
+            if (!(fl & (ITEM_DONE | ITEM_BAD))) {
+                // runs of equal cells (particles are sorted by cell inside a block)
+                const uint32_t q1 = it.q1;
+                const T* cellv = buf + Y_CELL * WIN;
+                for (uint32_t q = q0 + tid; q < q1; q += NCONS) {
+                    const int e = (int)cellv[pay_pos(q) - base];
+                    if ((unsigned)e >= (unsigned)NC) continue; // 255 marks a particle whose key disagreed
+                    const int ep = q > q0 ? (int)cellv[pay_pos(q - 1) - base] : -1;
+                    if (ep > e) check_failed(a.st, 3); // cells must ascend inside a block: the staged data is not what was written
+                    if (q == q0 || ep != e) {
+                        cfirst[b][e] = (int16_t)(q - q0);
+                        ctag[b][e] = seq;
+                    }
+                    if (q + 1 == q1 || (int)cellv[pay_pos(q + 1) - base] != e) clast[b][e] = (int16_t)(q + 1 - q0);
+                }
+            }
+        }
+        bar_sync(1, NCONS);
+        if (s_stop || (fl & ITEM_DONE)) break;
+        const int nf = it.nf;
+        const bool damage = nf == NACC;
+        if ((fl & ITEM_LAST) && tid < 8) s_nbr[tid] = it.nbr[tid]; // read before this warp releases the item
+        // per (cell, stencil x-offset): register accumulators of the thread's 9 nodes
+        T acc[9][NACC];
+        zero_acc(acc);
+        // decided once: after the release below, faster warps may already mark the next chunk
+        const bool mine = !(fl & ITEM_BAD) && ctag[b][c] == seq;
+        if (mine) {
+            const uint32_t qa = q0 + cfirst[b][c], qb = q0 + clast[b][c];
+            for (uint32_t q = qa; q < qb; q++) accumulate_particle<T, WIN>(acc, buf + (pay_pos(q) - base), ii, damage);
+        }
+        // the chunk's payload is no longer needed: release the buffer (and the item) to the producer
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&empty[b]);
+        if (mine) add_to_tile<T, L>(acc, tile, cx, cy, cz, ii, nf);
+        if (fl & ITEM_LAST) {
+            bar_sync(1, NCONS); // every chunk of the group is in the tile
+            if (!(fl & ITEM_BAD)) flush_tile<T, L>(a, tile, s_nbr, nf, tid, NCONS);
+        }
+        b = NBUF == 2 ? b ^ 1 : 0;
+    }
+}
+
+// The fused P2G: one kernel per substep with the same arithmetic, the stress evaluated in the kernel. Per
+// group, phase 1 (thread per particle) loads the particle state through the sorted order and stages its
+// payload in shared memory (bank-staggered at q + q/8); phases 2 and 3 are those of k_scatter. No payload
+// round trip through HBM, at the price of the state loads' latency inside the kernel: the autotuner times
+// both forms on the workload.
+template <class T>
+struct FusedShape {
+    using L = typename LayoutOf<T>::type;
+    static constexpr int NT = 3 * L::nodes; // cells x stencil x-offsets
+    static constexpr int CHUNK = sizeof(T) == 4 ? 512 : 256;
+    static constexpr int CPAD = CHUNK + CHUNK / 8;
+    static constexpr size_t dyn_bytes = sizeof(T) * Y_CELL * CPAD; // fields Y_F..Y_D
+};
+
+template <class T, int MODELS>
+__global__ void __launch_bounds__(FusedShape<T>::NT, 2) k_p2g_fused(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    using S = FusedShape<T>;
+    constexpr int NT = S::NT, CHUNK = S::CHUNK, CPAD = S::CPAD, NC = L::nodes;
+    constexpr int TN = (L::sx + 2) * (L::sy + 2) * (L::sz + 2);
+    extern __shared__ __align__(16) unsigned char fused_dyn[];
+    T* pay = reinterpret_cast<T*>(fused_dyn);
     __shared__ T tile[NACC * TN];
     __shared__ uint8_t cellof[CHUNK];
     __shared__ int16_t cfirst[NC], clast[NC];
-    __shared__ int s_g, s_nbr[8], s_scene;
+    __shared__ int s_g, s_scene, s_bad;
+    __shared__ int32_t s_nbr[8];
     __shared__ int s_org[3];
     if (aborted_cta(a.st)) return;
     const uint32_t G = a.st->n_groups;
     const int tid = threadIdx.x;
-    // phase-2 role of this thread: cell c, stencil x-offset ii
     const int ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    for (int q = tid; q < NACC * TN; q += NT) tile[q] = (T)0;
+    uint32_t fallbacks = 0;
     for (;;) {
-        if (tid == 0) s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
+        if (tid == 0) {
+            s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
+            s_bad = 0;
+        }
         __syncthreads();
         const int g = s_g;
         if (g >= (int)G) break;
         const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
         if (tid < 8) {
-            uint64_t key0 = a.keys_sorted[start];
-            uint64_t scene = a.kl.scene(key0);
-            uint32_t bi, bj, bk;
-            L::block_of_page(a.kl.page(key0), bi, bj, bk);
-            int dl = tid;
-            uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
-            int slot = hash_find(a.h_keys, a.h_vals, a.h_mask, hk);
-            if (slot < 0) raise_flag(a.st, FLAG_CAPACITY);
-            s_nbr[dl] = slot;
-            a.g_nbr[g * 8 + dl] = slot;
-            if (dl == 0) {
-                s_scene = (int)scene;
+            const int slot = a.g_nbr[g * 8 + tid];
+            s_nbr[tid] = slot;
+            if (slot < 0 || (uint32_t)slot >= a.b_cap) s_bad = 1; // a failed lookup already raised FLAG_CAPACITY
+            if (tid == 0) {
+                const uint64_t key0 = a.keys_sorted[start];
+                uint32_t bi, bj, bk;
+                L::block_of_page(a.kl.page(key0), bi, bj, bk);
+                s_scene = (int)a.kl.scene(key0);
                 s_org[0] = (int)(bi * L::sx);
                 s_org[1] = (int)(bj * L::sy);
                 s_org[2] = (int)(bk * L::sz);
             }
         }
-        for (int q = tid; q < NACC * TN; q += NT) tile[q] = (T)0;
         __syncthreads();
-        bool bad_slot = false;
-        for (int d = 0; d < 8; d++) bad_slot |= s_nbr[d] < 0;
+        const bool bad = s_bad != 0;
         const SceneParams<T>& sp = a.scenes[s_scene];
-        const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt;
-        const bool damage = sp.damage != 0;
-        const int nf = damage ? NACC : 4;
-        for (uint32_t c0 = start; c0 < end && !bad_slot; c0 += CHUNK) {
+        const int nf = sp.damage ? NACC : 4;
+        for (uint32_t c0 = start; c0 < end && !bad; c0 += CHUNK) {
             const int cnt = (int)min((uint32_t)CHUNK, end - c0);
             // ---- phase 1: per particle
             if (tid < NC) {
                 cfirst[tid] = 0;
                 clast[tid] = 0;
             }
-            const Pool<T>& P = a.pin;
             for (int q = tid; q < cnt; q += NT) {
-                const uint32_t j = a.vals_sorted[c0 + q];
-                T x[3], v[3], Cm[9], F[9];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    x[e] = P.f[(P_X + e) * P.stride + j];
-                    v[e] = P.f[(P_V + e) * P.stride + j];
-                }
-#pragma unroll
-                for (int e = 0; e < 9; e++) {
-                    Cm[e] = P.f[(P_C + e) * P.stride + j];
-                    F[e] = P.f[(P_F + e) * P.stride + j];
-                }
-                const T mass = P.f[P_M * P.stride + j], V0 = P.f[P_V0 * P.stride + j];
-                const T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
-                const uint32_t mat = P.pid[j] >> L::index_bits;
-                const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
-                T tau[9];
-                if (MODELS == 1 || (MODELS == 3 && mt.model == MODEL_COROTATED)) {
-                    if (tau_corotated(mt, F, tau)) atomicAdd(&a.st->fallback, 1u);
-                }
-                else
-                    tau_nhb(mt, F, (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1, tau);
-                T fr[3];
-                int l[3];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    const T xs = mul_rn(x[e], inv_dx);
-                    const int b = int_floor(sub_rn(xs, (T)0.5));
-                    fr[e] = xs - (T)b;
-                    l[e] = b - s_org[e];
-                }
-                const bool inside = l[0] >= 0 && l[0] < L::sx && l[1] >= 0 && l[1] < L::sy && l[2] >= 0 && l[2] < L::sz;
+                int b[3];
+                particle_payload<T, MODELS>(a.pin, a.vals_sorted[c0 + q], sp, pay + (q + (q >> 3)), CPAD, b, fallbacks);
+                const int l0 = b[0] - s_org[0], l1 = b[1] - s_org[1], l2 = b[2] - s_org[2];
+                const bool inside = l0 >= 0 && l0 < L::sx && l1 >= 0 && l1 < L::sy && l2 >= 0 && l2 < L::sz;
                 if (!inside) raise_flag(a.st, FLAG_CAPACITY); // keys and positions disagree: abort the substep
-                cellof[q] = inside ? (uint8_t)L::element(l[0], l[1], l[2]) : (uint8_t)0xff;
-                T* y = pay + pay_slot(q);
-                const T kf = -dt * V0 * inv_dx;
-#pragma unroll
-                for (int e = 0; e < 3; e++) y[(Y_F + e) * CPAD] = fr[e];
-                y[Y_M * CPAD] = mass;
-#pragma unroll
-                for (int r = 0; r < 3; r++) {
-                    const T m0 = mass * Cm[3 * r], m1 = mass * Cm[3 * r + 1], m2 = mass * Cm[3 * r + 2];
-                    y[(Y_A + r) * CPAD] = mass * v[r] - dx * (m0 * fr[0] + m1 * fr[1] + m2 * fr[2]);
-                    y[(Y_B + 3 * r) * CPAD] = dx * m0;
-                    y[(Y_B + 3 * r + 1) * CPAD] = dx * m1;
-                    y[(Y_B + 3 * r + 2) * CPAD] = dx * m2;
-                    y[(Y_K + 3 * r) * CPAD] = kf * tau[3 * r];
-                    y[(Y_K + 3 * r + 1) * CPAD] = kf * tau[3 * r + 1];
-                    y[(Y_K + 3 * r + 2) * CPAD] = kf * tau[3 * r + 2];
-                }
-                y[Y_D * CPAD] = dd;
+                cellof[q] = inside ? (uint8_t)L::element(l0, l1, l2) : (uint8_t)0xff;
             }
             __syncthreads();
             // particles of one cell are contiguous (sorted by cell inside the block)
             for (int q = tid; q < cnt; q += NT) {
                 const int e = cellof[q];
-                if (e == 0xff) continue;
+                if (e >= NC) continue;
                 if (q == 0 || cellof[q - 1] != e) cfirst[e] = (int16_t)q;
                 if (q == cnt - 1 || cellof[q + 1] != e) clast[e] = (int16_t)(q + 1);
             }
             __syncthreads();
-            // ---- phase 2: per (cell, stencil x-offset), register accumulators of the thread's 9 nodes
-            if (ii < 3) {
-                T acc[9][NACC];
-#pragma unroll
-                for (int n = 0; n < 9; n++)
-#pragma unroll
-                    for (int f = 0; f < NACC; f++) acc[n][f] = (T)0;
-                const int q1 = clast[c];
-                for (int q = cfirst[c]; q < q1; q++) {
-                    const T* y = pay + pay_slot(q);
-                    T w[3][3], dw[3][3];
-#pragma unroll
-                    for (int e = 0; e < 3; e++) {
-                        const T d0 = y[(Y_F + e) * CPAD];
-                        const T z = (T)1.5 - d0, d1 = d0 - (T)1, zz = d0 - (T)0.5;
-                        w[e][0] = (T)0.5 * z * z;
-                        w[e][1] = (T)0.75 - d1 * d1;
-                        w[e][2] = (T)0.5 * zz * zz;
-                        dw[e][0] = -z;
-                        dw[e][1] = (T)-2 * d1;
-                        dw[e][2] = zz;
-                    }
-                    const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
-                    const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
-                    const T mass = y[Y_M * CPAD];
-                    const T dd = y[Y_D * CPAD];
-                    T Ai[3], B1[3], B2[3], K0[3], K1[3], K2[3];
-#pragma unroll
-                    for (int r = 0; r < 3; r++) {
-                        Ai[r] = y[(Y_A + r) * CPAD] + (T)ii * y[(Y_B + 3 * r) * CPAD];
-                        B1[r] = y[(Y_B + 3 * r + 1) * CPAD];
-                        B2[r] = y[(Y_B + 3 * r + 2) * CPAD];
-                        K0[r] = y[(Y_K + 3 * r) * CPAD];
-                        K1[r] = y[(Y_K + 3 * r + 1) * CPAD];
-                        K2[r] = y[(Y_K + 3 * r + 2) * CPAD];
-                    }
-                    // node (ii, jj, kk) receives, per momentum component r,
-                    //   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
-                    //   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
-#pragma unroll
-                    for (int jj = 0; jj < 3; jj++) {
-                        const T c0 = wx * w[1][jj], gx = dwx * w[1][jj], gy = wx * dw[1][jj];
-                        T al[3], be[3], ga[3];
-#pragma unroll
-                        for (int r = 0; r < 3; r++) {
-                            al[r] = c0 * (jj ? Ai[r] + (T)jj * B1[r] : Ai[r]) + (K0[r] * gx + K1[r] * gy);
-                            be[r] = c0 * B2[r];
-                            ga[r] = c0 * K2[r];
-                        }
-                        const T mc = mass * c0, dc = dd * c0;
-#pragma unroll
-                        for (int kk = 0; kk < 3; kk++) {
-                            const T wk = w[2][kk], dwk = dw[2][kk];
-                            T* ac = acc[jj * 3 + kk];
-                            ac[0] += mc * wk;
-#pragma unroll
-                            for (int r = 0; r < 3; r++) ac[1 + r] += wk * al[r] + (kk ? ((T)kk * wk) * be[r] : (T)0) + dwk * ga[r];
-                            if (damage) {
-                                ac[4] += dc * wk;
-                                ac[5] += c0 * wk;
-                            }
-                        }
-                    }
-                }
-                // ---- phase 3: registers -> shared tile (distinct nodes within a warp, so no contention)
-                if (q1 > cfirst[c]) {
-#pragma unroll
-                    for (int jj = 0; jj < 3; jj++)
-#pragma unroll
-                        for (int kk = 0; kk < 3; kk++) {
-                            T* t = tile + ((cx + ii) * TY + (cy + jj)) * TZ + (cz + kk);
-                            const T* ac = acc[jj * 3 + kk];
-                            for (int f = 0; f < nf; f++) atomicAdd(t + f * TN, ac[f]);
-                        }
-                }
-            }
+            // ---- phases 2 and 3
+            T acc[9][NACC];
+            zero_acc(acc);
+            const int qa = cfirst[c], qb = clast[c];
+            for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD>(acc, pay + (q + (q >> 3)), ii, nf == NACC);
+            if (qb > qa) add_to_tile<T, L>(acc, tile, cx, cy, cz, ii, nf);
             __syncthreads();
         }
-        if (!bad_slot) {
-            // tile -> global: z columns split at the block boundary (4 + 2 nodes)
-            for (int q = tid; q < nf * TX * TY * 2; q += NT) {
-                const int half = q & 1, col = q >> 1;
-                const int f = col / (TX * TY), ab = col % (TX * TY), ta = ab / TY, tb = ab % TY;
-                const int ax = ta >= L::sx, ay = tb >= L::sy;
-                const int slot = s_nbr[ax * 4 + ay * 2 + half];
-                T* dst = a.acc + ((size_t)slot * NACC + f) * L::nodes + L::element(ta - ax * L::sx, tb - ay * L::sy, 0);
-                const T* src = tile + f * TN + (ta * TY + tb) * TZ + half * L::sz;
-                flush_column(dst, src, half ? TZ - L::sz : L::sz);
-            }
-        }
+        if (!bad) flush_tile<T, L>(a, tile, s_nbr, nf, tid, NT);
         __syncthreads();
     }
+    if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -566,7 +887,7 @@ __global__ void k_grid(StepArgs<T> a)
 // G2P
 // ---------------------------------------------------------------------------------------------------
 template <class T, int NT>
-__global__ void __launch_bounds__(NT, 4) k_g2p(StepArgs<T> a)
+__global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 512 : 256) / NT) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
     __shared__ __align__(16) T sv[8 * NVEL * L::nodes];
@@ -600,7 +921,8 @@ __global__ void __launch_bounds__(NT, 4) k_g2p(StepArgs<T> a)
             for (int q = threadIdx.x; q < 8 * V4; q += NT) {
                 const int d = q / V4, r = q % V4;
                 const int slot = s_nbr[d];
-                dst[q] = slot >= 0 ? reinterpret_cast<const uint4*>(a.vel + (size_t)slot * NVEL * L::nodes)[r] : make_uint4(0, 0, 0, 0);
+                dst[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? reinterpret_cast<const uint4*>(a.vel + (size_t)slot * NVEL * L::nodes)[r]
+                                                                  : make_uint4(0, 0, 0, 0);
             }
         }
         __syncthreads();
