@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
     ap.add_argument("--schedule", default="auto",
-                    help="auto (the autotuner), or fused:CTAS:G2P or split:CHUNK:BUFFERS:CTAS:G2P (a fixed launch schedule)")
+                    help="auto (the autotuner), or fused:CTAS:G2P, fused2:CTAS:G2P or split:CHUNK:BUFFERS:CTAS:G2P (a fixed launch schedule)")
     return ap.parse_args()
 
 
@@ -259,8 +259,8 @@ def apply_schedule(obj, spec):
     if spec == "auto":
         return
     f = spec.split(":")
-    if f[0] == "fused":
-        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused=True)
+    if f[0] in ("fused", "fused2"):
+        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused=1 if f[0] == "fused" else 2)
     else:
         obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]))
 

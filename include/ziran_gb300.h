@@ -137,7 +137,8 @@ int zr_scene_get_timing(zr_scene* s, double out5[5], int64_t* steps);
  * mode 0 = a fixed default schedule, 1 = autotuned: measured with trial substeps on the scene's own state
  * when it first steps (the trials are rolled back) and cached per workload class in the process,
  * 2 = autotuned, re-measured per batch. Schedules differ only in the order of floating-point sums.
- * get: out6 = fused, chunk, buffers, CTAs per SM, G2P threads, 1 if measured. set: in5 = fused (1 or 0),
+ * get: out6 = fused, chunk, buffers, CTAs per SM, G2P threads, 1 if measured. set: in5 = fused (0 split,
+ * 1 fused, 2 fused with registers cut for one more CTA per SM),
  * (chunk, buffers) one of (512, 1), (512, 2), (256, 2) in FP32 or (256, 1), (256, 2), (128, 2) in FP64
  * (ignored when fused), CTAs per SM, G2P threads (64, 128 or 256); an explicit schedule disables the
  * autotuner for the scene. */

@@ -21,7 +21,7 @@ def test_every_schedule_matches_the_oracle(prec):
     r = o.state()
     big = 512 if prec == zr.F32 else 256
     # split form: (particles per staged chunk, staging buffers); fused form: one kernel, chunk = a block
-    variants = ((False, big, 1), (False, big, 2), (False, big // 2, 2), (True, big, 0))
+    variants = ((0, big, 1), (0, big, 2), (0, big // 2, 2), (1, big, 0), (2, big, 0))
     xtol = 1e-12 if prec == zr.F64 else 2e-6
     for (fused, chunk, nbuf), ctas, nt in itertools.product(variants, (1, 2), (64, 128, 256)):
         s = scenes.gpu_scene(d, prec)

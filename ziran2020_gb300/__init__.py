@@ -322,7 +322,8 @@ class Scene:
         self._check(self.L.zr_scene_set_autotune(self.h, int(mode)))
 
     def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=False):
-        """chunk/buffers select the split P2G form's staging; fused=True selects the one-kernel P2G."""
+        """chunk/buffers select the split P2G form's staging; fused=1 selects the one-kernel P2G, fused=2 the
+        same with registers cut for one more CTA per SM."""
         arr = (C.c_int32 * 5)(int(fused), chunk, buffers, p2g_ctas_per_sm, g2p_threads)
         self._check(self.L.zr_scene_set_schedule(self.h, arr))
 
@@ -426,7 +427,7 @@ class Batch:
 def _schedule(fn, h):
     out = (C.c_int32 * 6)()
     rc = fn(h, out)
-    return rc, {"fused": bool(out[0]), "chunk": out[1], "buffers": out[2], "p2g_ctas_per_sm": out[3], "g2p_threads": out[4], "tuned": bool(out[5])}
+    return rc, {"fused": out[0], "chunk": out[1], "buffers": out[2], "p2g_ctas_per_sm": out[3], "g2p_threads": out[4], "tuned": bool(out[5])}
 
 
 

@@ -41,6 +41,8 @@ class Engine final : public EngineBase {
     static constexpr int VAR_CHUNK[3] = { CH_BIG, CH_BIG, CH_BIG / 2 };
     static constexpr int VAR_NBUF[3] = { 1, 2, 2 };
     static constexpr int G2P_NT[3] = { 64, 128, 256 };
+    // fused P2G register budgets: cut for 2 or 3 CTAs per SM (FP32), 1 or 2 (FP64)
+    static constexpr int FUSED_MINB[2] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2 };
 
 public:
     Engine() { init_device(); }
@@ -496,9 +498,9 @@ public:
     Schedule schedule() const override { return sched_; }
     int set_schedule(const Schedule& sc) override
     {
-        if ((!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0 || sc.scatter_ctas_per_sm < 1
-            || sc.scatter_ctas_per_sm > 8)
-            return arg("schedule: unknown (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
+        if (sc.fused < 0 || sc.fused > 2 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
+            || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8)
+            return arg("schedule: unknown P2G form, (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
         sched_ = sc;
         if (sc.fused) {
             sched_.chunk = FusedShape<T>::CHUNK;
@@ -537,7 +539,8 @@ private:
     DevStatus* hst_ = nullptr;
     void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
-    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[3] = { 1, 1, 1 }, occ_fused_[3] = { 1, 1, 1 };
+    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[3] = { 1, 1, 1 };
+    int occ_fused_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } }; // [register budget variant][model set]
     int models_ = 3; // bit 0: a corotated material is present, bit 1: a Neo-Hookean (Borden) material
     bool any_damage_ = false;
     T* pay_ = nullptr;
@@ -676,9 +679,12 @@ private:
         scatter_setup<0>();
         scatter_setup<1>();
         scatter_setup<2>();
-        fused_setup<1>(0);
-        fused_setup<2>(1);
-        fused_setup<3>(2);
+        fused_setup<1, FUSED_MINB[0]>(0, 0);
+        fused_setup<2, FUSED_MINB[0]>(0, 1);
+        fused_setup<3, FUSED_MINB[0]>(0, 2);
+        fused_setup<1, FUSED_MINB[1]>(1, 0);
+        fused_setup<2, FUSED_MINB[1]>(1, 1);
+        fused_setup<3, FUSED_MINB[1]>(1, 2);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[0], k_stress<T, 1>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 3>, 256, 0);
@@ -823,13 +829,12 @@ private:
         k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
         if (sched_.fused) {
-            const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[models_slot()]);
-            if (models_ == 1)
-                k_p2g_fused<T, 1><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
-            else if (models_ == 2)
-                k_p2g_fused<T, 2><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            const int fv = sched_.fused == 2 ? 1 : 0;
+            const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[fv][models_slot()]);
+            if (fv == 0)
+                launch_fused<FUSED_MINB[0]>(a, fctas);
             else
-                k_p2g_fused<T, 3><<<fctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+                launch_fused<FUSED_MINB[1]>(a, fctas);
         }
         else {
             if (models_ == 1)
@@ -966,13 +971,24 @@ private:
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_scatter_[V], k, S::NT, S::dyn_bytes);
     }
-    template <int M>
-    void fused_setup(int slot)
+    template <int M, int MINB>
+    void fused_setup(int var, int slot)
     {
-        cudaFuncSetAttribute(k_p2g_fused<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedShape<T>::dyn_bytes);
-        cudaFuncSetAttribute(k_p2g_fused<T, M>, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[slot], k_p2g_fused<T, M>, FusedShape<T>::NT, FusedShape<T>::dyn_bytes);
-        occ_fused_[slot] = std::max(1, occ_fused_[slot]);
+        auto k = k_p2g_fused<T, M, MINB>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[var][slot], k, FusedShape<T>::NT, FusedShape<T>::dyn_bytes);
+        occ_fused_[var][slot] = std::max(1, occ_fused_[var][slot]);
+    }
+    template <int MINB>
+    void launch_fused(const StepArgs<T>& a, int ctas)
+    {
+        if (models_ == 1)
+            k_p2g_fused<T, 1, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+        else if (models_ == 2)
+            k_p2g_fused<T, 2, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+        else
+            k_p2g_fused<T, 3, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
     }
     int models_slot() const { return models_ == 1 ? 0 : (models_ == 2 ? 1 : 2); }
     template <int V>
@@ -1069,8 +1085,10 @@ private:
         for (int vi = 0; vi < 3; vi++)
             for (int c = occ_scatter_[vi]; c >= std::max(1, occ_scatter_[vi] - 1); c--)
                 p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 1 });
-        const int of = occ_fused_[models_slot()];
-        for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 1 });
+        for (int fv = 0; fv < 2; fv++) {
+            const int of = occ_fused_[fv][models_slot()];
+            for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1 + fv, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 1 });
+        }
         constexpr int REPS = 2; // the first run of a candidate warms caches and instruction memory
         Schedule best = p2g_c[0];
         float best_p2g = 1e30f, best_g2p = 1e30f;

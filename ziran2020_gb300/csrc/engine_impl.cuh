@@ -739,8 +739,9 @@ struct FusedShape {
     static constexpr size_t dyn_bytes = sizeof(T) * Y_CELL * CPAD; // fields Y_F..Y_D
 };
 
-template <class T, int MODELS>
-__global__ void __launch_bounds__(FusedShape<T>::NT, 2) k_p2g_fused(StepArgs<T> a)
+// MINB: CTAs per SM the register budget is cut for (more CTAs hide more load latency; fewer registers may spill)
+template <class T, int MODELS, int MINB>
+__global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
     using S = FusedShape<T>;
