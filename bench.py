@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
     ap.add_argument("--schedule", default="auto",
-                    help="auto (the autotuner), or fused:CTAS:G2P, fused2:CTAS:G2P or split:CHUNK:BUFFERS:CTAS:G2P (a fixed launch schedule)")
+                    help="auto (the autotuner), or fused:CTAS:G2P[:TIGHT], fused2:CTAS:G2P[:TIGHT] or split:CHUNK:BUFFERS:CTAS:G2P[:TIGHT] "
+                         "(a fixed launch schedule)")
     return ap.parse_args()
 
 
@@ -260,9 +261,9 @@ def apply_schedule(obj, spec):
         return
     f = spec.split(":")
     if f[0] in ("fused", "fused2"):
-        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused=1 if f[0] == "fused" else 2)
+        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused=1 if f[0] == "fused" else 2, g2p_tight=int(f[3]) if len(f) > 3 else 0)
     else:
-        obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]))
+        obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]), g2p_tight=int(f[5]) if len(f) > 5 else 0)
 
 
 def _config(args):

@@ -137,14 +137,14 @@ int zr_scene_get_timing(zr_scene* s, double out5[5], int64_t* steps);
  * mode 0 = a fixed default schedule, 1 = autotuned: measured with trial substeps on the scene's own state
  * when it first steps (the trials are rolled back) and cached per workload class in the process,
  * 2 = autotuned, re-measured per batch. Schedules differ only in the order of floating-point sums.
- * get: out6 = fused, chunk, buffers, CTAs per SM, G2P threads, 1 if measured. set: in5 = fused (0 split,
- * 1 fused, 2 fused with registers cut for one more CTA per SM),
+ * get: out7 = fused, chunk, buffers, CTAs per SM, G2P threads, G2P register cut, 1 if measured.
+ * set: in6 = fused (0 split, 1 fused, 2 fused with registers cut for one more CTA per SM),
  * (chunk, buffers) one of (512, 1), (512, 2), (256, 2) in FP32 or (256, 1), (256, 2), (128, 2) in FP64
- * (ignored when fused), CTAs per SM, G2P threads (64, 128 or 256); an explicit schedule disables the
- * autotuner for the scene. */
+ * (ignored when fused), CTAs per SM, G2P threads (64, 128 or 256), G2P register cut (0 or 1: more
+ * resident threads per SM); an explicit schedule disables the autotuner for the scene. */
 int zr_scene_set_autotune(zr_scene* s, int mode);
-int zr_scene_set_schedule(zr_scene* s, const int32_t in5[5]);
-int zr_scene_get_schedule(zr_scene* s, int32_t out6[6]);
+int zr_scene_set_schedule(zr_scene* s, const int32_t in6[6]);
+int zr_scene_get_schedule(zr_scene* s, int32_t out7[7]);
 /* kernels launched per substep (CUDA-graph node count) and device bytes held by the scene. */
 int zr_scene_stats(zr_scene* s, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
 
@@ -203,7 +203,7 @@ int zr_batch_reductions(zr_batch* b, int slot, double out[7]);
 int64_t zr_batch_count(zr_batch* b, int slot);
 int zr_batch_set_timing(zr_batch* b, int on);
 int zr_batch_set_autotune(zr_batch* b, int mode);
-int zr_batch_get_schedule(zr_batch* b, int32_t out6[6]);
+int zr_batch_get_schedule(zr_batch* b, int32_t out7[7]);
 int zr_batch_get_timing(zr_batch* b, double out5[5], int64_t* steps);
 int zr_batch_stats(zr_batch* b, int64_t* launches_per_step, int64_t* device_bytes, int64_t* fallbacks);
 const char* zr_batch_last_error(zr_batch* b);

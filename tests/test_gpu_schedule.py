@@ -23,9 +23,9 @@ def test_every_schedule_matches_the_oracle(prec):
     # split form: (particles per staged chunk, staging buffers); fused form: one kernel, chunk = a block
     variants = ((0, big, 1), (0, big, 2), (0, big // 2, 2), (1, big, 0), (2, big, 0))
     xtol = 1e-12 if prec == zr.F64 else 2e-6
-    for (fused, chunk, nbuf), ctas, nt in itertools.product(variants, (1, 2), (64, 128, 256)):
+    for (fused, chunk, nbuf), ctas, (nt, tight) in itertools.product(variants, (1, 2), ((64, 0), (128, 0), (256, 0), (64, 1), (128, 1))):
         s = scenes.gpu_scene(d, prec)
-        s.set_schedule(chunk, nbuf, ctas, nt, fused=fused)
+        s.set_schedule(chunk, nbuf, ctas, nt, fused=fused, g2p_tight=tight)
         s.step(12)
         sc = s.schedule()
         assert (sc["fused"], sc["chunk"], sc["buffers"], sc["g2p_threads"], sc["tuned"]) == (fused, chunk, nbuf, nt, False)

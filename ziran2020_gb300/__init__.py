@@ -321,10 +321,10 @@ class Scene:
         """0 fixed default schedule, 1 autotuned and cached per workload class, 2 re-measured per batch."""
         self._check(self.L.zr_scene_set_autotune(self.h, int(mode)))
 
-    def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=False):
+    def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=0, g2p_tight=0):
         """chunk/buffers select the split P2G form's staging; fused=1 selects the one-kernel P2G, fused=2 the
-        same with registers cut for one more CTA per SM."""
-        arr = (C.c_int32 * 5)(int(fused), chunk, buffers, p2g_ctas_per_sm, g2p_threads)
+        same with registers cut for one more CTA per SM; g2p_tight=1 cuts G2P registers likewise."""
+        arr = (C.c_int32 * 6)(int(fused), chunk, buffers, p2g_ctas_per_sm, g2p_threads, int(g2p_tight))
         self._check(self.L.zr_scene_set_schedule(self.h, arr))
 
     def schedule(self):
@@ -425,9 +425,10 @@ class Batch:
 
 
 def _schedule(fn, h):
-    out = (C.c_int32 * 6)()
+    out = (C.c_int32 * 7)()
     rc = fn(h, out)
-    return rc, {"fused": out[0], "chunk": out[1], "buffers": out[2], "p2g_ctas_per_sm": out[3], "g2p_threads": out[4], "tuned": bool(out[5])}
+    return rc, {"fused": out[0], "chunk": out[1], "buffers": out[2], "p2g_ctas_per_sm": out[3], "g2p_threads": out[4], "g2p_tight": out[5],
+                "tuned": bool(out[6])}
 
 
 

@@ -532,15 +532,16 @@ int zr_scene_set_autotune(zr_scene* s, int mode)
     return ZR_OK;
 }
 
-int zr_scene_set_schedule(zr_scene* s, const int32_t in5[5])
+int zr_scene_set_schedule(zr_scene* s, const int32_t in6[6])
 {
-    if (!s || !in5) return ZR_ERR_ARG;
+    if (!s || !in6) return ZR_ERR_ARG;
     zr::Schedule sc;
-    sc.fused = in5[0];
-    sc.chunk = in5[1];
-    sc.buffers = in5[2];
-    sc.scatter_ctas_per_sm = in5[3];
-    sc.g2p_threads = in5[4];
+    sc.fused = in6[0];
+    sc.chunk = in6[1];
+    sc.buffers = in6[2];
+    sc.scatter_ctas_per_sm = in6[3];
+    sc.g2p_threads = in6[4];
+    sc.g2p_tight = in6[5];
     if (s->eng) {
         int rc = s->eng->set_schedule(sc);
         if (rc) s->err = s->eng->last_error();
@@ -551,21 +552,22 @@ int zr_scene_set_schedule(zr_scene* s, const int32_t in5[5])
     return ZR_OK;
 }
 
-static void schedule_out(const zr::Schedule& sc, int32_t out6[6])
+static void schedule_out(const zr::Schedule& sc, int32_t out7[7])
 {
-    out6[0] = sc.fused;
-    out6[1] = sc.chunk;
-    out6[2] = sc.buffers;
-    out6[3] = sc.scatter_ctas_per_sm;
-    out6[4] = sc.g2p_threads;
-    out6[5] = sc.tuned;
+    out7[0] = sc.fused;
+    out7[1] = sc.chunk;
+    out7[2] = sc.buffers;
+    out7[3] = sc.scatter_ctas_per_sm;
+    out7[4] = sc.g2p_threads;
+    out7[5] = sc.g2p_tight;
+    out7[6] = sc.tuned;
 }
 
-int zr_scene_get_schedule(zr_scene* s, int32_t out6[6])
+int zr_scene_get_schedule(zr_scene* s, int32_t out7[7])
 {
     NEED_ENGINE(s);
-    if (!out6) return ZR_ERR_ARG;
-    schedule_out(s->eng->schedule(), out6);
+    if (!out7) return ZR_ERR_ARG;
+    schedule_out(s->eng->schedule(), out7);
     return ZR_OK;
 }
 
@@ -805,11 +807,11 @@ int zr_batch_set_autotune(zr_batch* b, int mode)
     return ZR_OK;
 }
 
-int zr_batch_get_schedule(zr_batch* b, int32_t out6[6])
+int zr_batch_get_schedule(zr_batch* b, int32_t out7[7])
 {
     NEED_BATCH(b);
-    if (!out6) return ZR_ERR_ARG;
-    schedule_out(b->eng->schedule(), out6);
+    if (!out7) return ZR_ERR_ARG;
+    schedule_out(b->eng->schedule(), out7);
     return ZR_OK;
 }
 

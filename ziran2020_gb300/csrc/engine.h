@@ -67,6 +67,7 @@ struct Schedule {
     int buffers = 1; // P2G: staging buffers (2: the next chunk's copy overlaps the whole current chunk)
     int scatter_ctas_per_sm = 0; // P2G scatter: persistent CTAs per SM
     int g2p_threads = 0; // G2P: threads per CTA, i.e. particles per pass over a group
+    int g2p_tight = 0; // G2P: 1 = registers cut for more resident threads per SM
     int tuned = 0; // 1 when chosen by the autotuner's measurements
 };
 

@@ -41,6 +41,8 @@ class Engine final : public EngineBase {
     static constexpr int VAR_CHUNK[3] = { CH_BIG, CH_BIG, CH_BIG / 2 };
     static constexpr int VAR_NBUF[3] = { 1, 2, 2 };
     static constexpr int G2P_NT[3] = { 64, 128, 256 };
+    // G2P register budgets: threads per SM (FP32: 128 or ~100 registers; FP64: ~255 or ~200)
+    static constexpr int G2P_RES[2] = { sizeof(T) == 4 ? 512 : 256, sizeof(T) == 4 ? 640 : 320 };
     // fused P2G register budgets: cut for 2 or 3 CTAs per SM (FP32), 1 or 2 (FP64)
     static constexpr int FUSED_MINB[2] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2 };
 
@@ -499,7 +501,7 @@ public:
     int set_schedule(const Schedule& sc) override
     {
         if (sc.fused < 0 || sc.fused > 2 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
-            || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8)
+            || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8 || sc.g2p_tight < 0 || sc.g2p_tight > 1)
             return arg("schedule: unknown P2G form, (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
         sched_ = sc;
         if (sc.fused) {
@@ -539,13 +541,13 @@ private:
     DevStatus* hst_ = nullptr;
     void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
-    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[3] = { 1, 1, 1 };
+    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
     int occ_fused_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } }; // [register budget variant][model set]
     int models_ = 3; // bit 0: a corotated material is present, bit 1: a Neo-Hookean (Borden) material
     bool any_damage_ = false;
     T* pay_ = nullptr;
     int64_t pstride_ = 0;
-    Schedule sched_{ 0, VAR_CHUNK[0], VAR_NBUF[0], 2, 128, 0 };
+    Schedule sched_{ 0, VAR_CHUNK[0], VAR_NBUF[0], 2, 128, 0, 0 };
     int autotune_mode_ = 1; // 0 off (defaults), 1 on (cached), 2 always re-tune on a new batch
     bool tuned_ = false;
     bool fixed_schedule_ = false;
@@ -688,12 +690,16 @@ private:
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[0], k_stress<T, 1>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 3>, 256, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[0], k_g2p<T, G2P_NT[0]>, G2P_NT[0], 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[1], k_g2p<T, G2P_NT[1]>, G2P_NT[1], 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[2], k_g2p<T, G2P_NT[2]>, G2P_NT[2], 0);
+        g2p_setup<0, 0>();
+        g2p_setup<0, 1>();
+        g2p_setup<0, 2>();
+        g2p_setup<1, 0>();
+        g2p_setup<1, 1>();
+        g2p_setup<1, 2>();
         for (int& o : occ_scatter_) o = std::max(1, o);
         for (int& o : occ_stress_) o = std::max(1, o);
-        for (int& o : occ_g2p_) o = std::max(1, o);
+        for (auto& row : occ_g2p_)
+            for (int& o : row) o = std::max(1, o);
         sched_.scatter_ctas_per_sm = occ_scatter_[0];
         sched_.tuned = 0;
         if (const char* e = std::getenv("ZR_AUTOTUNE")) autotune_mode_ = std::atoi(e);
@@ -856,12 +862,10 @@ private:
         k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));
         const int gi = std::max(0, g2p_index(sched_.g2p_threads));
-        if (gi == 0)
-            k_g2p<T, G2P_NT[0]><<<nsm_ * occ_g2p_[0], G2P_NT[0], 0, stream_>>>(a);
-        else if (gi == 1)
-            k_g2p<T, G2P_NT[1]><<<nsm_ * occ_g2p_[1], G2P_NT[1], 0, stream_>>>(a);
+        if (sched_.g2p_tight)
+            launch_g2p<1>(a, gi);
         else
-            k_g2p<T, G2P_NT[2]><<<nsm_ * occ_g2p_[2], G2P_NT[2], 0, stream_>>>(a);
+            launch_g2p<0>(a, gi);
         k_step_end<T><<<1, 256, 0, stream_>>>(d_scenes_, n_scenes(), st_);
         if (ev) ZR_CUDA(cudaEventRecord(ev[5], stream_));
         ZR_CUDA(cudaGetLastError());
@@ -971,6 +975,21 @@ private:
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_scatter_[V], k, S::NT, S::dyn_bytes);
     }
+    template <int R, int N>
+    void g2p_setup()
+    {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[R][N], k_g2p<T, G2P_NT[N], G2P_RES[R]>, G2P_NT[N], 0);
+    }
+    template <int R>
+    void launch_g2p(const StepArgs<T>& a, int gi)
+    {
+        if (gi == 0)
+            k_g2p<T, G2P_NT[0], G2P_RES[R]><<<nsm_ * occ_g2p_[R][0], G2P_NT[0], 0, stream_>>>(a);
+        else if (gi == 1)
+            k_g2p<T, G2P_NT[1], G2P_RES[R]><<<nsm_ * occ_g2p_[R][1], G2P_NT[1], 0, stream_>>>(a);
+        else
+            k_g2p<T, G2P_NT[2], G2P_RES[R]><<<nsm_ * occ_g2p_[R][2], G2P_NT[2], 0, stream_>>>(a);
+    }
     template <int M, int MINB>
     void fused_setup(int var, int slot)
     {
@@ -1067,7 +1086,7 @@ private:
         return false;
     }
 
-    Schedule default_schedule() const { return Schedule{ 0, VAR_CHUNK[0], VAR_NBUF[0], occ_scatter_[0], G2P_NT[1], 0 }; }
+    Schedule default_schedule() const { return Schedule{ 0, VAR_CHUNK[0], VAR_NBUF[0], occ_scatter_[0], G2P_NT[1], 0, 0 }; }
 
     int autotune_trials()
     {
@@ -1084,10 +1103,10 @@ private:
         std::vector<Schedule> p2g_c;
         for (int vi = 0; vi < 3; vi++)
             for (int c = occ_scatter_[vi]; c >= std::max(1, occ_scatter_[vi] - 1); c--)
-                p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 1 });
+                p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 0, 1 });
         for (int fv = 0; fv < 2; fv++) {
             const int of = occ_fused_[fv][models_slot()];
-            for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1 + fv, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 1 });
+            for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1 + fv, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 0, 1 });
         }
         constexpr int REPS = 2; // the first run of a candidate warms caches and instruction memory
         Schedule best = p2g_c[0];
@@ -1111,9 +1130,11 @@ private:
                 best = sc;
             }
         }
-        for (int gi = 0; gi < 3; gi++) {
+        for (int gc = 0; gc < 6; gc++) {
+            const int gi = gc % 3;
             Schedule sc = best;
             sc.g2p_threads = G2P_NT[gi];
+            sc.g2p_tight = gc / 3;
             float mg = 1e30f;
             for (int r = 0; r < REPS; r++) {
                 float p = 0, g = 0;
@@ -1130,6 +1151,7 @@ private:
             if (mg < best_g2p) {
                 best_g2p = mg;
                 best.g2p_threads = sc.g2p_threads;
+                best.g2p_tight = sc.g2p_tight;
             }
         }
         best.tuned = 1;

@@ -887,8 +887,9 @@ __global__ void k_grid(StepArgs<T> a)
 // ---------------------------------------------------------------------------------------------------
 // G2P
 // ---------------------------------------------------------------------------------------------------
-template <class T, int NT>
-__global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 512 : 256) / NT) k_g2p(StepArgs<T> a)
+// NT threads per CTA; RESIDENT: threads per SM the register budget is cut for
+template <class T, int NT, int RESIDENT>
+__global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
     __shared__ __align__(16) T sv[8 * NVEL * L::nodes];
