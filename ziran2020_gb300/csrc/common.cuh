@@ -6,9 +6,11 @@
 #if defined(__CUDACC__)
 #define ZR_HD __host__ __device__ __forceinline__
 #define ZR_D __device__ __forceinline__
+#define ZR_COLD __host__ __device__ __noinline__
 #else
 #define ZR_HD inline
 #define ZR_D inline
+#define ZR_COLD inline
 #endif
 
 namespace zr {

@@ -249,6 +249,18 @@ ZR_HD void svd3_jacobi(const double* A, double* U, double* s, double* V)
 // Determinant-scaled Newton iteration X <- (g X + X^{-T}/g)/2 in T; it converges quadratically to R
 // whenever det F > 0. Inverted, nearly singular or ill-conditioned F goes to the FP64 SVD.
 // Returns true when the FP64 path was taken.
+// The FP64 path of polar_rotation, kept out of line: it is rare, and inlining it into every kernel that
+// decomposes F would crowd the instruction cache of the hot loops.
+template <class T>
+ZR_COLD void polar_rotation_fp64(const T* F, T* R)
+{
+    double A[9], U[9], s[3], V[9];
+    for (int i = 0; i < 9; i++) A[i] = (double)F[i];
+    svd3_jacobi(A, U, s, V);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) R[3 * r + c] = (T)(U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + U[3 * r + 2] * V[3 * c + 2]);
+}
+
 template <class T>
 ZR_HD bool polar_rotation(const T* F, T* R)
 {
@@ -289,11 +301,7 @@ ZR_HD bool polar_rotation(const T* F, T* R)
         for (int i = 0; i < 9; i++) R[i] = X[i];
         return false;
     }
-    double A[9], U[9], s[3], V[9];
-    for (int i = 0; i < 9; i++) A[i] = (double)F[i];
-    svd3_jacobi(A, U, s, V);
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) R[3 * r + c] = (T)(U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + U[3 * r + 2] * V[3 * c + 2]);
+    polar_rotation_fp64(F, R);
     return true;
 }
 
