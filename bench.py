@@ -29,11 +29,14 @@ WORKLOADS = {
     "aniso_slab_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256)),
     "aniso_slab_dx128": (1, dict()),
     "elastic_box_dx64": (0, dict()),
+    # the same slab with the QR-stable Neo-Hookean model and fibre stiffness 10 mu (examples/tubepull.h:104-107)
+    "aniso_slab_qr_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256, model=2, fiber_stiffness=10.0)),
 }
 # CPU sample: the same slab at the same resolution, cropped to a 0.125 x 0.1 x 0.125 m piece
 CPU_SAMPLE = {"aniso_slab_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125)),
               "aniso_slab_dx128": dict(size=(0.25, 0.1, 0.25)),
-              "elastic_box_dx64": dict()}
+              "elastic_box_dx64": dict(),
+              "aniso_slab_qr_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), model=2, fiber_stiffness=10.0)}
 
 
 def parse():
@@ -251,7 +254,8 @@ def error_vs_oracle(steps):
 def _desc_for(kind, over, scenes):
     if kind == 1:
         dx = over.get("dx", 1 / 128)
-        return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345)
+        return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345, model=over.get("model") or None,
+                                 fiber=over.get("fiber_stiffness", 0.0))
     return scenes.elastic_box(size=over.get("size", 0.25), dx=over.get("dx", 1 / 64), seed=12345)
 
 

@@ -40,6 +40,7 @@ extern "C" {
 /* ---- constitutive models ---- */
 #define ZR_COROTATED 0           /* Physics/ConstitutiveModel/CorotatedElasticity.cpp */
 #define ZR_NEOHOOKEAN_BORDEN 1   /* Physics/ConstitutiveModel/NeoHookeanBorden.cpp */
+#define ZR_QR_STABLE_NEOHOOKEAN 2 /* Physics/ConstitutiveModel/QRStableNeoHookean.h */
 
 /* ---- collision object types (Math/Geometry/CollisionObject.h:47-50) ---- */
 #define ZR_STICKY 1
@@ -89,8 +90,12 @@ int zr_scene_add_particles(zr_scene* s, int64_t n, const double* x, const double
 int zr_scene_add_corotated(zr_scene* s, int64_t first, int64_t count, double E, double nu);
 /* MpmParticleHandleBase::addFBasedMpmForce(NeoHookeanBorden(E, nu)). */
 int zr_scene_add_neohookean_borden(zr_scene* s, int64_t first, int64_t count, double E, double nu);
+/* MpmParticleHandleBase::addFBasedMpmForce(QRStableNeoHookean(E, nu)) after setExtraFiberStiffness(0, fiber_x)
+ * and setExtraFiberStiffness(1, fiber_y) (QRStableNeoHookean.h:98-107): fibre stiffness kx = fiber_x mu
+ * along the material x axis (r00 of F = QR) and ky = fiber_y mu; 0 and 0 give the isotropic model. */
+int zr_scene_add_qr_stable_neohookean(zr_scene* s, int64_t first, int64_t count, double E, double nu, double fiber_x, double fiber_y);
 /* MpmParticleHandleBase::addFBasedMpmForceWithAnisotropicPhaseField (MpmParticleHandleBase.cpp:175-222) for a
- * range that already has a Neo-Hookean (Borden) model: one structural director a0 = e1 with weight alpha
+ * range that already has a Neo-Hookean (Borden) or QR-stable Neo-Hookean model: one structural director a0 = e1 with weight alpha
  * (fibre directions are encoded in the initial F, see zr_rotated_F), length scale l0, viscosity eta,
  * scale zeta, residual stiffness; sigma_crit holds one critical stress per particle of the range. */
 int zr_scene_add_aniso_damage(zr_scene* s, int64_t first, int64_t count, double alpha, double l0, double eta, double zeta, double residual,
@@ -170,7 +175,8 @@ typedef struct zr_scene_recipe {
     double pull_speed;    /* ANISO_SLAB: the two x ends move apart at +-pull_speed */
     double grip_cells;    /* ANISO_SLAB: width of each sticky end plate in cells */
     int32_t domain_cells; /* 0 = round(1/dx) + 4 (the unit box) */
-    int32_t reserved;
+    int32_t model;        /* ANISO_SLAB: 0 or ZR_NEOHOOKEAN_BORDEN (default), or ZR_QR_STABLE_NEOHOOKEAN */
+    double fiber_stiffness; /* ANISO_SLAB with ZR_QR_STABLE_NEOHOOKEAN: kx in units of mu (setExtraFiberStiffness(0, .)) */
 } zr_scene_recipe;
 
 /* Defaults: ELASTIC_BOX = unit box, dx 1/64, cube side 0.25 at (0.5,0.6,0.5), 8 ppc, corotated E=1e4
@@ -188,6 +194,9 @@ int zr_scene_from_recipe(zr_scene* s, const zr_scene_recipe* r);
 void zr_rotated_F(const double a0[3], double F[9]);
 /* NeoHookeanBorden::getSigmaCrit(percentage) (NeoHookeanBorden.cpp:38-44): psi at F = (1+p) I. */
 double zr_nhb_sigma_crit(double E, double nu, double percentage);
+/* QRStableNeoHookean::getSigmaCrit(percentage) (QRStableNeoHookean.h:68-84): psi at F = (1+p) I of the
+ * undegraded isotropic model. */
+double zr_qrnh_sigma_crit(double E, double nu, double percentage);
 
 /* ================================ batch: many scenes, one launch per kernel ================================ */
 int zr_batch_create(int precision, zr_batch** out);

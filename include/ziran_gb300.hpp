@@ -44,6 +44,25 @@ struct NeoHookeanBorden {
     T getSigmaCrit(T percentage) const { return (T)zr_nhb_sigma_crit(E, nu, percentage); }
 };
 
+// QRStableNeoHookean(E, nu) with setExtraFiberStiffness (QRStableNeoHookean.h:58-107)
+template <class T>
+struct QRStableNeoHookean {
+    T E, nu;
+    T kx_scale = 0, ky_scale = 0; // fibre stiffness in units of mu
+    QRStableNeoHookean(T E_, T nu_) : E(E_), nu(nu_) {}
+    void setExtraFiberStiffness(int component, T scale)
+    {
+        if (component == 0)
+            kx_scale = scale;
+        else if (component == 1)
+            ky_scale = scale;
+        else
+            throw std::runtime_error("It is not allowed to put fiber at z direction");
+    }
+    // QRStableNeoHookean::getSigmaCrit (QRStableNeoHookean.h:68-84)
+    T getSigmaCrit(T percentage) const { return (T)zr_qrnh_sigma_crit(E, nu, percentage); }
+};
+
 enum CollisionType { STICKY = ZR_STICKY, SLIP = ZR_SLIP, SEPARATE = ZR_SEPARATE };
 
 template <class T>
@@ -62,11 +81,16 @@ public:
     // MpmParticleHandleBase::addFBasedMpmForce (MpmParticleHandleBase.cpp:132-145)
     void addFBasedMpmForce(const CorotatedElasticity<T>& m) { sim_->check(zr_scene_add_corotated(sim_->h_, first, count, m.E, m.nu)); }
     void addFBasedMpmForce(const NeoHookeanBorden<T>& m) { sim_->check(zr_scene_add_neohookean_borden(sim_->h_, first, count, m.E, m.nu)); }
+    void addFBasedMpmForce(const QRStableNeoHookean<T>& m)
+    {
+        sim_->check(zr_scene_add_qr_stable_neohookean(sim_->h_, first, count, m.E, m.nu, m.kx_scale, m.ky_scale));
+    }
 
     // MpmParticleHandleBase::addFBasedMpmForceWithAnisotropicPhaseField (MpmParticleHandleBase.cpp:175-222) with one
     // director a0 = e1 (fibre directions are carried by the initial F, see fibreRotatedF) and a critical stress per
     // particle (the reference sets one per handle from `percentage`; pass model.getSigmaCrit(percentage) to all).
-    void addFBasedMpmForceWithAnisotropicPhaseField(T alpha, T l0, const NeoHookeanBorden<T>& model, T eta, T zeta, T residual,
+    template <class Model> // NeoHookeanBorden<T> or QRStableNeoHookean<T>
+    void addFBasedMpmForceWithAnisotropicPhaseField(T alpha, T l0, const Model& model, T eta, T zeta, T residual,
         const std::vector<T>& sigma_crit)
     {
         addFBasedMpmForce(model);

@@ -591,12 +591,13 @@ inline void sym_eigen(const double S[3][3], double lam[3], double Q[3][3])
 // ----------------------------------------------------------------------------------------------
 // Materials
 // ----------------------------------------------------------------------------------------------
-enum { MODEL_COROTATED = 0, MODEL_NHB = 1 };
+enum { MODEL_COROTATED = 0, MODEL_NHB = 1, MODEL_QRNH = 2 };
 
 template <class T>
 struct Material {
     int model = MODEL_COROTATED;
     T mu = 0, lambda = 0, kappa = 0;
+    T kx = 0, ky = 0; // QRStableNeoHookean fibre stiffness (QRStableNeoHookean.h:98-107)
     bool damage = false;
     T alpha = 0, l0 = 0, eta = 1, zeta = 1, residual = 0;
 };
@@ -632,6 +633,84 @@ inline M3<T> tau_nhb(const Material<T>& mat, const M3<T>& F, T g)
             tau(r, c) = (J >= 1) ? g * (td + tv) : g * td + tv;
         }
     return tau;
+}
+
+// Givens QR, GivensQR.h:10-48 (inplaceGivensQR: for each column j, rows i = m-1 .. j+1, a rotation of rows
+// (i-1, i) built from (A(i-1,j), A(i,j)) applied to A and to M = I; Q = M^T), then the 3D sign convention of
+// QRStableNeoHookean::updateScratch (QRStableNeoHookean.h:108-122)
+template <class T>
+inline void givens_qr(const M3<T>& F, M3<T>& Q, M3<T>& R)
+{
+    T A[3][3], M[3][3] = { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 } };
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) A[r][c] = F(r, c);
+    for (int j = 0; j < 3; j++)
+        for (int i = 2; i > j; i--) {
+            Givens<T> g(i - 1, i);
+            g.compute(A[i - 1][j], A[i][j]);
+            g.rows(A);
+            g.rows(M);
+        }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            R(r, c) = A[r][c];
+            Q(r, c) = M[c][r];
+        }
+    if (R(0, 0) < 0) {
+        R(0, 0) *= -1;
+        for (int r = 0; r < 3; r++) Q(r, 0) *= -1;
+        R(0, 1) *= -1;
+        R(0, 2) *= -1;
+        R(2, 2) *= -1;
+        for (int r = 0; r < 3; r++) Q(r, 2) *= -1;
+    }
+    if (R(1, 1) < 0) {
+        R(1, 1) *= -1;
+        for (int r = 0; r < 3; r++) Q(r, 1) *= -1;
+        R(1, 2) *= -1;
+        R(2, 2) *= -1;
+        for (int r = 0; r < 3; r++) Q(r, 2) *= -1;
+    }
+}
+
+// QRStableNeoHookean::updateScratch (QRStableNeoHookean.h:102-173) -> dPsiHat/dR; firstPiola through
+// QrBasedHelper::evaluateP (QrBasedHelper.h:30-40): A = dPsiHatdR R^T with the lower triangle mirrored,
+// P = Q A R^{-T}; kirchhoff = P F^T (HyperelasticConstitutiveModel.h:75-80). effective: g = 1, kx = ky = 0
+// (evaluateEffectiveCauchyStress, QRStableNeoHookean.h:86-96). J (from R) is returned through Jout.
+template <class T>
+inline M3<T> tau_qrnh(const Material<T>& mat, const M3<T>& F, T g, bool effective, T* Jout = nullptr)
+{
+    M3<T> Q, R;
+    givens_qr(F, Q, R);
+    T kx = mat.kx, ky = mat.ky;
+    if (effective) {
+        g = 1;
+        kx = 0;
+        ky = 0;
+    }
+    T J = 1;
+    for (int i = 0; i < 3; i++) J *= R(i, i);
+    M3<T> D{};
+    if (J >= 1)
+        for (int i = 0; i < 3; i++) D(i, i) += g * mat.lambda * (J - 1) * J / R(i, i);
+    else
+        for (int i = 0; i < 3; i++) D(i, i) += mat.lambda * (J - 1) * J / R(i, i);
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) D(i, j) += g * mat.mu * R(i, j);
+    for (int i = 0; i < 3; i++) D(i, i) -= g * mat.mu * J / R(i, i);
+    D(0, 0) += kx * (R(0, 0) - 1);
+    T ss = std::sqrt(R(0, 1) * R(0, 1) + R(1, 1) * R(1, 1));
+    D(0, 1) += ky * (ss - 1) * R(0, 1) / ss;
+    D(1, 1) += ky * (ss - 1) * R(1, 1) / ss;
+    M3<T> A = mul_bt(D, R); // dPsiHatdR * R^T
+    for (int i = 1; i < 3; i++)
+        for (int j = 0; j < i; j++) A(i, j) = A(j, i);
+    M3<T> RinvT = cofactor(R); // R^{-T} = cofactor(R) / det(R)
+    T dR = det(R);
+    for (int a = 0; a < 9; a++) RinvT.a[a] /= dR;
+    M3<T> P = mul(mul(Q, A), RinvT);
+    if (Jout) *Jout = J;
+    return mul_bt(P, F);
 }
 
 template <class T>
@@ -863,10 +942,13 @@ struct Scene {
         for (int64_t p = 0; p < n; p++) {
             const Material<T>& mt = materials[mat[p]];
             M3<T> tau;
+            const T g = damage && mt.damage ? degradation(d[p], mt.residual) : (T)1;
             if (mt.model == MODEL_COROTATED)
-                tau = tau_corotated(mt, F[p]);
+                tau = tau_corotated(mt, F[p]); // no degradation member: never damaged (AnisoFractureSimulation.h:343-352)
+            else if (mt.model == MODEL_QRNH)
+                tau = tau_qrnh(mt, F[p], g, false);
             else
-                tau = tau_nhb(mt, F[p], damage ? degradation(d[p], mt.residual) : (T)1);
+                tau = tau_nhb(mt, F[p], g);
             for (int a = 0; a < 9; a++) vtau[p].a[a] = tau.a[a] * V0[p]; // FBasedMpmForceHelper.cpp:58-62
         }
     }
@@ -1001,10 +1083,16 @@ struct Scene {
             const Material<T>& mt = materials[mat[p]];
             // the reference damages only particles that carry a phase field and one of its damageable models
             // (AnisoFractureSimulation.h:210-218,343-352); NeoHookeanBorden is the one restated here
-            if (mt.model != MODEL_NHB || !mt.damage) continue;
+            if ((mt.model != MODEL_NHB && mt.model != MODEL_QRNH) || !mt.damage) continue;
             T geo = d[p] - (mt.l0 * mt.l0 * lap[p]);
-            M3<T> tau = tau_nhb(mt, F[p], (T)1);
-            T J = det(F[p]);
+            T J;
+            M3<T> tau;
+            if (mt.model == MODEL_QRNH)
+                tau = tau_qrnh(mt, F[p], (T)1, true, &J); // cauchy = P F^T / J, J from the QR (QRStableNeoHookean.h:86-96)
+            else {
+                tau = tau_nhb(mt, F[p], (T)1);
+                J = det(F[p]);
+            }
             double S[3][3], lam[3], Q[3][3];
             for (int r = 0; r < 3; r++)
                 for (int c = 0; c < 3; c++) S[r][c] = (double)(tau(r, c) / J);
@@ -1235,8 +1323,10 @@ void orc_destroy(void* hp)
     delete h;
 }
 
-// model 0 = fixed corotated, 1 = Neo-Hookean (Borden). Returns the material index.
-int orc_add_material(void* hp, int model, double E, double nu, int damage, double alpha, double l0, double eta, double zeta, double residual)
+// model 0 = fixed corotated, 1 = Neo-Hookean (Borden), 2 = QR-stable Neo-Hookean with fibre stiffness
+// kx = kx_scale mu, ky = ky_scale mu. Returns the material index.
+int orc_add_material(void* hp, int model, double E, double nu, int damage, double alpha, double l0, double eta, double zeta, double residual,
+    double kx_scale, double ky_scale)
 {
     Handle* h = (Handle*)hp;
     int id = -1;
@@ -1250,6 +1340,8 @@ int orc_add_material(void* hp, int model, double E, double nu, int damage, doubl
         mt.mu = Et / ((T)2 * ((T)1 + nut));
         mt.lambda = lambda;
         mt.kappa = (T).666666 * mt.mu + lambda;
+        mt.kx = (T)kx_scale * mt.mu; // QRStableNeoHookean::setExtraFiberStiffness (QRStableNeoHookean.h:98-107)
+        mt.ky = (T)ky_scale * mt.mu;
         mt.damage = damage != 0;
         mt.alpha = (T)alpha;
         mt.l0 = (T)l0;
@@ -1419,6 +1511,40 @@ void orc_svd3(int precision, const double* A, double* U, double* sigma, double* 
         run(0.0f);
     else
         run(0.0);
+}
+
+// Kirchhoff stress of one model at one F (row-major), for unit tests: g = degradation, effective = the
+// undegraded isotropic form the damage update uses. Returns J as the model defines it.
+double orc_tau(int precision, int model, double E, double nu, double kx_scale, double ky_scale, double g, int effective, const double* F, double* tau)
+{
+    double J = 0;
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        Material<T> mt;
+        mt.model = model;
+        T Et = (T)E, nut = (T)nu;
+        mt.lambda = Et * nut / (((T)1 + nut) * ((T)1 - (T)2 * nut));
+        mt.mu = Et / ((T)2 * ((T)1 + nut));
+        mt.kappa = (T).666666 * mt.mu + mt.lambda;
+        mt.kx = (T)kx_scale * mt.mu;
+        mt.ky = (T)ky_scale * mt.mu;
+        M3<T> f, t;
+        for (int i = 0; i < 9; i++) f.a[i] = (T)F[i];
+        T Jm = det(f);
+        if (model == MODEL_COROTATED)
+            t = tau_corotated(mt, f);
+        else if (model == MODEL_QRNH)
+            t = tau_qrnh(mt, f, (T)g, effective != 0, &Jm);
+        else
+            t = tau_nhb(mt, f, effective ? (T)1 : (T)g);
+        for (int i = 0; i < 9; i++) tau[i] = t.a[i];
+        J = Jm;
+    };
+    if (precision == 4)
+        run(0.0f);
+    else
+        run(0.0);
+    return J;
 }
 
 // FP64-accumulated reductions (MpmSimulationDataAnalysis.h:67-151): out = {mass, px, py, pz, kinetic energy, max speed}

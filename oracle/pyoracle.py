@@ -34,7 +34,9 @@ def lib():
         L.orc_create.argtypes = [i32, d, d, P(d), d, d]
         L.orc_destroy.argtypes = [vp]
         L.orc_add_material.restype = i32
-        L.orc_add_material.argtypes = [vp, i32, d, d, i32, d, d, d, d, d]
+        L.orc_add_material.argtypes = [vp, i32, d, d, i32, d, d, d, d, d, d, d]
+        L.orc_tau.restype = d
+        L.orc_tau.argtypes = [i32, i32, d, d, d, d, d, i32, P(d), P(d)]
         L.orc_add_halfspace.argtypes = [vp, P(d), P(d), i32, d, P(d)]
         L.orc_set_particles.argtypes = [vp, i64] + [P(d)] * 8 + [P(C.c_int32)]
         L.orc_step.restype = i32
@@ -85,8 +87,8 @@ class OracleScene:
         except Exception:
             pass
 
-    def add_material(self, model, E, nu, damage=False, alpha=0.0, l0=0.0, eta=1.0, zeta=1.0, residual=0.0):
-        return self.L.orc_add_material(self.h, model, E, nu, int(damage), alpha, l0, eta, zeta, residual)
+    def add_material(self, model, E, nu, damage=False, alpha=0.0, l0=0.0, eta=1.0, zeta=1.0, residual=0.0, kx_scale=0.0, ky_scale=0.0):
+        return self.L.orc_add_material(self.h, model, E, nu, int(damage), alpha, l0, eta, zeta, residual, kx_scale, ky_scale)
 
     def add_halfspace(self, origin, normal, type_, friction=0.0, velocity=(0.0, 0.0, 0.0)):
         o, n, v = (np.asarray(a, dtype=np.float64) for a in (origin, normal, velocity))
@@ -150,6 +152,14 @@ def svd3(precision, A):
     U, s, V = np.zeros(9), np.zeros(3), np.zeros(9)
     lib().orc_svd3(precision, _p(A), _p(U), _p(s), _p(V))
     return U.reshape(3, 3), s, V.reshape(3, 3)
+
+
+def tau(precision, model, E, nu, F, g=1.0, effective=False, kx_scale=0.0, ky_scale=0.0):
+    """Kirchhoff stress of one constitutive model at F (3x3); returns (tau, J)."""
+    F = np.ascontiguousarray(F, dtype=np.float64).reshape(9)
+    out = np.zeros(9)
+    J = lib().orc_tau(precision, model, E, nu, kx_scale, ky_scale, g, int(effective), _p(F), _p(out))
+    return out.reshape(3, 3), J
 
 
 def num_threads():

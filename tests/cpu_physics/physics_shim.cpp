@@ -52,6 +52,43 @@ void shim_tau(int model, double E, double nu, const double* F, double g, double*
     else
         tau_nhb(m, F, g, tau);
 }
+// any model with fibre stiffness (scales of mu) and the effective (undegraded, isotropic) form; returns J
+double shim_tau2(int prec, int model, double E, double nu, double kx, double ky, const double* F, double g, int effective, double* tau)
+{
+    if (prec == 4) {
+        Material<float> m = mat<float>(model, E, nu);
+        m.kx = (float)kx * m.mu;
+        m.ky = (float)ky * m.mu;
+        float f[9], t[9];
+        for (int i = 0; i < 9; i++) f[i] = (float)F[i];
+        float J = model == MODEL_QR_STABLE_NEOHOOKEAN ? tau_qrnh(m, f, (float)g, t, effective != 0) : det3(f);
+        if (model == MODEL_NEOHOOKEAN_BORDEN) tau_nhb(m, f, effective ? 1.f : (float)g, t);
+        if (model == MODEL_COROTATED) tau_corotated(m, f, t);
+        for (int i = 0; i < 9; i++) tau[i] = t[i];
+        return J;
+    }
+    Material<double> m = mat<double>(model, E, nu);
+    m.kx = kx * m.mu;
+    m.ky = ky * m.mu;
+    double J = model == MODEL_QR_STABLE_NEOHOOKEAN ? tau_qrnh(m, F, g, tau, effective != 0) : det3(F);
+    if (model == MODEL_NEOHOOKEAN_BORDEN) tau_nhb(m, F, effective ? 1.0 : g, tau);
+    if (model == MODEL_COROTATED) tau_corotated(m, F, tau);
+    return J;
+}
+void shim_qr(const double* F, double* Q, double* R) { givens_qr3(F, Q, R); }
+double shim_damage2(int model, double E, double nu, double alpha, double l0, double eta, double zeta, double k, const double* F, double d, double lap,
+    double sc, double dt)
+{
+    Material<double> m = mat<double>(model, E, nu);
+    m.damage = 1;
+    m.alpha = alpha;
+    m.l0 = l0;
+    m.eta = eta;
+    m.zeta = zeta;
+    m.residual = k;
+    bool fb = false;
+    return damage_update(m, F, d, lap, sc, dt, fb);
+}
 double shim_damage(double E, double nu, double alpha, double l0, double eta, double zeta, double k, const double* F, double d, double lap, double sc,
     double dt)
 {

@@ -1,5 +1,6 @@
 """The C++ shim (include/ziran_gb300.hpp) compiles against the C ABI and links to the in-tree library; on a
-GPU the demo scene runs and conserves momentum up to the gravity impulse."""
+GPU the demo scenes run: a corotated cube conserves momentum up to the gravity impulse, and a QR-stable
+Neo-Hookean piece with fibre stiffness and anisotropic damage tears when pulled."""
 import os
 import subprocess
 
@@ -33,3 +34,7 @@ def test_shim_demo_runs(tmp_path):
     assert abs(t - 20 * 1e-4) < 1e-9
     m_total = n * 1000 * (1 / 64) ** 3 / 8
     assert abs(py - m_total * (-1.0 - 9.8 * 20e-4)) < 1e-4 * m_total
+    # the QR-stable Neo-Hookean piece with fibre stiffness and anisotropic damage: pulled at 1 m/s, it tears
+    n2, dmax = int(out[7]), float(out[9])
+    assert n2 == 12 * 4 * 4 * 8
+    assert 0 < dmax <= 1

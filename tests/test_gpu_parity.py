@@ -71,6 +71,24 @@ def test_aniso_slab_fp64_matches_oracle(steps):
         assert r["d"].max() > 0  # damage actually grew, so the comparison covers the damage path
 
 
+@pytest.mark.parametrize("fiber", [0.0, 10.0])
+def test_qr_stable_slab_matches_oracle(fiber):
+    """QR-stable Neo-Hookean (the AnisoMPM demos' model, fibre stiffness kx = fiber mu as in
+    examples/tubepull.h:104-107) with anisotropic damage: FP64 within 1e-12 of the FP64 oracle after 30
+    substeps, FP32 within 1e-5 after 30."""
+    d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0, model=zr.QR_STABLE_NEOHOOKEAN, fiber=fiber)
+    o = scenes.oracle_scene(d, 8)
+    o.step(30)
+    r = o.state()
+    assert r["d"].max() > 0  # damage grew
+    for prec, xtol in ((zr.F64, 1e-12), (zr.F32, 1e-5)):
+        s = scenes.gpu_scene(d, prec)
+        s.step(30)
+        e = scenes.errors(scenes.gpu_state(s), r)
+        assert e["x"][0] < xtol, (prec, e)
+        assert e["d"][0] < (1e-9 if prec == zr.F64 else 2e-2), (prec, e)
+
+
 def test_aniso_slab_fp32_close_to_fp64_oracle():
     d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0)
     s, o, g, r = run_pair(d, zr.F32, 60)

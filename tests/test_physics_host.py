@@ -27,6 +27,11 @@ def shim(tmp_path_factory):
     L.shim_damage.restype = C.c_double
     L.shim_damage.argtypes = [C.c_double] * 7 + [pd] + [C.c_double] * 4
     L.shim_key.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint, C.POINTER(C.c_ulonglong)]
+    L.shim_tau2.restype = C.c_double
+    L.shim_tau2.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, pd, C.c_double, C.c_int, pd]
+    L.shim_qr.argtypes = [pd, pd, pd]
+    L.shim_damage2.restype = C.c_double
+    L.shim_damage2.argtypes = [C.c_int] + [C.c_double] * 7 + [pd] + [C.c_double] * 4
     return L
 
 
@@ -164,3 +169,96 @@ def test_gpu_key_function_matches_oracle_layout(shim):
             data_bits = 6 if prec == 4 else 7
             want = ((po.linear_offset(prec, i, j, k) >> data_bits) << (32 - bb)) + idx
             assert key.value == want
+
+
+# ---------------------------------------------------------------- QR-stable Neo-Hookean (QRStableNeoHookean.h)
+E_, NU_ = 5e4, 0.25
+LAM_, MU_ = E_ * NU_ / ((1 + NU_) * (1 - 2 * NU_)), E_ / (2 * (1 + NU_))
+
+
+def qrnh_psi(F, g=1.0, kx=0.0, ky=0.0):
+    """The model's energy from the R of F = QR (QRStableNeoHookean.h:124-151); |r| makes it independent of
+    the sign convention of the factorisation, except J = det F."""
+    R = np.abs(np.linalg.qr(F)[1])
+    J = np.linalg.det(F)
+    vol = 0.5 * LAM_ * (J - 1) ** 2 * (g if J >= 1 else 1.0)
+    dev = g * (MU_ / 2 * (np.sum(np.triu(R) ** 2) - 3) - MU_ * (J - 1))
+    fib = kx * MU_ / 2 * (R[0, 0] - 1) ** 2 + ky * MU_ / 2 * (np.sqrt(R[0, 1] ** 2 + R[1, 1] ** 2) - 1) ** 2
+    return vol + dev + fib
+
+
+def random_F(rng, spread=0.15):
+    while True:
+        F = np.eye(3) + spread * rng.normal(size=(3, 3))
+        if np.linalg.det(F) > 0.3:
+            return F
+
+
+def test_givens_qr_convention(shim):
+    rng = np.random.default_rng(11)
+    for t in range(200):
+        F = np.ascontiguousarray(rng.normal(size=(3, 3)))
+        Q, R = np.zeros(9), np.zeros(9)
+        shim.shim_qr(p(F), p(Q), p(R))
+        Q, R = Q.reshape(3, 3), R.reshape(3, 3)
+        assert np.abs(Q @ R - F).max() < 1e-12 and np.abs(Q.T @ Q - np.eye(3)).max() < 1e-12
+        assert abs(np.linalg.det(Q) - 1) < 1e-12 and np.abs(np.tril(R, -1)).max() < 1e-12
+        assert R[0, 0] >= 0 and R[1, 1] >= 0 and np.sign(R[2, 2]) == np.sign(np.linalg.det(F))
+
+
+@pytest.mark.parametrize("g,kx,ky", [(1.0, 0.0, 0.0), (0.3, 0.0, 0.0), (1.0, 10.0, 0.0), (0.5, 4.0, 2.0)])
+def test_qrnh_stress_is_the_energy_gradient_and_matches_the_oracle(shim, g, kx, ky):
+    rng = np.random.default_rng(12)
+    for t in range(40):
+        F = np.ascontiguousarray(random_F(rng))
+        got = np.zeros(9)
+        J = shim.shim_tau2(8, 2, E_, NU_, kx, ky, p(F), g, 0, p(got))
+        got = got.reshape(3, 3)
+        ref, Jr = po.tau(8, 2, E_, NU_, F, g=g, kx_scale=kx, ky_scale=ky)
+        assert abs(J - np.linalg.det(F)) < 1e-12 and abs(Jr - J) < 1e-12
+        assert np.abs(got - ref).max() < 1e-9 * np.abs(ref).max(), t  # tau = Q A Q^T here, P F^T in the oracle
+        # P = dpsi/dF by central differences, tau = P F^T
+        h, P = 1e-6, np.zeros((3, 3))
+        for a in range(3):
+            for b in range(3):
+                Fp, Fm = F.copy(), F.copy()
+                Fp[a, b] += h
+                Fm[a, b] -= h
+                P[a, b] = (qrnh_psi(Fp, g, kx, ky) - qrnh_psi(Fm, g, kx, ky)) / (2 * h)
+        assert np.abs(P @ F.T - ref).max() < 1e-5 * max(1.0, np.abs(ref).max()), t
+        got32 = np.zeros(9)
+        shim.shim_tau2(4, 2, E_, NU_, kx, ky, p(F), g, 0, p(got32))
+        assert np.abs(got32.reshape(3, 3) - ref).max() < 2e-5 * np.abs(ref).max()
+
+
+def test_qrnh_effective_stress_and_sigma_crit(shim):
+    import ziran2020_gb300 as zr
+
+    rng = np.random.default_rng(13)
+    for t in range(20):
+        F = np.ascontiguousarray(random_F(rng))
+        eff = np.zeros(9)
+        shim.shim_tau2(8, 2, E_, NU_, 10.0, 3.0, p(F), 0.2, 1, p(eff))
+        iso = np.zeros(9)
+        shim.shim_tau2(8, 2, E_, NU_, 0.0, 0.0, p(F), 1.0, 0, p(iso))
+        assert np.abs(eff - iso).max() < 1e-9 * np.abs(iso).max()  # undegraded, fibres off
+    for pc in (0.05, 0.2):
+        assert abs(zr.qrnh_sigma_crit(E_, NU_, pc) - qrnh_psi((1 + pc) * np.eye(3))) < 1e-9 * qrnh_psi((1 + pc) * np.eye(3))
+
+
+def test_qrnh_damage_update_matches_reference_formula(shim):
+    rng = np.random.default_rng(14)
+    alpha, l0, eta, zeta, k = -1.0, 0.002, 0.1, 1.0, 0.01
+    for t in range(100):
+        F = np.ascontiguousarray(np.eye(3) + 0.05 * rng.normal(size=(3, 3)))
+        d, lap, sc, dt = rng.uniform(0, 0.5), rng.normal() * 100, rng.uniform(50, 500), 5e-5
+        got = shim.shim_damage2(2, E_, NU_, alpha, l0, eta, zeta, k, p(F), d, lap, sc, dt)
+        tau, J = po.tau(8, 2, E_, NU_, F, effective=True)
+        S = tau / J
+        w, Q = np.linalg.eigh((S + S.T) / 2)
+        sp = Q @ np.diag(np.maximum(w, 0)) @ Q.T
+        a = oracle_R(8, F)[:, 0]
+        A = np.eye(3) + alpha * np.outer(a, a)
+        phi = np.sum((A @ sp) * (sp @ A)) / sc ** 2
+        want = min(d + dt / eta * max((1 - d) * zeta * max(phi - 1, 0) - (d - l0 * l0 * lap), 0), 1)
+        assert abs(got - want) < 1e-10, t

@@ -19,7 +19,7 @@ ZR_ERR_ARG, ZR_ERR_CUDA, ZR_ERR_CFL, ZR_ERR_NONFINITE, ZR_ERR_OUT_OF_DOMAIN = 1,
 ZR_ERR_BUDGET, ZR_ERR_TIMEOUT, ZR_ERR_CAPACITY, ZR_ERR_STATE = 6, 7, 8, 9
 ERROR_NAMES = {1: "ARG", 2: "CUDA", 3: "CFL", 4: "NONFINITE", 5: "OUT_OF_DOMAIN", 6: "BUDGET", 7: "TIMEOUT", 8: "CAPACITY", 9: "STATE"}
 F32, F64 = 4, 8
-COROTATED, NEOHOOKEAN_BORDEN = 0, 1
+COROTATED, NEOHOOKEAN_BORDEN, QR_STABLE_NEOHOOKEAN = 0, 1, 2
 STICKY, SLIP, SEPARATE = 1, 2, 3
 FIELD = {"x": (0, 3), "v": (1, 3), "C": (2, 9), "F": (3, 9), "d": (4, 1), "m": (5, 1), "V0": (6, 1), "sigma_c": (7, 1)}
 RECIPE_ELASTIC_BOX, RECIPE_ANISO_SLAB = 0, 1
@@ -42,7 +42,7 @@ class Recipe(C.Structure):
                 ("E", C.c_double), ("nu", C.c_double), ("rho", C.c_double), ("apic_rpic_ratio", C.c_double), ("ground_y", C.c_double),
                 ("kappa_vmf", C.c_double), ("alpha", C.c_double), ("l0", C.c_double), ("eta", C.c_double), ("zeta", C.c_double),
                 ("residual", C.c_double), ("sigma_c_mean", C.c_double), ("sigma_c_std", C.c_double), ("pull_speed", C.c_double),
-                ("grip_cells", C.c_double), ("domain_cells", C.c_int32), ("reserved", C.c_int32)]
+                ("grip_cells", C.c_double), ("domain_cells", C.c_int32), ("model", C.c_int32), ("fiber_stiffness", C.c_double)]
 
 
 _lib = None
@@ -99,6 +99,8 @@ def load_library(build_if_needed=True):
         "zr_scene_from_recipe": (i32, [vp, P(Recipe)]),
         "zr_rotated_F": (None, [pd, pd]),
         "zr_nhb_sigma_crit": (d, [d, d, d]),
+        "zr_qrnh_sigma_crit": (d, [d, d, d]),
+        "zr_scene_add_qr_stable_neohookean": (i32, [vp, i64, i64, d, d, d, d]),
         "zr_batch_create": (i32, [i32, P(vp)]),
         "zr_batch_destroy": (i32, [vp]),
         "zr_batch_add_scene": (i32, [vp, vp, P(i32)]),
@@ -187,6 +189,10 @@ def nhb_sigma_crit(E, nu, percentage):
     return float(load_library().zr_nhb_sigma_crit(E, nu, percentage))
 
 
+def qrnh_sigma_crit(E, nu, percentage):
+    return float(load_library().zr_qrnh_sigma_crit(E, nu, percentage))
+
+
 class Scene:
     """One explicit-MPM simulation on the GPU (MpmSimulationBase<T,3> with the AnisoMPM damage override)."""
 
@@ -228,6 +234,9 @@ class Scene:
 
     def add_neohookean_borden(self, first, count, E, nu):
         self._check(self.L.zr_scene_add_neohookean_borden(self.h, first, count, E, nu))
+
+    def add_qr_stable_neohookean(self, first, count, E, nu, fiber_x=0.0, fiber_y=0.0):
+        self._check(self.L.zr_scene_add_qr_stable_neohookean(self.h, first, count, E, nu, fiber_x, fiber_y))
 
     def add_aniso_damage(self, first, count, alpha, l0, eta, zeta, residual, sigma_crit):
         sc = _f64(sigma_crit)

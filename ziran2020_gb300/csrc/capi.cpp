@@ -138,6 +138,15 @@ void zr_rotated_F(const double a0[3], double F[9])
 }
 
 // NeoHookeanBorden::getSigmaCrit: psi((1+p) I) with g = 1 (NeoHookeanBorden.cpp:38-68)
+double zr_qrnh_sigma_crit(double E, double nu, double p)
+{
+    double lambda = E * nu / ((1 + nu) * (1 - 2 * nu));
+    double mu = E / (2 * (1 + nu));
+    double r = 1 + p, J = r * r * r;
+    // R = (1+p) I: sum_{i<=j} r_ij^2 = 3 r^2
+    return 0.5 * lambda * (J - 1) * (J - 1) + (mu / 2 * (3 * r * r - 3) - mu * (J - 1));
+}
+
 double zr_nhb_sigma_crit(double E, double nu, double p)
 {
     double lambda = E * nu / ((1 + nu) * (1 - 2 * nu));
@@ -319,6 +328,20 @@ static int add_model(zr_scene* s, int64_t first, int64_t count, int model, doubl
 }
 
 int zr_scene_add_corotated(zr_scene* s, int64_t first, int64_t count, double E, double nu) { return add_model(s, first, count, ZR_COROTATED, E, nu); }
+int zr_scene_add_qr_stable_neohookean(zr_scene* s, int64_t first, int64_t count, double E, double nu, double fiber_x, double fiber_y)
+{
+    if (!s) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "materials must be attached before the first substep");
+    if (!(E > 0) || !(nu > -1 && nu < 0.5)) return set_err(s->err, ZR_ERR_ARG, "need E > 0 and -1 < nu < 0.5");
+    if (!(fiber_x >= 0) || !(fiber_y >= 0)) return set_err(s->err, ZR_ERR_ARG, "fibre stiffness scales must be >= 0");
+    SceneDesc::Mat m;
+    m.model = ZR_QR_STABLE_NEOHOOKEAN;
+    m.E = E;
+    m.nu = nu;
+    m.kx_scale = fiber_x;
+    m.ky_scale = fiber_y;
+    return assign_material(s->desc, first, count, m, s->err);
+}
 int zr_scene_add_neohookean_borden(zr_scene* s, int64_t first, int64_t count, double E, double nu)
 {
     return add_model(s, first, count, ZR_NEOHOOKEAN_BORDEN, E, nu);
@@ -335,8 +358,8 @@ int zr_scene_add_aniso_damage(zr_scene* s, int64_t first, int64_t count, double 
     const uint8_t base = d.material[first];
     for (int64_t i = first; i < first + count; i++)
         if (d.material[i] != base) return set_err(s->err, ZR_ERR_ARG, "the range must carry a single model");
-    if (d.materials[base].model != ZR_NEOHOOKEAN_BORDEN)
-        return set_err(s->err, ZR_ERR_ARG, "anisotropic damage is defined for the Neo-Hookean (Borden) model");
+    if (d.materials[base].model != ZR_NEOHOOKEAN_BORDEN && d.materials[base].model != ZR_QR_STABLE_NEOHOOKEAN)
+        return set_err(s->err, ZR_ERR_ARG, "anisotropic damage is defined for the Neo-Hookean (Borden) and QR-stable Neo-Hookean models");
     if (!(eta > 0)) return set_err(s->err, ZR_ERR_ARG, "eta must be positive");
     SceneDesc::Mat m = d.materials[base];
     m.damage = 1;
@@ -632,7 +655,10 @@ static int desc_from_recipe(SceneDesc& d, const zr_scene_recipe* r, std::string&
         d.objects.push_back(g);
     }
     else if (r->kind == ZR_RECIPE_ANISO_SLAB) {
-        m.model = ZR_NEOHOOKEAN_BORDEN;
+        if (r->model != 0 && r->model != ZR_NEOHOOKEAN_BORDEN && r->model != ZR_QR_STABLE_NEOHOOKEAN)
+            return set_err(err, ZR_ERR_ARG, "recipe model must be Neo-Hookean (Borden) or QR-stable Neo-Hookean");
+        m.model = r->model == ZR_QR_STABLE_NEOHOOKEAN ? ZR_QR_STABLE_NEOHOOKEAN : ZR_NEOHOOKEAN_BORDEN;
+        if (m.model == ZR_QR_STABLE_NEOHOOKEAN) m.kx_scale = r->fiber_stiffness;
         m.damage = 1;
         m.alpha = r->alpha;
         m.l0 = r->l0;

@@ -136,7 +136,7 @@ struct DevStatus {
 constexpr int MAX_OBJECTS = 8;
 constexpr int MAX_MATERIALS = 16;
 
-enum { MODEL_COROTATED = 0, MODEL_NEOHOOKEAN_BORDEN = 1 };
+enum { MODEL_COROTATED = 0, MODEL_NEOHOOKEAN_BORDEN = 1, MODEL_QR_STABLE_NEOHOOKEAN = 2 };
 enum { OBJ_STICKY = 1, OBJ_SLIP = 2, OBJ_SEPARATE = 3 };
 
 template <class T>
@@ -144,6 +144,7 @@ struct Material {
     int model;
     int damage; // AnisoMPM phase-field damage attached
     T mu, lambda, kappa;
+    T kx, ky; // QR-stable Neo-Hookean fibre stiffness (scale x mu, QRStableNeoHookean.h:75-86)
     T alpha, l0, eta, zeta, residual; // structural-tensor weight, length scale, viscosity, scale, residual stiffness
 };
 

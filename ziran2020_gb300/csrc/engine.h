@@ -22,8 +22,9 @@ struct SceneDesc {
     double time = 0;
     int32_t domain_cells = 0; // base nodes must stay in [0, domain_cells); 0 = the full 4096^3 SPGrid range
     struct Mat {
-        int model = 0; // 0 fixed corotated, 1 Neo-Hookean (Borden)
+        int model = 0; // 0 fixed corotated, 1 Neo-Hookean (Borden), 2 QR-stable Neo-Hookean
         double E = 1e4, nu = 0.3;
+        double kx_scale = 0, ky_scale = 0; // QR-stable Neo-Hookean fibre stiffness, in units of mu
         int damage = 0;
         double alpha = 0, l0 = 0, eta = 1, zeta = 1, residual = 0;
     };

@@ -185,7 +185,7 @@ public:
         models_ = 0;
         any_damage_ = false;
         for (auto& sp : h_scenes_) {
-            for (int k = 0; k < sp.n_materials; k++) models_ |= sp.materials[k].model == MODEL_COROTATED ? 1 : 2;
+            for (int k = 0; k < sp.n_materials; k++) models_ |= 1 << sp.materials[k].model;
             any_damage_ = any_damage_ || sp.damage;
         }
         tuned_ = false;
@@ -541,9 +541,9 @@ private:
     DevStatus* hst_ = nullptr;
     void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
-    int occ_stress_[3] = { 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
-    int occ_fused_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } }; // [register budget variant][model set]
-    int models_ = 3; // bit 0: a corotated material is present, bit 1: a Neo-Hookean (Borden) material
+    int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
+    int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [register budget variant][model set]
+    int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
     T* pay_ = nullptr;
     int64_t pstride_ = 0;
@@ -600,6 +600,8 @@ private:
             mt.lambda = E * nu / (((T)1 + nu) * ((T)1 - (T)2 * nu)); // CorotatedElasticity.cpp:16-21
             mt.mu = E / ((T)2 * ((T)1 + nu));
             mt.kappa = (T).666666 * mt.mu + mt.lambda; // NeoHookeanBorden.cpp:20
+            mt.kx = (T)m.kx_scale * mt.mu; // QRStableNeoHookean::setExtraFiberStiffness (QRStableNeoHookean.h:98-107)
+            mt.ky = (T)m.ky_scale * mt.mu;
             mt.alpha = (T)m.alpha;
             mt.l0 = (T)m.l0;
             mt.eta = (T)m.eta;
@@ -683,13 +685,16 @@ private:
         scatter_setup<2>();
         fused_setup<1, FUSED_MINB[0]>(0, 0);
         fused_setup<2, FUSED_MINB[0]>(0, 1);
-        fused_setup<3, FUSED_MINB[0]>(0, 2);
+        fused_setup<4, FUSED_MINB[0]>(0, 2);
+        fused_setup<7, FUSED_MINB[0]>(0, 3);
         fused_setup<1, FUSED_MINB[1]>(1, 0);
         fused_setup<2, FUSED_MINB[1]>(1, 1);
-        fused_setup<3, FUSED_MINB[1]>(1, 2);
+        fused_setup<4, FUSED_MINB[1]>(1, 2);
+        fused_setup<7, FUSED_MINB[1]>(1, 3);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[0], k_stress<T, 1>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 3>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 4>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[3], k_stress<T, 7>, 256, 0);
         g2p_setup<0, 0>();
         g2p_setup<0, 1>();
         g2p_setup<0, 2>();
@@ -843,12 +848,15 @@ private:
                 launch_fused<FUSED_MINB[1]>(a, fctas);
         }
         else {
-            if (models_ == 1)
+            const int ms = models_slot();
+            if (ms == 0)
                 k_stress<T, 1><<<nsm_ * occ_stress_[0], 256, 0, stream_>>>(a);
-            else if (models_ == 2)
+            else if (ms == 1)
                 k_stress<T, 2><<<nsm_ * occ_stress_[1], 256, 0, stream_>>>(a);
+            else if (ms == 2)
+                k_stress<T, 4><<<nsm_ * occ_stress_[2], 256, 0, stream_>>>(a);
             else
-                k_stress<T, 3><<<nsm_ * occ_stress_[2], 256, 0, stream_>>>(a);
+                k_stress<T, 7><<<nsm_ * occ_stress_[3], 256, 0, stream_>>>(a);
             const int vi = std::max(0, variant_index(sched_.chunk, sched_.buffers));
             const int sctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_scatter_[vi]);
             if (vi == 0)
@@ -1002,14 +1010,17 @@ private:
     template <int MINB>
     void launch_fused(const StepArgs<T>& a, int ctas)
     {
-        if (models_ == 1)
+        const int ms = models_slot();
+        if (ms == 0)
             k_p2g_fused<T, 1, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
-        else if (models_ == 2)
+        else if (ms == 1)
             k_p2g_fused<T, 2, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+        else if (ms == 2)
+            k_p2g_fused<T, 4, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
         else
-            k_p2g_fused<T, 3, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            k_p2g_fused<T, 7, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
     }
-    int models_slot() const { return models_ == 1 ? 0 : (models_ == 2 ? 1 : 2); }
+    int models_slot() const { return models_ == 1 ? 0 : (models_ == 2 ? 1 : (models_ == 4 ? 2 : 3)); }
     template <int V>
     void launch_scatter(const StepArgs<T>& a, int ctas)
     {

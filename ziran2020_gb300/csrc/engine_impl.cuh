@@ -325,11 +325,14 @@ __device__ __forceinline__ void particle_payload(const Pool<T>& P, uint32_t j, c
     const uint32_t mat = P.pid[j] >> L::index_bits;
     const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
     T tau[9];
-    if (MODELS == 1 || (MODELS == 3 && mt.model == MODEL_COROTATED)) {
+    const T g = (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1;
+    if (MODELS == 1 || (MODELS == 7 && mt.model == MODEL_COROTATED)) { // the reference degrades no corotated model
         if (tau_corotated(mt, F, tau)) fallbacks++;
     }
+    else if (MODELS == 4 || (MODELS == 7 && mt.model == MODEL_QR_STABLE_NEOHOOKEAN))
+        tau_qrnh(mt, F, g, tau);
     else
-        tau_nhb(mt, F, (damage && mt.damage) ? degradation(dd, mt.residual) : (T)1, tau);
+        tau_nhb(mt, F, g, tau);
     const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt;
     T fr[3];
 #pragma unroll
@@ -1084,7 +1087,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                 // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
                 const uint32_t mat = pid >> L::index_bits;
                 const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
-                if (mt.damage && mt.model == MODEL_NEOHOOKEAN_BORDEN) {
+                if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
                     bool fb = false;
                     dd = damage_update(mt, F, dd, lap, sc, dt, fb);
                     if (fb) atomicAdd(&a.st->fallback, 1u);

@@ -428,6 +428,102 @@ ZR_HD void tau_nhb(const Material<T>& mt, const T* F, T g, T* tau)
         for (int c = 0; c < 3; c++) tau[3 * r + c] = gd * (B[3 * r + c] - (r == c ? tr3 : (T)0)) + (r == c ? gv : (T)0);
 }
 
+// Givens QR of a 3x3 matrix, F = Q R, with Ziran's rotation order (GivensQR.h: for each column j, rows
+// i = 2 .. j+1 bottom-up, a rotation of rows (i-1, i) zeroing R(i, j), applied to R and accumulated into
+// Q^T) and the sign convention of QRStableNeoHookean::updateScratch (QRStableNeoHookean.h:102-122): R(0,0)
+// and R(1,1) made non-negative by flipping a column of Q with the matching row of R and, to keep Q a
+// rotation, column 2 of Q with R(2,2).
+template <class T>
+ZR_HD void givens_qr3(const T* F, T* Q, T* R)
+{
+    T M[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 }; // Q^T
+    for (int i = 0; i < 9; i++) R[i] = F[i];
+    for (int j = 0; j < 3; j++)
+        for (int i = 2; i > j; i--) {
+            // rotation (c -s; s c) of rows (i-1, i) with (c -s; s c) (a; b) = (r; 0) (Givens.h GivensRotation)
+            const T a = R[3 * (i - 1) + j], b = R[3 * i + j];
+            const T d = a * a + b * b;
+            T c = 1, sn = 0;
+            if (d != (T)0) {
+                const T t = (T)1 / sqrt(d);
+                c = a * t;
+                sn = -b * t;
+            }
+            for (int k = 0; k < 3; k++) {
+                const T r1 = R[3 * (i - 1) + k], r2 = R[3 * i + k];
+                R[3 * (i - 1) + k] = c * r1 - sn * r2;
+                R[3 * i + k] = sn * r1 + c * r2;
+                const T m1 = M[3 * (i - 1) + k], m2 = M[3 * i + k];
+                M[3 * (i - 1) + k] = c * m1 - sn * m2;
+                M[3 * i + k] = sn * m1 + c * m2;
+            }
+        }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) Q[3 * r + c] = M[3 * c + r];
+    if (R[0] < (T)0) {
+        R[0] = -R[0];
+        R[1] = -R[1];
+        R[2] = -R[2];
+        R[8] = -R[8];
+        for (int r = 0; r < 3; r++) {
+            Q[3 * r] = -Q[3 * r];
+            Q[3 * r + 2] = -Q[3 * r + 2];
+        }
+    }
+    if (R[4] < (T)0) {
+        R[4] = -R[4];
+        R[5] = -R[5];
+        R[8] = -R[8];
+        for (int r = 0; r < 3; r++) {
+            Q[3 * r + 1] = -Q[3 * r + 1];
+            Q[3 * r + 2] = -Q[3 * r + 2];
+        }
+    }
+}
+
+// QR-stable Neo-Hookean with fibre stiffness (QRStableNeoHookean.h:102-173, QrBasedHelper.h:30-40): with
+// F = Q R, J = r00 r11 r22 and the energy
+//   psi = [g] lambda/2 (J-1)^2 + g (mu/2 (sum_{i<=j} r_ij^2 - 3) - mu (J-1)) + kx/2 (r00-1)^2
+//         + ky/2 (sqrt(r01^2 + r11^2) - 1)^2,
+// where the volume term is degraded only when J >= 1 and the fibre terms never, D = dpsi/dR (upper
+// triangular) and A = D R^T with its lower triangle mirrored from the upper, P = Q A R^{-T}. The Kirchhoff
+// stress P F^T (HyperelasticConstitutiveModel.h:75-80) is then Q A Q^T, evaluated here in that form (no
+// inverse of R). With effective = true the model is undegraded and isotropic (g = 1, kx = ky = 0), as
+// evaluateEffectiveCauchyStress uses it (QRStableNeoHookean.h:86-96). Returns J.
+template <class T>
+ZR_HD T tau_qrnh(const Material<T>& mt, const T* F, T g, T* tau, bool effective = false)
+{
+    T Q[9], R[9];
+    givens_qr3(F, Q, R);
+    const T J = R[0] * R[4] * R[8];
+    const T kx = effective ? (T)0 : mt.kx, ky = effective ? (T)0 : mt.ky;
+    if (effective) g = (T)1;
+    T D[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    const T lam = (J >= (T)1 ? g : (T)1) * mt.lambda * (J - (T)1) * J;
+    for (int i = 0; i < 3; i++) D[4 * i] += lam / R[4 * i];
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) D[3 * i + j] += g * mt.mu * R[3 * i + j];
+    for (int i = 0; i < 3; i++) D[4 * i] -= g * mt.mu * J / R[4 * i];
+    D[0] += kx * (R[0] - (T)1);
+    if (ky != (T)0) {
+        const T ss = sqrt(R[1] * R[1] + R[4] * R[4]);
+        D[1] += ky * (ss - (T)1) * R[1] / ss;
+        D[4] += ky * (ss - (T)1) * R[4] / ss;
+    }
+    T A[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) { // (D R^T)_ij = sum_k D_ik R_jk, D upper triangular
+            T acc = 0;
+            for (int k = j; k < 3; k++) acc += D[3 * i + k] * R[3 * j + k];
+            A[3 * i + j] = acc;
+            A[3 * j + i] = acc;
+        }
+    T QA[9];
+    mul3(Q, A, QA);
+    mul3_bt(QA, Q, tau);
+    return J;
+}
+
 // degradation g(d) = (1-d)^2 (1-k) + k (AnisoFractureSimulation.h:279-280)
 template <class T>
 ZR_HD T degradation(T d, T k)
@@ -441,9 +537,14 @@ template <class T>
 ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, T dt, bool& fallback)
 {
     T geo = d - mt.l0 * mt.l0 * lap;
-    T tau[9];
-    tau_nhb(mt, F, (T)1, tau);
-    T invJ = (T)1 / det3(F);
+    T tau[9], invJ;
+    if (mt.model == MODEL_QR_STABLE_NEOHOOKEAN) {
+        invJ = (T)1 / tau_qrnh(mt, F, (T)1, tau, true); // cauchy = P F^T / J with J from the QR (QRStableNeoHookean.h:86-96)
+    }
+    else {
+        tau_nhb(mt, F, (T)1, tau);
+        invJ = (T)1 / det3(F);
+    }
     T S[9], sp[9];
     for (int i = 0; i < 9; i++) S[i] = tau[i] * invJ; // undegraded Cauchy stress
     tension_part(S, sp); // sum of Macaulay-bracketed principal stresses times their projectors
