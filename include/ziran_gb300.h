@@ -118,6 +118,23 @@ int zr_scene_set_state(zr_scene* s, const void* in, int dtype);
 int zr_scene_reductions(zr_scene* s, double out[7]);
 int zr_scene_set_dt(zr_scene* s, double dt);
 double zr_scene_time(zr_scene* s);
+/* Snapshots (SimulationBase::write/read, SimulationBase.h:149-187, with MpmSimulationBase::writeState/readState,
+ * MpmSimulationBase.cpp:1060-1114): a versioned binary image of the dynamic state (header, then x v C F d m V0
+ * sigma_c in the caller's particle order and the scene's precision, so a restore is exact) with the clock and
+ * dt. zr_scene_state_bytes gives the image size; load_state needs a scene with the same precision and particle
+ * count (built the same way, as the reference re-runs its scene set-up before readState). */
+int64_t zr_scene_state_bytes(zr_scene* s);
+int zr_scene_save_state(zr_scene* s, void* buf, int64_t bytes);
+int zr_scene_load_state(zr_scene* s, const void* buf, int64_t bytes);
+int zr_scene_write_state_file(zr_scene* s, const char* path);
+int zr_scene_read_state_file(zr_scene* s, const char* path);
+/* Advance whole frames the way SimulationBase::simulate does (SimulationBase.h:275-354): substeps from
+ * TimeStepping::nextDt (TimeStepping.h:45-59) between min_dt and the scene's dt (max_dt), hitting every frame
+ * boundary exactly; with cfl_dt != 0 the wanted substep is cfl dx / max particle speed (calculateDt,
+ * MpmSimulationBase.cpp:1128-1151). A substep that moves a particle more than a cell restarts the frame from
+ * its start with max_dt halved (the autorestart of MpmSimulationBase.cpp:1480-1510); *restarts counts them.
+ * max_dt stays shrunk for later calls, as step.max_dt does. ZR_ERR_CFL if max_dt is already at min_dt. */
+int zr_scene_advance_frames(zr_scene* s, int frames, double frame_dt, double min_dt, int cfl_dt, int* restarts);
 int64_t zr_scene_count(zr_scene* s);
 const char* zr_scene_last_error(zr_scene* s);
 /* device time (ms) of the substeps of the last zr_scene_step call: CUDA events on the scene's stream */

@@ -173,6 +173,21 @@ public:
         return out;
     }
     double time() const { return zr_scene_time(h_); }
+
+    // SimulationBase::write / read (SimulationBase.h:149-187): the dynamic state to and from a file
+    void writeState(const std::string& path) { check(zr_scene_write_state_file(h_, path.c_str())); }
+    void readState(const std::string& path) { check(zr_scene_read_state_file(h_, path.c_str())); }
+
+    // SimulationBase::simulate with autorestart (SimulationBase.h:275-354, MpmSimulationBase.cpp:1480-1510):
+    // frames of frame_dt, substeps up to dt (shrunk by half and the frame redone after a CFL violation);
+    // returns the number of restarts
+    int simulate(int frames, double frame_dt, double min_dt = 1e-6, bool cfl_dt = false)
+    {
+        push_params();
+        int restarts = 0;
+        check(zr_scene_advance_frames(h_, frames, frame_dt, min_dt, cfl_dt ? 1 : 0, &restarts));
+        return restarts;
+    }
     int64_t particleCount() const { return zr_scene_count(h_); }
 
 private:

@@ -90,6 +90,12 @@ def load_library(build_if_needed=True):
         "zr_scene_set_timing": (i32, [vp, i32]),
         "zr_scene_get_timing": (i32, [vp, pd, P(i64)]),
         "zr_scene_set_autotune": (i32, [vp, i32]),
+        "zr_scene_state_bytes": (i64, [vp]),
+        "zr_scene_save_state": (i32, [vp, vp, i64]),
+        "zr_scene_load_state": (i32, [vp, vp, i64]),
+        "zr_scene_write_state_file": (i32, [vp, C.c_char_p]),
+        "zr_scene_read_state_file": (i32, [vp, C.c_char_p]),
+        "zr_scene_advance_frames": (i32, [vp, i32, d, d, i32, P(i32)]),
         "zr_scene_set_schedule": (i32, [vp, P(i32)]),
         "zr_scene_get_schedule": (i32, [vp, P(i32)]),
         "zr_scene_stats": (i32, [vp, P(i64), P(i64), P(i64)]),
@@ -329,6 +335,31 @@ class Scene:
     def set_autotune(self, mode):
         """0 fixed default schedule, 1 autotuned and cached per workload class, 2 re-measured per batch."""
         self._check(self.L.zr_scene_set_autotune(self.h, int(mode)))
+
+    def save_state(self):
+        """The scene's dynamic state as a binary image (bytes)."""
+        n = self.L.zr_scene_state_bytes(self.h)
+        if n < 0:
+            raise ZrError(ZR_ERR_STATE, "no particles")
+        buf = C.create_string_buffer(n)
+        self._check(self.L.zr_scene_save_state(self.h, buf, n))
+        return buf.raw
+
+    def load_state(self, image):
+        buf = C.create_string_buffer(bytes(image), len(image))
+        self._check(self.L.zr_scene_load_state(self.h, buf, len(image)))
+
+    def write_state(self, path):
+        self._check(self.L.zr_scene_write_state_file(self.h, os.fsencode(path)))
+
+    def read_state(self, path):
+        self._check(self.L.zr_scene_read_state_file(self.h, os.fsencode(path)))
+
+    def advance_frames(self, frames, frame_dt, min_dt=1e-6, cfl_dt=False):
+        """Whole frames with the reference's time stepping and CFL restarts; returns the number of restarts."""
+        r = C.c_int()
+        self._check(self.L.zr_scene_advance_frames(self.h, int(frames), float(frame_dt), float(min_dt), int(cfl_dt), C.byref(r)))
+        return r.value
 
     def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=0, g2p_tight=0):
         """chunk/buffers select the split P2G form's staging; fused=1 selects the one-kernel P2G, fused=2 the

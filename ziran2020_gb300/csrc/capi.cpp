@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -17,6 +18,8 @@
 using namespace zr;
 
 struct zr_scene {
+    // TimeStepping state of zr_scene_advance_frames (TimeStepping.h:17-31): max_dt shrinks on restarts
+    double max_dt = -1, max_dt_original = -1;
     int autotune = -1; // -1: the engine's default
     bool has_schedule = false;
     zr::Schedule schedule;
@@ -506,6 +509,206 @@ double zr_scene_time(zr_scene* s)
 }
 
 int64_t zr_scene_count(zr_scene* s) { return s ? s->desc.n : -1; }
+
+// ---------------------------------------------------------------------------------------------------
+// snapshots: SimulationBase::write/read + MpmSimulationBase::writeState/readState (SimulationBase.h:149-187,
+// MpmSimulationBase.cpp:1060-1114), as one versioned binary image of the dynamic state
+// ---------------------------------------------------------------------------------------------------
+namespace {
+struct StateHeader {
+    char magic[8]; // "ZRSTATE"
+    uint32_t version;
+    int32_t precision;
+    int64_t n;
+    double time, dt;
+    uint32_t fields, reserved;
+};
+static_assert(sizeof(StateHeader) == 48, "state header layout");
+const char kStateMagic[8] = { 'Z', 'R', 'S', 'T', 'A', 'T', 'E', 0 };
+// stored fields, in order, with their component counts: x v C F d m V0 sigma_c
+const int kStateFields[8] = { ZR_FIELD_X, ZR_FIELD_V, ZR_FIELD_C, ZR_FIELD_F, ZR_FIELD_D, ZR_FIELD_M, ZR_FIELD_V0, ZR_FIELD_SIGMA_C };
+const int kStateComps[8] = { 3, 3, 9, 9, 1, 1, 1, 1 };
+int64_t state_bytes(int precision, int64_t n) { return (int64_t)sizeof(StateHeader) + n * 28 * (precision == ZR_F64 ? 8 : 4); }
+} // namespace
+
+int64_t zr_scene_state_bytes(zr_scene* s)
+{
+    if (!s || s->desc.n <= 0) return -1;
+    return state_bytes(s->precision, s->desc.n);
+}
+
+int zr_scene_save_state(zr_scene* s, void* buf, int64_t bytes)
+{
+    NEED_ENGINE(s);
+    const int64_t n = s->desc.n, need = state_bytes(s->precision, n);
+    if (!buf || bytes < need) return set_err(s->err, ZR_ERR_ARG, "state buffer smaller than zr_scene_state_bytes");
+    StateHeader h;
+    std::memcpy(h.magic, kStateMagic, 8);
+    h.version = 1;
+    h.precision = s->precision;
+    h.n = n;
+    h.time = s->eng->time(0);
+    h.dt = s->eng->dt(0);
+    h.fields = 8;
+    h.reserved = 0;
+    std::memcpy(buf, &h, sizeof h);
+    char* p = (char*)buf + sizeof h;
+    const size_t es = s->precision == ZR_F64 ? 8 : 4;
+    for (int f = 0; f < 8; f++) {
+        // native precision: the image restores the state bit for bit
+        int rc = s->eng->get_field(0, kStateFields[f], p, s->precision == ZR_F32);
+        if (rc) {
+            s->err = s->eng->last_error();
+            return rc;
+        }
+        p += (size_t)n * kStateComps[f] * es;
+    }
+    return ZR_OK;
+}
+
+int zr_scene_load_state(zr_scene* s, const void* buf, int64_t bytes)
+{
+    NEED_ENGINE(s);
+    if (!buf || bytes < (int64_t)sizeof(StateHeader)) return set_err(s->err, ZR_ERR_ARG, "state image too short");
+    StateHeader h;
+    std::memcpy(&h, buf, sizeof h);
+    if (std::memcmp(h.magic, kStateMagic, 8) != 0) return set_err(s->err, ZR_ERR_ARG, "not a state image");
+    if (h.version != 1 || h.fields != 8) return set_err(s->err, ZR_ERR_ARG, "state image of an unknown version");
+    if (h.precision != s->precision) return set_err(s->err, ZR_ERR_ARG, "state image of the other precision");
+    if (h.n != s->desc.n) return set_err(s->err, ZR_ERR_ARG, "state image of a scene with a different particle count");
+    if (bytes < state_bytes(s->precision, h.n) || !(h.dt > 0) || !(h.time >= 0)) return set_err(s->err, ZR_ERR_ARG, "state image truncated or corrupt");
+    const char* p = (const char*)buf + sizeof h;
+    const size_t es = s->precision == ZR_F64 ? 8 : 4;
+    for (int f = 0; f < 8; f++) {
+        int rc = s->eng->set_field(0, kStateFields[f], p, s->precision == ZR_F32);
+        if (rc) {
+            s->err = s->eng->last_error();
+            return rc;
+        }
+        p += (size_t)h.n * kStateComps[f] * es;
+    }
+    int rc = s->eng->set_time(0, h.time);
+    if (!rc) rc = s->eng->set_dt(0, h.dt);
+    if (rc) s->err = s->eng->last_error();
+    s->desc.dt = h.dt;
+    return rc;
+}
+
+int zr_scene_write_state_file(zr_scene* s, const char* path)
+{
+    if (!s || !path) return ZR_ERR_ARG;
+    const int64_t nb = zr_scene_state_bytes(s);
+    if (nb < 0) return set_err(s->err, ZR_ERR_STATE, "no particles");
+    std::vector<char> buf((size_t)nb);
+    int rc = zr_scene_save_state(s, buf.data(), nb);
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return set_err(s->err, ZR_ERR_ARG, std::string("cannot open ") + path + " for writing");
+    const bool ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    const bool closed = std::fclose(f) == 0;
+    return ok && closed ? ZR_OK : set_err(s->err, ZR_ERR_ARG, std::string("short write to ") + path);
+}
+
+int zr_scene_read_state_file(zr_scene* s, const char* path)
+{
+    if (!s || !path) return ZR_ERR_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_err(s->err, ZR_ERR_ARG, std::string("cannot open ") + path);
+    std::vector<char> buf;
+    char tmp[1 << 16];
+    size_t got;
+    while ((got = std::fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
+    std::fclose(f);
+    return zr_scene_load_state(s, buf.data(), (int64_t)buf.size());
+}
+
+// ---------------------------------------------------------------------------------------------------
+// frames with the reference driver's time stepping and restarts (SimulationBase::simulate/advanceOneFrame,
+// SimulationBase.h:275-354; TimeStepping::nextDt, TimeStepping.h:45-59; calculateDt,
+// MpmSimulationBase.cpp:1128-1151; the autorestart of MpmSimulationBase.cpp:1480-1510)
+// ---------------------------------------------------------------------------------------------------
+int zr_scene_advance_frames(zr_scene* s, int frames, double frame_dt, double min_dt, int cfl_dt, int* restarts)
+{
+    if (restarts) *restarts = 0;
+    NEED_ENGINE(s);
+    if (frames < 0 || !(frame_dt > 0) || !(min_dt > 0)) return set_err(s->err, ZR_ERR_ARG, "need frames >= 0, frame_dt > 0, min_dt > 0");
+    if (s->max_dt_original <= 0) {
+        s->max_dt_original = s->eng->dt(0); // the scene's dt is the largest substep (step.max_dt)
+        s->max_dt = s->max_dt_original;
+    }
+    int nrestart = 0;
+    for (int f = 0; f < frames; f++) {
+        int rc = s->eng->checkpoint_save(); // the frame-start state a restart reads back
+        if (rc) {
+            s->err = s->eng->last_error();
+            return rc;
+        }
+        double since = 0;
+        bool restart = false;
+        while (since < frame_dt && !restart) {
+            double want = s->max_dt;
+            if (cfl_dt) { // cfl dx / max particle speed
+                double red[7];
+                rc = s->eng->reductions(0, red);
+                if (rc) {
+                    s->err = s->eng->last_error();
+                    return rc;
+                }
+                if (red[5] > 0) want = s->desc.cfl * s->desc.dx / red[5];
+            }
+            // TimeStepping::nextDt; without a CFL-derived dt, the equal substeps up to the frame's last two run as one launch
+            const double maxd = std::min(s->max_dt, s->max_dt_original);
+            double dt = want < min_dt ? min_dt : (want > maxd ? maxd : want);
+            int k = 1;
+            if (since + dt >= frame_dt)
+                dt = frame_dt - since;
+            else if (since + 2 * dt > frame_dt)
+                dt = (frame_dt - since) / 2;
+            else if (!cfl_dt) {
+                double t = since;
+                k = 0;
+                while (t + 2 * dt <= frame_dt && t + dt < frame_dt) {
+                    t += dt;
+                    k++;
+                }
+                k = std::max(k, 1);
+            }
+            if (s->eng->dt(0) != dt) {
+                rc = s->eng->set_dt(0, dt);
+                if (rc) {
+                    s->err = s->eng->last_error();
+                    return rc;
+                }
+            }
+            StepReport rep;
+            rc = s->eng->step(k, &rep);
+            s->last_ms = rep.device_ms;
+            s->fallbacks += rep.fallback;
+            if (rc == ZR_ERR_CFL) {
+                // a particle moved more than a cell: halve max_dt and redo the frame from its start
+                if (s->max_dt <= min_dt) return set_err(s->err, ZR_ERR_CFL, "unable to shrink dt further (max_dt at min_dt)");
+                s->max_dt = std::max(s->max_dt / 2, min_dt);
+                rc = s->eng->checkpoint_restore();
+                if (rc) {
+                    s->err = s->eng->last_error();
+                    return rc;
+                }
+                nrestart++;
+                restart = true;
+                break;
+            }
+            if (rc) {
+                s->err = s->eng->last_error();
+                return rc;
+            }
+            for (int q = 0; q < k; q++) since += dt; // TimeStepping::advance, one substep at a time
+        }
+        if (restart) f--;
+    }
+    if (restarts) *restarts = nrestart;
+    s->desc.dt = s->eng->dt(0);
+    return ZR_OK;
+}
 
 const char* zr_scene_last_error(zr_scene* s) { return s ? s->err.c_str() : "null scene"; }
 

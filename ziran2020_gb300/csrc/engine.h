@@ -99,7 +99,13 @@ public:
     // FP64-accumulated reductions: mass, momentum(3), kinetic energy, max speed, grid mass
     virtual int reductions(int scene, double* out7) = 0;
     virtual int set_dt(int scene, double dt) = 0;
+    virtual double dt(int scene) const = 0;
     virtual double time(int scene) const = 0;
+    virtual int set_time(int scene, double t) = 0;
+    // Device-side checkpoint of the whole batch (particle state, ids, scene clocks and dt): save, then restore
+    // to return to it (a re-formed batch invalidates it).
+    virtual int checkpoint_save() = 0;
+    virtual int checkpoint_restore() = 0;
     virtual int64_t count(int scene) const = 0;
     virtual int n_scenes() const = 0;
     // Binning products of the current substep input (for parity tests): sorted keys (scene bits

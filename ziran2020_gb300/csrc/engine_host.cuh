@@ -190,6 +190,7 @@ public:
         }
         tuned_ = false;
         sorted_storage_ = false;
+        ck_valid_ = false;
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * scene_cap_, stream_));
         ZR_CUDA(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), sizeof(SceneParams<T>) * h_scenes_.size(), cudaMemcpyHostToDevice, stream_));
@@ -408,6 +409,51 @@ public:
         return 0;
     }
 
+    double dt(int s) const override { return (s >= 0 && s < n_scenes()) ? (double)h_scenes_[s].dt : NAN; }
+
+    int set_time(int s, double t) override
+    {
+        if (s < 0 || s >= n_scenes() || !(t >= 0)) return arg("bad scene or time");
+        ZR_CUDA(cudaMemcpyAsync((char*)(d_scenes_ + s) + offsetof(SceneParams<T>, time), &t, 8, cudaMemcpyHostToDevice, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    int checkpoint_save() override
+    {
+        if (!N_) return fail(ZR_ERR_STATE_, "no scenes loaded");
+        const size_t pool_b = sizeof(T) * P_NF * (size_t)cap_, pid_b = 4 * (size_t)cap_, sc_b = sizeof(SceneParams<T>) * h_scenes_.size();
+        if (!ck_pool_ || ck_cap_ != cap_ || ck_scenes_n_ < h_scenes_.size()) {
+            dfree(ck_pool_);
+            dfree(ck_pid_);
+            dfree(ck_scenes_);
+            if (alloc(&ck_pool_, pool_b) || alloc(&ck_pid_, pid_b) || alloc(&ck_scenes_, sc_b)) return ZR_ERR_CUDA_;
+            ck_cap_ = cap_;
+            ck_scenes_n_ = h_scenes_.size();
+        }
+        ZR_CUDA(cudaMemcpyAsync(ck_pool_, pool_[cur_], pool_b, cudaMemcpyDeviceToDevice, stream_));
+        ZR_CUDA(cudaMemcpyAsync(ck_pid_, pid_[cur_], pid_b, cudaMemcpyDeviceToDevice, stream_));
+        ZR_CUDA(cudaMemcpyAsync(ck_scenes_, d_scenes_, sc_b, cudaMemcpyDeviceToDevice, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        ck_host_scenes_ = h_scenes_;
+        ck_valid_ = true;
+        return 0;
+    }
+
+    int checkpoint_restore() override
+    {
+        if (!ck_valid_ || ck_cap_ != cap_ || ck_host_scenes_.size() != h_scenes_.size()) return fail(ZR_ERR_STATE_, "no checkpoint of this batch");
+        const size_t pool_b = sizeof(T) * P_NF * (size_t)cap_, pid_b = 4 * (size_t)cap_, sc_b = sizeof(SceneParams<T>) * h_scenes_.size();
+        ZR_CUDA(cudaMemcpyAsync(pool_[cur_], ck_pool_, pool_b, cudaMemcpyDeviceToDevice, stream_));
+        ZR_CUDA(cudaMemcpyAsync(pid_[cur_], ck_pid_, pid_b, cudaMemcpyDeviceToDevice, stream_));
+        ZR_CUDA(cudaMemcpyAsync(d_scenes_, ck_scenes_, sc_b, cudaMemcpyDeviceToDevice, stream_));
+        h_scenes_ = ck_host_scenes_;
+        // a clean grid and the keys of the restored positions
+        ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
+        ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+        return rekey();
+    }
+
     double time(int s) const override
     {
         if (s < 0 || s >= n_scenes()) return NAN;
@@ -552,6 +598,11 @@ private:
     bool tuned_ = false;
     bool fixed_schedule_ = false;
     bool sorted_storage_ = false; // particles sit in the sorted order of their last substep (after one G2P)
+    void *ck_pool_ = nullptr, *ck_pid_ = nullptr, *ck_scenes_ = nullptr; // device checkpoint
+    uint64_t ck_cap_ = 0;
+    size_t ck_scenes_n_ = 0;
+    bool ck_valid_ = false;
+    std::vector<SceneParams<T>> ck_host_scenes_;
     void* scenes_backup_ = nullptr;
     size_t scenes_backup_bytes_ = 0;
     bool graphs_on_ = true, timing_ = false;
@@ -1191,7 +1242,7 @@ private:
     {
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
-            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_ };
+            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1212,6 +1263,10 @@ private:
         pstride_ = 0;
         scenes_backup_ = nullptr;
         scenes_backup_bytes_ = 0;
+        ck_pool_ = ck_pid_ = ck_scenes_ = nullptr;
+        ck_cap_ = 0;
+        ck_scenes_n_ = 0;
+        ck_valid_ = false;
         tuned_ = false;
         N_ = 0;
         cap_ = 0;
