@@ -105,10 +105,11 @@ public:
         KeyLayout kl;
         const int cb = bitlen((uint64_t)(max_domain + 2 * std::max(L::sx, std::max(L::sy, L::sz)) - 1));
         const uint32_t maxc = (1u << cb) - 1;
-        kl.ib = 0; // hot-path keys carry no particle index: k_cellfix orders each cell by original index
+        kl.ib = 0; // hot-path keys carry no particle index (binning() restores the reference's in-cell order)
         kl.cp = bitlen(L::offset(maxc, maxc, maxc)) - L::data_bits;
         kl.sb = bitlen((uint64_t)(np.size() - 1));
         kl.block_bits = L::block_bits;
+        kl.wide = kl.total() > 32;
         if (kl.total() > 64) return arg("batch too large for 64-bit keys: reduce the number of scenes or their domain");
         drop_graphs();
         // particle buffers: the free half of the current pair, or a larger pair
@@ -148,8 +149,11 @@ public:
                 return ZR_ERR_CUDA_;
             ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
             k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
-            size_t sb = 0, se = 0;
+            size_t sb = 0, sb32 = 0, se = 0;
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, cap, 0, 64, stream_));
+            ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb32, (uint32_t*)keys_in_, (uint32_t*)keys_sorted_, iota_, vals_sorted_, cap, 0, 32,
+                stream_));
+            sb = std::max(sb, sb32); // the key width follows the batch: room for either
             ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, (uint32_t*)nullptr, cap,
                 GroupHead{ keys_sorted_, kl }, stream_));
             sort_bytes_ = sb;
@@ -212,7 +216,7 @@ public:
         }
         // keys, and a first binning pass that sizes the grid (every group activates at most 8 blocks)
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
-        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, (int64_t)N_, 0, kl_.total(), stream_));
+        ZR_CUDA(sort_keys((int64_t)N_));
         ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)N_,
             GroupHead{ keys_sorted_, kl_ }, stream_));
         DevStatus hs;
@@ -470,8 +474,8 @@ public:
             ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
             StepArgs<T> a = args(cur_);
-            ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
-            k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[cur_], N_);
+            ZR_CUDA(sort_keys(n));
+            k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[cur_], N_, kl_);
             ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
             k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
             ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
@@ -485,7 +489,13 @@ public:
         const uint32_t G = hst_->n_groups, B = std::min(hst_->n_blocks, b_cap_);
         std::vector<uint64_t> sk(n), bk(B);
         std::vector<uint32_t> gs(G), vs(n), pd(n);
-        ZR_CUDA(cudaMemcpy(sk.data(), keys_sorted_, 8 * n, cudaMemcpyDeviceToHost));
+        if (kl_.wide)
+            ZR_CUDA(cudaMemcpy(sk.data(), keys_sorted_, 8 * n, cudaMemcpyDeviceToHost));
+        else {
+            std::vector<uint32_t> sk32(n);
+            ZR_CUDA(cudaMemcpy(sk32.data(), keys_sorted_, 4 * n, cudaMemcpyDeviceToHost));
+            for (int64_t i = 0; i < n; i++) sk[i] = sk32[i];
+        }
         ZR_CUDA(cudaMemcpy(vs.data(), vals_sorted_, 4 * n, cudaMemcpyDeviceToHost));
         ZR_CUDA(cudaMemcpy(pd.data(), pid_[cur_], 4 * n, cudaMemcpyDeviceToHost));
         ZR_CUDA(cudaMemcpy(gs.data(), g_start_, 4 * (size_t)G, cudaMemcpyDeviceToHost));
@@ -614,6 +624,16 @@ private:
     int64_t dev_bytes_ = 0;
 
     Pool<T> pool(int which) const { return Pool<T>{ pool_[which], pid_[which], (int64_t)cap_ }; }
+
+    // radix sort of the n keys in keys_in_ (32- or 64-bit words, as the key layout says) with their storage
+    // indices; stable, so particles of one cell keep their storage order
+    cudaError_t sort_keys(int64_t n)
+    {
+        if (kl_.wide)
+            return cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_);
+        return cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, (uint32_t*)keys_in_, (uint32_t*)keys_sorted_, iota_, vals_sorted_, n, 0,
+            kl_.total(), stream_);
+    }
 
     int params_from_desc(const SceneDesc& sdr, SceneParams<T>& sp)
     {
@@ -882,8 +902,7 @@ private:
         StepArgs<T> a = args(parity);
         const int64_t n = N_;
         if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
-        ZR_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_));
-        k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[parity], N_);
+        ZR_CUDA(sort_keys(n));
         ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());

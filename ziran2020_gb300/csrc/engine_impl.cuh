@@ -58,7 +58,16 @@ struct KeyLayout {
     int cp; // bits of (offset >> data_bits): page and in-block cell
     int sb; // bits of the scene slot
     int block_bits;
+    int wide; // keys are stored as 64-bit words; 0: as 32-bit words (total() <= 32), a third less sort traffic
     __host__ __device__ int total() const { return sb + cp + ib; }
+    __host__ __device__ uint64_t at(const uint64_t* k, uint32_t i) const { return wide ? k[i] : (uint64_t)reinterpret_cast<const uint32_t*>(k)[i]; }
+    __host__ __device__ void put(uint64_t* k, uint32_t i, uint64_t v) const
+    {
+        if (wide)
+            k[i] = v;
+        else
+            reinterpret_cast<uint32_t*>(k)[i] = (uint32_t)v;
+    }
     __host__ __device__ uint32_t scene(uint64_t k) const { return (uint32_t)(k >> (cp + ib)); }
     __host__ __device__ uint64_t page(uint64_t k) const { return (k >> (ib + block_bits)) & ((1ULL << (cp - block_bits)) - 1); }
     __host__ __device__ uint64_t group(uint64_t k) const { return k >> (ib + block_bits); }
@@ -166,25 +175,26 @@ __global__ void k_keys(Pool<T> p, const SceneParams<T>* scenes, int n_scenes, ui
             raise_flag(st, FLAG_OUT_OF_DOMAIN);
             b[0] = b[1] = b[2] = 0;
         }
-        keys[i] = ((uint64_t)lo << (kl.cp + kl.ib)) | ((L::offset(b[0], b[1], b[2]) >> L::data_bits) << kl.ib);
+        kl.put(keys, i, ((uint64_t)lo << (kl.cp + kl.ib)) | ((L::offset(b[0], b[1], b[2]) >> L::data_bits) << kl.ib));
     }
 }
 
 // The hot-path keys hold (scene, page, cell) only, so the radix sort needs 4 passes instead of 7; a
-// stable sort of storage-ordered input leaves the particles of one cell in their previous order. This pass
-// restores the reference's order inside each cell (ascending original index, the low bits of the
-// reference key, MpmSimulationBase.cpp:1547-1552) with an insertion sort per run of equal keys; runs are
-// short (~8) and nearly sorted (a cell keeps most of its particles from one substep to the next).
+// stable sort of storage-ordered input leaves the particles of one cell in their previous order, which is
+// deterministic and changes nothing in the substep but the order of floating-point sums. For the binning
+// products (zr_scene_binning) this pass restores the reference's order inside each cell (ascending original
+// index, the low bits of the reference key, MpmSimulationBase.cpp:1547-1552) with an insertion sort per run
+// of equal keys; runs are short (~8) and nearly sorted.
 template <class T>
-__global__ void k_cellfix(const uint64_t* ks, uint32_t* vals, const uint32_t* pid, uint32_t n)
+__global__ void k_cellfix(const uint64_t* ks, uint32_t* vals, const uint32_t* pid, uint32_t n, KeyLayout kl)
 {
     using L = typename LayoutOf<T>::type;
     const uint32_t mask = (1u << L::index_bits) - 1;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = ks[i];
-        if (i > 0 && ks[i - 1] == k) continue; // not the first of its run
+        const uint64_t k = kl.at(ks, i);
+        if (i > 0 && kl.at(ks, i - 1) == k) continue; // not the first of its run
         uint32_t e = i + 1;
-        while (e < n && ks[e] == k) e++;
+        while (e < n && kl.at(ks, e) == k) e++;
         for (uint32_t q = i + 1; q < e; q++) {
             const uint32_t v = vals[q], o = pid[v] & mask;
             uint32_t r = q;
@@ -203,7 +213,7 @@ __global__ void k_cellfix(const uint64_t* ks, uint32_t* vals, const uint32_t* pi
 struct GroupHead {
     const uint64_t* k;
     KeyLayout kl;
-    __device__ bool operator()(uint32_t i) const { return i == 0 || kl.group(k[i]) != kl.group(k[i - 1]); }
+    __device__ bool operator()(uint32_t i) const { return i == 0 || kl.group(kl.at(k, i)) != kl.group(kl.at(k, i - 1)); }
 };
 
 template <class T>
@@ -219,7 +229,7 @@ __global__ void k_activate(StepArgs<T> a)
     }
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
         uint32_t g = t >> 3, dl = t & 7;
-        uint64_t key0 = a.keys_sorted[a.g_start[g]];
+        uint64_t key0 = a.kl.at(a.keys_sorted, a.g_start[g]);
         uint64_t scene = a.kl.scene(key0);
         uint32_t bi, bj, bk;
         L::block_of_page(a.kl.page(key0), bi, bj, bk);
@@ -262,7 +272,7 @@ __global__ void k_nbr(StepArgs<T> a)
     if (G > a.b_cap) return; // activation already raised FLAG_CAPACITY
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
         const uint32_t g = t >> 3, dl = t & 7;
-        const uint64_t key0 = a.keys_sorted[a.g_start[g]];
+        const uint64_t key0 = a.kl.at(a.keys_sorted, a.g_start[g]);
         uint32_t bi, bj, bk;
         L::block_of_page(a.kl.page(key0), bi, bj, bk);
         const uint64_t scene = a.kl.scene(key0);
@@ -369,7 +379,7 @@ __global__ void __launch_bounds__(256) k_stress(StepArgs<T> a)
     const int64_t S = a.pstride;
     uint32_t flags = 0, fallbacks = 0;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
-        const uint64_t key = a.keys_sorted[q];
+        const uint64_t key = a.kl.at(a.keys_sorted, q);
         T* y = a.pay + pay_pos(q);
         int b[3];
         particle_payload<T, MODELS>(a.pin, a.vals_sorted[q], a.scenes[kl.scene(key)], y, S, b, fallbacks);
@@ -563,7 +573,7 @@ __device__ void scatter_producer(const StepArgs<T>& a, unsigned char* dyn, uint6
         if (g < G) {
             qs = a.g_start[g];
             qe = (g + 1 < G) ? a.g_start[g + 1] : a.n_total;
-            nf = a.scenes[a.kl.scene(a.keys_sorted[qs])].damage ? NACC : 4;
+            nf = a.scenes[a.kl.scene(a.kl.at(a.keys_sorted, qs))].damage ? NACC : 4;
 #pragma unroll
             for (int d = 0; d < 8; d++) {
                 nbr[d] = a.g_nbr[g * 8 + d];
@@ -779,7 +789,7 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
             s_nbr[tid] = slot;
             if (slot < 0 || (uint32_t)slot >= a.b_cap) s_bad = 1; // a failed lookup already raised FLAG_CAPACITY
             if (tid == 0) {
-                const uint64_t key0 = a.keys_sorted[start];
+                const uint64_t key0 = a.kl.at(a.keys_sorted, start);
                 uint32_t bi, bj, bk;
                 L::block_of_page(a.kl.page(key0), bi, bj, bk);
                 s_scene = (int)a.kl.scene(key0);
@@ -909,7 +919,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
         if (threadIdx.x < 8) {
             s_nbr[threadIdx.x] = a.g_nbr[g * 8 + threadIdx.x];
             if (threadIdx.x == 0) {
-                uint64_t key0 = a.keys_sorted[start];
+                uint64_t key0 = a.kl.at(a.keys_sorted, start);
                 uint32_t bi, bj, bk;
                 L::block_of_page(kl.page(key0), bi, bj, bk);
                 s_scene = (int)kl.scene(key0);
@@ -1078,7 +1088,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                     flags |= FLAG_OUT_OF_DOMAIN;
                     nb[0] = nb[1] = nb[2] = 0;
                 }
-                a.keys_next[i] = ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib);
+                kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
             }
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
