@@ -905,7 +905,10 @@ template <class T, int NT, int RESIDENT>
 __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    __shared__ __align__(16) T sv[8 * NVEL * L::nodes];
+    // the grid velocities around the group's block as one dense node tile (the block plus 2 nodes on the
+    // + side of every axis, the reach of the quadratic stencil): every stencil read is a fixed offset
+    constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
+    __shared__ T tv[NVEL * TN];
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
     if (aborted_cta(a.st)) return;
     const uint32_t G = a.st->n_groups;
@@ -929,16 +932,15 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             }
         }
         __syncthreads();
-        // stage the velocities of the 8 neighbouring blocks (1 KiB contiguous per block, 16-byte loads)
-        {
-            constexpr int V4 = NVEL * L::nodes * (int)sizeof(T) / 16; // 16-byte words per block
-            uint4* dst = reinterpret_cast<uint4*>(sv);
-            for (int q = threadIdx.x; q < 8 * V4; q += NT) {
-                const int d = q / V4, r = q % V4;
-                const int slot = s_nbr[d];
-                dst[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? reinterpret_cast<const uint4*>(a.vel + (size_t)slot * NVEL * L::nodes)[r]
-                                                                  : make_uint4(0, 0, 0, 0);
-            }
+        // stage the tile from the 8 neighbouring blocks
+        for (int q = threadIdx.x; q < NVEL * TN; q += NT) {
+            const int f = q / TN, node = q % TN;
+            const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
+            const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+            const int slot = s_nbr[ax * 4 + ay * 2 + az];
+            tv[q] = (slot >= 0 && (uint32_t)slot < a.b_cap)
+                ? a.vel[((size_t)slot * NVEL + f) * L::nodes + L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)]
+                : (T)0;
         }
         __syncthreads();
         const SceneParams<T>& sp = a.scenes[s_scene];
@@ -979,29 +981,27 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             //   pv = sum w v,  M_rc = sum w v_r delta_c,  G_rc = sum v_r (grad w)_c dx,
             // and the APIC moment sum w v (x_i - x_p)^T = dx (M - pv fr^T) because x_i - x_p = (delta - fr) dx.
             T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0;
+            const T* nv0 = tv + (l[0] * TY + l[1]) * TZ + l[2];
 #pragma unroll
             for (int ii = 0; ii < 3; ii++) {
-                const int tx = l[0] + ii, ax = tx >= L::sx, ex = tx - ax * L::sx;
                 T Si[3] = { 0, 0, 0 }, Ji[3] = { 0, 0, 0 }, Ki[3] = { 0, 0, 0 }, Ui[3] = { 0, 0, 0 }, Ti[3] = { 0, 0, 0 };
                 T lA = 0, lB = 0, lC = 0;
 #pragma unroll
                 for (int jj = 0; jj < 3; jj++) {
-                    const int ty = l[1] + jj, ay = ty >= L::sy, ey = ty - ay * L::sy;
                     T sj[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 }, pz = 0, p1 = 0;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
-                        const int tz = l[2] + kk, az = tz >= L::sz, ez = tz - az * L::sz;
-                        const T* nv = sv + (ax * 4 + ay * 2 + az) * NVEL * L::nodes + L::element(ex, ey, ez);
+                        const T* nv = nv0 + (ii * TY + jj) * TZ + kk;
                         const T wk = w[2][kk], dwk = dw[2][kk];
 #pragma unroll
                         for (int r = 0; r < 3; r++) {
-                            const T vr = nv[r * L::nodes];
+                            const T vr = nv[r * TN];
                             sj[r] += wk * vr;
                             tj[r] += dwk * vr;
                             if (kk) uj[r] += ((T)kk * wk) * vr;
                         }
                         if (damage) {
-                            const T pf = nv[3 * L::nodes];
+                            const T pf = nv[3 * TN];
                             pz += wk * pf;
                             p1 += pf;
                         }
