@@ -845,11 +845,13 @@ struct Scene {
     std::vector<Material<T>> materials;
     std::vector<HalfSpace<T>> objects;
     bool damage = false;
+    bool implicit = false; // AnisoFractureSimulation's implicit damage solve (--implicit_damage)
+    int cg_iterations = 0; // of the last solve
 
     int64_t n = 0;
     std::vector<std::array<T, 3>> x, v;
     std::vector<M3<T>> C, F, vtau, gradV;
-    std::vector<T> m, V0, d, sigc, lap, vol;
+    std::vector<T> m, V0, d, sigc, lap, vol, maxdt;
     std::vector<int32_t> mat;
 
     // binning products (MpmSimulationBase.cpp:1531-1573)
@@ -1075,16 +1077,34 @@ struct Scene {
         for (int64_t p = 0; p < n; p++) vol[p] = V0[p] * det(F[p]);
     }
 
+    bool damageable(int64_t p) const
+    {
+        // the reference damages only particles that carry a phase field and one of its damageable models
+        // (AnisoFractureSimulation.h:210-218,343-352)
+        const Material<T>& mt = materials[mat[p]];
+        return (mt.model == MODEL_NHB || mt.model == MODEL_QRNH) && mt.damage;
+    }
+
     // AnisoFractureSimulation.h:210-283, :365-391 (one director a0 = e1, one weight alpha)
     void update_damage()
     {
 #pragma omp parallel for schedule(static)
         for (int64_t p = 0; p < n; p++) {
+            if (!damageable(p)) continue;
             const Material<T>& mt = materials[mat[p]];
-            // the reference damages only particles that carry a phase field and one of its damageable models
-            // (AnisoFractureSimulation.h:210-218,343-352); NeoHookeanBorden is the one restated here
-            if ((mt.model != MODEL_NHB && mt.model != MODEL_QRNH) || !mt.damage) continue;
             T geo = d[p] - (mt.l0 * mt.l0 * lap[p]);
+            T dtilde = dtilde_of(p);
+            T diff = ((1 - d[p]) * dtilde) - geo;
+            T newd = d[p] + ((dt / mt.eta) * ((diff + std::abs(diff)) / 2));
+            d[p] = std::min(newd, (T)1);
+        }
+    }
+
+    // D-tilde = zeta <phi - 1> of one particle (AnisoFractureSimulation.h:224-270, updateDTildeHelper :292-333)
+    T dtilde_of(int64_t p) const
+    {
+        {
+            const Material<T>& mt = materials[mat[p]];
             T J;
             M3<T> tau;
             if (mt.model == MODEL_QRNH)
@@ -1114,10 +1134,185 @@ struct Scene {
             for (int a = 0; a < 9; a++) contraction += As.a[a] * sA.a[a];
             T phi = ((T)1 / (sigc[p] * sigc[p])) * contraction;
             T pm1 = phi - 1;
-            T dtilde = mt.zeta * ((pm1 + std::abs(pm1)) / 2);
-            T diff = ((1 - d[p]) * dtilde) - geo;
-            T newd = d[p] + ((dt / mt.eta) * ((diff + std::abs(diff)) / 2));
-            d[p] = std::min(newd, (T)1);
+            return mt.zeta * ((pm1 + std::abs(pm1)) / 2);
+        }
+    }
+
+    // damageP2G (AnisoFractureSimulation.h:393-435): normalised nodal phase field and vol = V0 det F
+    void damage_p2g()
+    {
+        colour_scatter([&](size_t g, const int o[3], int p) {
+            int b[3];
+            T w[3][3], dw[3][3];
+            weights(p, b, w, dw);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    for (int k = 0; k < 3; k++) {
+                        T wijk = w[0][i] * w[1][j] * w[2][k];
+                        Node<T>& nd = node_at(g, o, b, i, j, k);
+                        nd.pfm += wijk;
+                        nd.pf += d[p] * wijk;
+                    }
+        });
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < (int64_t)grid.size(); q++)
+            if (grid[q].m != 0) grid[q].pf /= grid[q].pfm;
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < n; p++) vol[p] = V0[p] * det(F[p]);
+    }
+
+    // solveDamageSystem (AnisoFractureSimulation.h:437-562) with ConjugateGradient::solve (ConjugateGradient.h,
+    // tolerance 1e-6, relative tolerance 1, at most 100 iterations, x0 = 0) and damageG2P (:564-626). Only
+    // particles of a damageable model take part, and the unknowns are the nodes they reach (the reference's
+    // nodes with mass, MpmGrid::getNumNodes, when every particle carries a phase field, as it assumes).
+    void solve_damage()
+    {
+        damage_p2g();
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < n; p++)
+            if (damageable(p)) maxdt[p] = std::max(dtilde_of(p), maxdt[p]); // updateDTilde (:334-338)
+        // the preconditioner's diagonal, sum_p vol (1 + dt/eta (D~ + 1)) w, per grid node; it selects the unknowns
+        std::vector<T> gdiag(grid.size(), 0);
+        colour_scatter([&](size_t g, const int o[3], int p) {
+            if (!damageable(p)) return;
+            const Material<T>& mt = materials[mat[p]];
+            int b[3];
+            T w[3][3], dw[3][3];
+            weights(p, b, w, dw);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    for (int k = 0; k < 3; k++)
+                        gdiag[&node_at(g, o, b, i, j, k) - grid.data()] += vol[p] * (1 + ((dt / mt.eta) * (maxdt[p] + 1))) * (w[0][i] * w[1][j] * w[2][k]);
+        });
+        std::vector<int64_t> id(grid.size(), -1);
+        int64_t nn = 0;
+        for (size_t q = 0; q < grid.size(); q++)
+            if (grid[q].m != 0 && gdiag[q] > 0) id[q] = nn++;
+        auto nid = [&](Node<T>& nd) { return id[&nd - grid.data()]; };
+        auto grad = [&](const T w[3][3], const T dw[3][3], int i, int j, int k, T gw[3]) {
+            T odx = 1 / dx;
+            gw[0] = odx * dw[0][i] * w[1][j] * w[2][k];
+            gw[1] = w[0][i] * odx * dw[1][j] * w[2][k];
+            gw[2] = w[0][i] * w[1][j] * odx * dw[2][k];
+        };
+        std::vector<T> xv(nn, 0), rhs(nn, 0), diag(nn, 0);
+        colour_scatter([&](size_t g, const int o[3], int p) {
+            if (!damageable(p)) return;
+            const Material<T>& mt = materials[mat[p]];
+            int b[3];
+            T w[3][3], dw[3][3];
+            weights(p, b, w, dw);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    for (int k = 0; k < 3; k++) {
+                        Node<T>& nd = node_at(g, o, b, i, j, k);
+                        int64_t q = nid(nd);
+                        if (q < 0) continue;
+                        T wijk = w[0][i] * w[1][j] * w[2][k];
+                        rhs[q] += (((dt * maxdt[p]) / mt.eta) + nd.pf) * vol[p] * wijk;
+                    }
+        });
+        for (size_t q = 0; q < grid.size(); q++)
+            if (id[q] >= 0) diag[id[q]] = gdiag[q];
+        std::vector<std::array<T, 3>> gradc(n);
+        auto multiply = [&](const std::vector<T>& xx, std::vector<T>& bb) {
+#pragma omp parallel for schedule(dynamic, 4)
+            for (int64_t g = 0; g < (int64_t)groups.size(); g++) {
+                int o[3];
+                group_origin(g, o);
+                for (int idx = groups[g].first; idx <= groups[g].second; idx++) {
+                    int p = order[idx];
+                    gradc[p] = { 0, 0, 0 };
+                    if (!damageable(p)) continue;
+                    const Material<T>& mt = materials[mat[p]];
+                    int b[3];
+                    T w[3][3], dw[3][3];
+                    weights(p, b, w, dw);
+                    for (int i = 0; i < 3; i++)
+                        for (int j = 0; j < 3; j++)
+                            for (int k = 0; k < 3; k++) {
+                                int64_t q = nid(node_at(g, o, b, i, j, k));
+                                if (q < 0) continue;
+                                T gw[3];
+                                grad(w, dw, i, j, k, gw);
+                                for (int a = 0; a < 3; a++) gradc[p][a] += xx[q] * gw[a];
+                            }
+                    for (int a = 0; a < 3; a++) gradc[p][a] *= vol[p] * (dt / mt.eta) * mt.l0 * mt.l0;
+                }
+            }
+            std::fill(bb.begin(), bb.end(), (T)0);
+            colour_scatter([&](size_t g, const int o[3], int p) {
+                if (!damageable(p)) return;
+                const Material<T>& mt = materials[mat[p]];
+                int b[3];
+                T w[3][3], dw[3][3];
+                weights(p, b, w, dw);
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < 3; k++) {
+                            int64_t q = nid(node_at(g, o, b, i, j, k));
+                            if (q < 0) continue;
+                            T wijk = w[0][i] * w[1][j] * w[2][k], gw[3];
+                            grad(w, dw, i, j, k, gw);
+                            bb[q] += vol[p] * (1 + ((dt / mt.eta) * (maxdt[p] + 1))) * wijk * xx[q];
+                            bb[q] += gradc[p][0] * gw[0] + gradc[p][1] * gw[1] + gradc[p][2] * gw[2];
+                        }
+            });
+        };
+        auto dotp = [&](const std::vector<T>& a, const std::vector<T>& c) {
+            T s = 0;
+            for (int64_t q = 0; q < nn; q++) s += a[q] * c[q];
+            return s;
+        };
+        std::vector<T> r(nn), qv(nn), pv(nn), tmp(nn);
+        multiply(xv, tmp);
+        for (int64_t q = 0; q < nn; q++) {
+            r[q] = rhs[q] - tmp[q];
+            qv[q] = r[q] / diag[q];
+        }
+        pv = qv;
+        T zTrk = dotp(r, qv), zTrk_last;
+        T res = std::sqrt(zTrk);
+        const T local_tol = std::min((T)1 * res, (T)1e-6);
+        int cnt = 0;
+        for (; cnt < 100; ++cnt) {
+            if (res <= local_tol) break;
+            multiply(pv, tmp);
+            T alpha = zTrk / dotp(tmp, pv);
+            for (int64_t q = 0; q < nn; q++) {
+                xv[q] += pv[q] * alpha;
+                r[q] -= tmp[q] * alpha;
+                qv[q] = r[q] / diag[q];
+            }
+            zTrk_last = zTrk;
+            zTrk = dotp(qv, r);
+            T beta = zTrk / zTrk_last;
+            for (int64_t q = 0; q < nn; q++) pv[q] = qv[q] + beta * pv[q];
+            res = std::sqrt(zTrk);
+        }
+        cg_iterations = cnt;
+        for (size_t q = 0; q < grid.size(); q++)
+            if (id[q] >= 0) grid[q].pf = xv[id[q]] - grid[q].pf; // the change of the nodal phase field
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int64_t g = 0; g < (int64_t)groups.size(); g++) {
+            int o[3];
+            group_origin(g, o);
+            for (int idx = groups[g].first; idx <= groups[g].second; idx++) {
+                int p = order[idx];
+                if (!damageable(p)) continue;
+                int b[3];
+                T w[3][3], dw[3][3];
+                weights(p, b, w, dw);
+                T pf = 0;
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < 3; k++) {
+                            Node<T>& nd = node_at(g, o, b, i, j, k);
+                            if (nid(nd) >= 0) pf += w[0][i] * w[1][j] * w[2][k] * nd.pf;
+                        }
+                T new_d = d[p] + pf;
+                d[p] = std::min(std::max(d[p], new_d), (T)1);
+            }
         }
     }
 
@@ -1234,7 +1429,9 @@ struct Scene {
         bin();
         stress();
         p2g();
-        if (damage) {
+        if (damage && implicit)
+            solve_damage();
+        else if (damage) {
             laplacians();
             update_damage();
         }
@@ -1259,6 +1456,7 @@ struct Scene {
         sigc.resize(n);
         lap.resize(n);
         vol.resize(n);
+        maxdt.assign(n, (T)0);
         mat.resize(n);
     }
 };
@@ -1405,6 +1603,22 @@ int orc_set_particles(void* hp, int64_t n, const double* x, const double* v, con
 
 // Runs nsteps substeps; returns the OR of the CFL flags (bit 0: a particle moved more than dx, the
 // reference's RestartException trigger; bit 1: more than cfl*dx/2).
+// damage by the implicit phase-field solve instead of the explicit update (AnisoFractureSimulation.h:129-141)
+void orc_set_implicit(void* hp, int on)
+{
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, { sc->implicit = on != 0; });
+}
+
+// CG iterations of the last implicit damage solve
+int orc_cg_iterations(void* hp)
+{
+    Handle* h = (Handle*)hp;
+    int it = 0;
+    DISPATCH(h, { it = sc->cg_iterations; });
+    return it;
+}
+
 int orc_step(void* hp, int nsteps)
 {
     Handle* h = (Handle*)hp;

@@ -35,6 +35,9 @@ def lib():
         L.orc_destroy.argtypes = [vp]
         L.orc_add_material.restype = i32
         L.orc_add_material.argtypes = [vp, i32, d, d, i32, d, d, d, d, d, d, d]
+        L.orc_set_implicit.argtypes = [vp, i32]
+        L.orc_cg_iterations.restype = i32
+        L.orc_cg_iterations.argtypes = [vp]
         L.orc_tau.restype = d
         L.orc_tau.argtypes = [i32, i32, d, d, d, d, d, i32, P(d), P(d)]
         L.orc_add_halfspace.argtypes = [vp, P(d), P(d), i32, d, P(d)]
@@ -89,6 +92,12 @@ class OracleScene:
 
     def add_material(self, model, E, nu, damage=False, alpha=0.0, l0=0.0, eta=1.0, zeta=1.0, residual=0.0, kx_scale=0.0, ky_scale=0.0):
         return self.L.orc_add_material(self.h, model, E, nu, int(damage), alpha, l0, eta, zeta, residual, kx_scale, ky_scale)
+
+    def set_implicit_damage(self, on=True):
+        self.L.orc_set_implicit(self.h, int(on))
+
+    def cg_iterations(self):
+        return self.L.orc_cg_iterations(self.h)
 
     def add_halfspace(self, origin, normal, type_, friction=0.0, velocity=(0.0, 0.0, 0.0)):
         o, n, v = (np.asarray(a, dtype=np.float64) for a in (origin, normal, velocity))
