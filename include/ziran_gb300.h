@@ -56,6 +56,8 @@ extern "C" {
 #define ZR_FIELD_M 5       /* 1, mass */
 #define ZR_FIELD_V0 6      /* 1, initial volume (element measure) */
 #define ZR_FIELD_SIGMA_C 7 /* 1, critical stress */
+#define ZR_FIELD_DTILDE_MAX 8 /* 1, largest damage drive so far: the implicit damage solve's history
+                               * (AnisoFractureSimulation.h:285-340, maxDTilde) */
 
 typedef struct zr_scene zr_scene;
 typedef struct zr_batch zr_batch;
@@ -94,6 +96,14 @@ int zr_scene_add_neohookean_borden(zr_scene* s, int64_t first, int64_t count, do
  * and setExtraFiberStiffness(1, fiber_y) (QRStableNeoHookean.h:98-107): fibre stiffness kx = fiber_x mu
  * along the material x axis (r00 of F = QR) and ky = fiber_y mu; 0 and 0 give the isotropic model. */
 int zr_scene_add_qr_stable_neohookean(zr_scene* s, int64_t first, int64_t count, double E, double nu, double fiber_x, double fiber_y);
+/* AnisoFractureSimulation's implicit damage (AnisoFractureSimulation.h:343-352 selects solveDamageSystem,
+ * :437-626, when implicit is set): after the grid update the nodal phase field is solved with
+ * Jacobi-preconditioned conjugate gradients (ConjugateGradient.h: tolerance 1e-6 on sqrt(r.z), at most 100
+ * iterations, x0 = 0) and G2P adds the interpolated change to the damage, which never decreases. on = 0
+ * restores the explicit update. Must be called before the first substep. */
+int zr_scene_set_implicit_damage(zr_scene* s, int on);
+/* Conjugate-gradient iterations of the last substep's implicit damage solve (0 without one). */
+int zr_scene_cg_iterations(zr_scene* s, int* iterations);
 /* MpmParticleHandleBase::addFBasedMpmForceWithAnisotropicPhaseField (MpmParticleHandleBase.cpp:175-222) for a
  * range that already has a Neo-Hookean (Borden) or QR-stable Neo-Hookean model: one structural director a0 = e1 with weight alpha
  * (fibre directions are encoded in the initial F, see zr_rotated_F), length scale l0, viscosity eta,
@@ -120,8 +130,8 @@ int zr_scene_set_dt(zr_scene* s, double dt);
 double zr_scene_time(zr_scene* s);
 /* Snapshots (SimulationBase::write/read, SimulationBase.h:149-187, with MpmSimulationBase::writeState/readState,
  * MpmSimulationBase.cpp:1060-1114): a versioned binary image of the dynamic state (header, then x v C F d m V0
- * sigma_c in the caller's particle order and the scene's precision, so a restore is exact) with the clock and
- * dt. zr_scene_state_bytes gives the image size; load_state needs a scene with the same precision and particle
+ * sigma_c and the damage drive history in the caller's particle order and the scene's precision, so a restore
+ * is exact) with the clock and dt. Images of version 1 (without the history) still load, with a zero history. zr_scene_state_bytes gives the image size; load_state needs a scene with the same precision and particle
  * count (built the same way, as the reference re-runs its scene set-up before readState). */
 int64_t zr_scene_state_bytes(zr_scene* s);
 int zr_scene_save_state(zr_scene* s, void* buf, int64_t bytes);
@@ -194,6 +204,8 @@ typedef struct zr_scene_recipe {
     int32_t domain_cells; /* 0 = round(1/dx) + 4 (the unit box) */
     int32_t model;        /* ANISO_SLAB: 0 or ZR_NEOHOOKEAN_BORDEN (default), or ZR_QR_STABLE_NEOHOOKEAN */
     double fiber_stiffness; /* ANISO_SLAB with ZR_QR_STABLE_NEOHOOKEAN: kx in units of mu (setExtraFiberStiffness(0, .)) */
+    int32_t implicit_damage; /* ANISO_SLAB: 1 = implicit damage solve (zr_scene_set_implicit_damage) */
+    int32_t reserved2;
 } zr_scene_recipe;
 
 /* Defaults: ELASTIC_BOX = unit box, dx 1/64, cube side 0.25 at (0.5,0.6,0.5), 8 ppc, corotated E=1e4

@@ -31,7 +31,7 @@ def test_snapshot_restores_exactly_and_replays(prec):
     s.step(5)
     t5, saved = s.time, state(s)
     image = s.save_state()
-    assert len(image) == 48 + len(d["m"]) * 28 * (8 if prec == zr.F64 else 4)
+    assert len(image) == 48 + len(d["m"]) * 29 * (8 if prec == zr.F64 else 4)  # x v C F d m V0 sigma_c, D~ history
     s.step(10)
     first = state(s)
     s.load_state(image)

@@ -21,7 +21,7 @@ ERROR_NAMES = {1: "ARG", 2: "CUDA", 3: "CFL", 4: "NONFINITE", 5: "OUT_OF_DOMAIN"
 F32, F64 = 4, 8
 COROTATED, NEOHOOKEAN_BORDEN, QR_STABLE_NEOHOOKEAN = 0, 1, 2
 STICKY, SLIP, SEPARATE = 1, 2, 3
-FIELD = {"x": (0, 3), "v": (1, 3), "C": (2, 9), "F": (3, 9), "d": (4, 1), "m": (5, 1), "V0": (6, 1), "sigma_c": (7, 1)}
+FIELD = {"x": (0, 3), "v": (1, 3), "C": (2, 9), "F": (3, 9), "d": (4, 1), "m": (5, 1), "V0": (6, 1), "sigma_c": (7, 1), "dtilde_max": (8, 1)}
 RECIPE_ELASTIC_BOX, RECIPE_ANISO_SLAB = 0, 1
 
 
@@ -42,7 +42,8 @@ class Recipe(C.Structure):
                 ("E", C.c_double), ("nu", C.c_double), ("rho", C.c_double), ("apic_rpic_ratio", C.c_double), ("ground_y", C.c_double),
                 ("kappa_vmf", C.c_double), ("alpha", C.c_double), ("l0", C.c_double), ("eta", C.c_double), ("zeta", C.c_double),
                 ("residual", C.c_double), ("sigma_c_mean", C.c_double), ("sigma_c_std", C.c_double), ("pull_speed", C.c_double),
-                ("grip_cells", C.c_double), ("domain_cells", C.c_int32), ("model", C.c_int32), ("fiber_stiffness", C.c_double)]
+                ("grip_cells", C.c_double), ("domain_cells", C.c_int32), ("model", C.c_int32), ("fiber_stiffness", C.c_double),
+                ("implicit_damage", C.c_int32), ("reserved2", C.c_int32)]
 
 
 _lib = None
@@ -80,6 +81,8 @@ def load_library(build_if_needed=True):
         "zr_scene_set_state": (i32, [vp, vp, i32]),
         "zr_scene_reductions": (i32, [vp, pd]),
         "zr_scene_set_dt": (i32, [vp, d]),
+        "zr_scene_set_implicit_damage": (i32, [vp, i32]),
+        "zr_scene_cg_iterations": (i32, [vp, P(i32)]),
         "zr_scene_time": (d, [vp]),
         "zr_scene_count": (i64, [vp]),
         "zr_scene_last_error": (C.c_char_p, [vp]),
@@ -293,6 +296,18 @@ class Scene:
 
     def set_dt(self, dt):
         self._check(self.L.zr_scene_set_dt(self.h, dt))
+
+    def set_implicit_damage(self, on=True):
+        """Solve the damage implicitly (AnisoFractureSimulation.h:437-626) instead of the explicit update;
+        before the first substep."""
+        self._check(self.L.zr_scene_set_implicit_damage(self.h, 1 if on else 0))
+
+    @property
+    def cg_iterations(self):
+        """Conjugate-gradient iterations of the last substep's implicit damage solve."""
+        it = C.c_int(0)
+        self._check(self.L.zr_scene_cg_iterations(self.h, C.byref(it)))
+        return it.value
 
     @property
     def last_step_ms(self):

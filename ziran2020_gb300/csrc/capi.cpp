@@ -491,6 +491,24 @@ int zr_scene_reductions(zr_scene* s, double out[7])
     return rc;
 }
 
+int zr_scene_set_implicit_damage(zr_scene* s, int on)
+{
+    if (!s) return ZR_ERR_ARG;
+    if (s->committed) return set_err(s->err, ZR_ERR_STATE, "the damage solve must be chosen before the first substep");
+    s->desc.implicit_damage = on ? 1 : 0;
+    return ZR_OK;
+}
+
+int zr_scene_cg_iterations(zr_scene* s, int* iterations)
+{
+    if (!s || !iterations) return ZR_ERR_ARG;
+    *iterations = 0;
+    if (!s->committed) return ZR_OK;
+    int rc = s->eng->cg_iterations(0, iterations);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
 int zr_scene_set_dt(zr_scene* s, double dt)
 {
     if (!s || !(dt > 0)) return ZR_ERR_ARG;
@@ -525,36 +543,45 @@ struct StateHeader {
 };
 static_assert(sizeof(StateHeader) == 48, "state header layout");
 const char kStateMagic[8] = { 'Z', 'R', 'S', 'T', 'A', 'T', 'E', 0 };
-// stored fields, in order, with their component counts: x v C F d m V0 sigma_c
-const int kStateFields[8] = { ZR_FIELD_X, ZR_FIELD_V, ZR_FIELD_C, ZR_FIELD_F, ZR_FIELD_D, ZR_FIELD_M, ZR_FIELD_V0, ZR_FIELD_SIGMA_C };
-const int kStateComps[8] = { 3, 3, 9, 9, 1, 1, 1, 1 };
-int64_t state_bytes(int precision, int64_t n) { return (int64_t)sizeof(StateHeader) + n * 28 * (precision == ZR_F64 ? 8 : 4); }
+// stored fields, in order, with their component counts: x v C F d m V0 sigma_c, and (version 2) the damage drive
+// history of the implicit damage solve
+const uint32_t kStateVersion = 2;
+const int kStateFields[9] = { ZR_FIELD_X, ZR_FIELD_V, ZR_FIELD_C, ZR_FIELD_F, ZR_FIELD_D, ZR_FIELD_M, ZR_FIELD_V0, ZR_FIELD_SIGMA_C, ZR_FIELD_DTILDE_MAX };
+const int kStateComps[9] = { 3, 3, 9, 9, 1, 1, 1, 1, 1 };
+int fields_of_version(uint32_t v) { return v == 1 ? 8 : (v == 2 ? 9 : -1); }
+int64_t state_bytes(int precision, int64_t n, int fields)
+{
+    int64_t vals = 0;
+    for (int f = 0; f < fields; f++) vals += kStateComps[f];
+    return (int64_t)sizeof(StateHeader) + n * vals * (precision == ZR_F64 ? 8 : 4);
+}
 } // namespace
 
 int64_t zr_scene_state_bytes(zr_scene* s)
 {
     if (!s || s->desc.n <= 0) return -1;
-    return state_bytes(s->precision, s->desc.n);
+    return state_bytes(s->precision, s->desc.n, fields_of_version(kStateVersion));
 }
 
 int zr_scene_save_state(zr_scene* s, void* buf, int64_t bytes)
 {
     NEED_ENGINE(s);
-    const int64_t n = s->desc.n, need = state_bytes(s->precision, n);
+    const int nf = fields_of_version(kStateVersion);
+    const int64_t n = s->desc.n, need = state_bytes(s->precision, n, nf);
     if (!buf || bytes < need) return set_err(s->err, ZR_ERR_ARG, "state buffer smaller than zr_scene_state_bytes");
     StateHeader h;
     std::memcpy(h.magic, kStateMagic, 8);
-    h.version = 1;
+    h.version = kStateVersion;
     h.precision = s->precision;
     h.n = n;
     h.time = s->eng->time(0);
     h.dt = s->eng->dt(0);
-    h.fields = 8;
+    h.fields = (uint32_t)nf;
     h.reserved = 0;
     std::memcpy(buf, &h, sizeof h);
     char* p = (char*)buf + sizeof h;
     const size_t es = s->precision == ZR_F64 ? 8 : 4;
-    for (int f = 0; f < 8; f++) {
+    for (int f = 0; f < nf; f++) {
         // native precision: the image restores the state bit for bit
         int rc = s->eng->get_field(0, kStateFields[f], p, s->precision == ZR_F32);
         if (rc) {
@@ -573,19 +600,28 @@ int zr_scene_load_state(zr_scene* s, const void* buf, int64_t bytes)
     StateHeader h;
     std::memcpy(&h, buf, sizeof h);
     if (std::memcmp(h.magic, kStateMagic, 8) != 0) return set_err(s->err, ZR_ERR_ARG, "not a state image");
-    if (h.version != 1 || h.fields != 8) return set_err(s->err, ZR_ERR_ARG, "state image of an unknown version");
+    const int nf = fields_of_version(h.version);
+    if (nf < 0 || h.fields != (uint32_t)nf) return set_err(s->err, ZR_ERR_ARG, "state image of an unknown version");
     if (h.precision != s->precision) return set_err(s->err, ZR_ERR_ARG, "state image of the other precision");
     if (h.n != s->desc.n) return set_err(s->err, ZR_ERR_ARG, "state image of a scene with a different particle count");
-    if (bytes < state_bytes(s->precision, h.n) || !(h.dt > 0) || !(h.time >= 0)) return set_err(s->err, ZR_ERR_ARG, "state image truncated or corrupt");
+    if (bytes < state_bytes(s->precision, h.n, nf) || !(h.dt > 0) || !(h.time >= 0)) return set_err(s->err, ZR_ERR_ARG, "state image truncated or corrupt");
     const char* p = (const char*)buf + sizeof h;
     const size_t es = s->precision == ZR_F64 ? 8 : 4;
-    for (int f = 0; f < 8; f++) {
+    for (int f = 0; f < nf; f++) {
         int rc = s->eng->set_field(0, kStateFields[f], p, s->precision == ZR_F32);
         if (rc) {
             s->err = s->eng->last_error();
             return rc;
         }
         p += (size_t)h.n * kStateComps[f] * es;
+    }
+    if (nf < 9) { // an image without the history: it restarts from zero
+        std::vector<char> zeros((size_t)h.n * es, 0);
+        int rc = s->eng->set_field(0, ZR_FIELD_DTILDE_MAX, zeros.data(), s->precision == ZR_F32);
+        if (rc) {
+            s->err = s->eng->last_error();
+            return rc;
+        }
     }
     int rc = s->eng->set_time(0, h.time);
     if (!rc) rc = s->eng->set_dt(0, h.dt);
@@ -869,6 +905,7 @@ static int desc_from_recipe(SceneDesc& d, const zr_scene_recipe* r, std::string&
         m.zeta = r->zeta;
         m.residual = r->residual;
         d.materials.push_back(m);
+        d.implicit_damage = r->implicit_damage ? 1 : 0;
         int64_t nc[3], lo[3];
         recipe_cells(r, nc, lo);
         const double x_lo = (double)lo[0] * r->dx, x_hi = (double)(lo[0] + nc[0]) * r->dx;

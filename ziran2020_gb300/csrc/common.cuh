@@ -130,7 +130,10 @@ struct DevStatus {
     uint32_t max_groups_seen;
     uint32_t check_code; // first failed internal check (0 = none)
     uint32_t check_count;
-    uint32_t pad[4];
+    uint32_t work_dmg; // work counters of the implicit damage solve's group kernels
+    uint32_t work_cg;
+    uint32_t cg_loops; // iterations of the damage solve's loop in this substep (any scene)
+    uint32_t pad;
 };
 
 constexpr int MAX_OBJECTS = 8;
@@ -170,6 +173,8 @@ struct SceneParams {
     int32_t n_objects;
     int32_t n_materials;
     int32_t damage;
+    int32_t implicit; // damage by the implicit phase-field solve (AnisoFractureSimulation.h:129-141)
+    int32_t pad_;
     Material<T> materials[MAX_MATERIALS];
     HalfSpaceObj<T> objects[MAX_OBJECTS];
 };

@@ -20,6 +20,7 @@ struct SceneDesc {
     double apic_rpic_ratio = 1.0; // 1 = APIC, 0 = RPIC (MpmSimulationBase.cpp:39-40)
     double cfl = 0.6;
     double time = 0;
+    int implicit_damage = 0; // solve the damage implicitly (AnisoFractureSimulation.h:437-626) instead of the explicit update
     int32_t domain_cells = 0; // base nodes must stay in [0, domain_cells); 0 = the full 4096^3 SPGrid range
     struct Mat {
         int model = 0; // 0 fixed corotated, 1 Neo-Hookean (Borden), 2 QR-stable Neo-Hookean
@@ -37,6 +38,7 @@ struct SceneDesc {
     std::vector<Obj> objects;
     int64_t n = 0;
     std::vector<double> x, v, C, F, m, V0, d, sigma_c; // C, F row-major 3x3 per particle
+    std::vector<double> dtilde_max; // implicit damage: the damage drive history max D~ (empty = 0)
     std::vector<uint8_t> material; // per particle material index (empty = all 0)
 };
 
@@ -49,6 +51,7 @@ enum Field : int {
     FIELD_M = 5, // 1 mass
     FIELD_V0 = 6, // 1 initial volume
     FIELD_SIGMA_C = 7, // 1 critical stress
+    FIELD_DTILDE_MAX = 8, // 1 largest damage drive so far (the implicit damage solve's history)
 };
 
 struct StepReport {
@@ -106,6 +109,8 @@ public:
     // to return to it (a re-formed batch invalidates it).
     virtual int checkpoint_save() = 0;
     virtual int checkpoint_restore() = 0;
+    // iterations of the last substep's implicit damage solve for a scene (0 when it solves nothing)
+    virtual int cg_iterations(int scene, int* out) = 0;
     virtual int64_t count(int scene) const = 0;
     virtual int n_scenes() const = 0;
     // Binning products of the current substep input (for parity tests): sorted keys (scene bits

@@ -176,10 +176,15 @@ public:
             dfree(p1);
             void* p2 = grid_mass_;
             dfree(p2);
+            void* p3 = cgs_;
+            dfree(p3);
             d_scenes_ = nullptr;
             grid_mass_ = nullptr;
+            cgs_ = nullptr;
             scene_cap_ = std::max<size_t>(np.size(), 2 * scene_cap_);
-            if (alloc((void**)&d_scenes_, sizeof(SceneParams<T>) * scene_cap_) || alloc((void**)&grid_mass_, 8 * scene_cap_)) return ZR_ERR_CUDA_;
+            if (alloc((void**)&d_scenes_, sizeof(SceneParams<T>) * scene_cap_) || alloc((void**)&grid_mass_, 8 * scene_cap_)
+                || alloc((void**)&cgs_, sizeof(CgScalars) * scene_cap_))
+                return ZR_ERR_CUDA_;
         }
         if (!st_ && alloc((void**)&st_, sizeof(DevStatus))) return ZR_ERR_CUDA_;
         h_scenes_ = np;
@@ -188,9 +193,11 @@ public:
         cur_ = dst;
         models_ = 0;
         any_damage_ = false;
+        implicit_ = false;
         for (auto& sp : h_scenes_) {
             for (int k = 0; k < sp.n_materials; k++) models_ |= 1 << sp.materials[k].model;
             any_damage_ = any_damage_ || sp.damage;
+            implicit_ = implicit_ || sp.implicit;
         }
         tuned_ = false;
         sorted_storage_ = false;
@@ -232,6 +239,8 @@ public:
         else {
             ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+            int rc = ensure_cg();
+            if (rc) return rc;
         }
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
@@ -297,6 +306,7 @@ public:
             // the aborted substep may have left partial grid sums, hash entries or next keys behind
             ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+            if (cg_) ZR_CUDA(cudaMemsetAsync(cg_, 0, sizeof(T) * CG_NF * (size_t)b_cap_ * L::nodes, stream_));
             ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
             k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
             ZR_CUDA(cudaStreamSynchronize(stream_));
@@ -441,6 +451,18 @@ public:
         ZR_CUDA(cudaStreamSynchronize(stream_));
         ck_host_scenes_ = h_scenes_;
         ck_valid_ = true;
+        return 0;
+    }
+
+    int cg_iterations(int s, int* out) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        *out = 0;
+        if (!h_scenes_[s].implicit || !cgs_) return 0;
+        CgScalars c;
+        ZR_CUDA(cudaMemcpyAsync(&c, cgs_ + s, sizeof c, cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        *out = c.iter;
         return 0;
     }
 
@@ -601,6 +623,12 @@ private:
     int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [register budget variant][model set]
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
+    bool implicit_ = false; // some scene solves its damage implicitly
+    T* cg_ = nullptr; // the damage solve's node vectors (CG_NF x b_cap_ blocks), allocated when implicit_
+    CgScalars* cgs_ = nullptr; // per scene (scene_cap_)
+    cudaStream_t side_ = nullptr; // captures the damage solve's loop body
+    cudaGraphExec_t cg_exec_ = nullptr; // the damage solve's loop alone, for substeps launched outside graphs
+    int occ_dmg_[2] = { 1, 1 };
     T* pay_ = nullptr;
     int64_t pstride_ = 0;
     Schedule sched_{ 0, VAR_CHUNK[0], VAR_NBUF[0], 2, 128, 0, 0 };
@@ -680,6 +708,8 @@ private:
             mt.residual = (T)m.residual;
             if (m.damage) sp.damage = 1;
         }
+        // the implicit solve replaces the explicit damage update (AnisoFractureSimulation.h:343-352 picks one)
+        sp.implicit = (sd->implicit_damage && sp.damage) ? 1 : 0;
         for (int k = 0; k < sp.n_objects; k++) {
             const auto& o = sd->objects[k];
             double nn = std::sqrt(o.normal[0] * o.normal[0] + o.normal[1] * o.normal[1] + o.normal[2] * o.normal[2]);
@@ -707,6 +737,7 @@ private:
         if (!sd.C.empty() && (int64_t)sd.C.size() != 9 * cnt) return arg("C must have 9n values");
         if (!sd.d.empty() && (int64_t)sd.d.size() != cnt) return arg("d must have n values");
         if (!sd.sigma_c.empty() && (int64_t)sd.sigma_c.size() != cnt) return arg("sigma_c must have n values");
+        if (!sd.dtilde_max.empty() && (int64_t)sd.dtilde_max.size() != cnt) return arg("dtilde_max must have n values");
         auto put = [&](int f0, int nc, const std::vector<double>& src, double dflt_diag, double dflt) -> int {
             buf.resize(cnt);
             for (int c = 0; c < nc; c++) {
@@ -718,7 +749,8 @@ private:
         };
         int rc;
         if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
-            || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1)))
+            || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1))
+            || (rc = put(P_MDT, 1, sd.dtilde_max, 0, 0)))
             return rc;
         const uint8_t* mp = nullptr;
         if (!sd.material.empty()) {
@@ -746,11 +778,16 @@ private:
             init_err_ = fail(ZR_ERR_CUDA_, "no CUDA device");
             return;
         }
-        if (cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking) != cudaSuccess || cudaMallocHost((void**)&hst_, sizeof(DevStatus)) != cudaSuccess
+        if (cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking) != cudaSuccess || cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess
+            || cudaMallocHost((void**)&hst_, sizeof(DevStatus)) != cudaSuccess
             || cudaEventCreate(&t0_) != cudaSuccess || cudaEventCreate(&t1_) != cudaSuccess) {
             init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
             return;
         }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[0], k_dmg_group<T, 0>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[1], k_dmg_group<T, 1>, 128, 0);
+        occ_dmg_[0] = std::max(1, occ_dmg_[0]);
+        occ_dmg_[1] = std::max(1, occ_dmg_[1]);
         scatter_setup<0>();
         scatter_setup<1>();
         scatter_setup<2>();
@@ -815,6 +852,9 @@ private:
         dfree(p);
         p = h_vals_;
         dfree(p);
+        p = cg_;
+        dfree(p);
+        cg_ = nullptr;
         g_nbr_ = nullptr;
         b_key_ = nullptr;
         acc_ = vel_ = nullptr;
@@ -830,7 +870,7 @@ private:
         ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)cap * NACC * L::nodes, stream_));
         ZR_CUDA(cudaMemsetAsync(vel_, 0, sizeof(T) * (size_t)cap * NVEL * L::nodes, stream_));
         ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)hs, stream_));
-        return 0;
+        return ensure_cg();
     }
 
     int ensure_stage(size_t bytes)
@@ -864,6 +904,7 @@ private:
         case FIELD_M: f0 = P_M; nc = 1; return true;
         case FIELD_V0: f0 = P_V0; nc = 1; return true;
         case FIELD_SIGMA_C: f0 = P_SC; nc = 1; return true;
+        case FIELD_DTILDE_MAX: f0 = P_MDT; nc = 1; return true;
         }
         return false;
     }
@@ -880,6 +921,8 @@ private:
         a.g_nbr = g_nbr_;
         a.pay = pay_;
         a.pstride = pstride_;
+        a.cg = cg_;
+        a.cgs = cgs_;
         a.b_key = b_key_;
         a.acc = acc_;
         a.vel = vel_;
@@ -938,6 +981,10 @@ private:
         }
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
         k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
+        if (implicit_) {
+            int rc = enqueue_damage_solve(a);
+            if (rc) return rc;
+        }
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));
         const int gi = std::max(0, g2p_index(sched_.g2p_threads));
         if (sched_.g2p_tight)
@@ -947,6 +994,84 @@ private:
         k_step_end<T><<<1, 256, 0, stream_>>>(d_scenes_, n_scenes(), st_);
         if (ev) ZR_CUDA(cudaEventRecord(ev[5], stream_));
         ZR_CUDA(cudaGetLastError());
+        return 0;
+    }
+
+    // Implicit damage solve of the substep (AnisoFractureSimulation.h:437-626): D~ history and coefficients,
+    // right-hand side and preconditioner sums, CG initialisation, the iterations, the nodal change for G2P.
+    int enqueue_damage_solve(const StepArgs<T>& a)
+    {
+        ZR_CUDA(cudaMemsetAsync(cgs_, 0, sizeof(CgScalars) * h_scenes_.size(), stream_));
+        k_dmg_prep<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+        k_dmg_group<T, 0><<<nsm_ * occ_dmg_[0], 128, 0, stream_>>>(a);
+        k_cg_nodes<T, 0><<<nsm_ * 8, 256, 0, stream_>>>(a);
+        k_cg_scalars<T, 0><<<1, 256, 0, stream_>>>(a, n_scenes(), cudaGraphConditionalHandle{});
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        ZR_CUDA(cudaStreamIsCapturing(stream_, &cs));
+        if (cs == cudaStreamCaptureStatusActive) {
+            int rc = capture_cg_loop(a);
+            if (rc) return rc;
+        }
+        else {
+            if (!cg_exec_) {
+                cudaGraph_t g;
+                ZR_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                int rc = capture_cg_loop(a);
+                cudaError_t e = cudaStreamEndCapture(stream_, &g);
+                if (rc) return rc;
+                if (e != cudaSuccess) return fail(ZR_ERR_CUDA_, std::string("damage solve capture: ") + cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&cg_exec_, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return fail(ZR_ERR_CUDA_, std::string("damage solve instantiate: ") + cudaGetErrorString(e));
+            }
+            ZR_CUDA(cudaGraphLaunch(cg_exec_, stream_));
+        }
+        k_cg_nodes<T, 4><<<nsm_ * 8, 256, 0, stream_>>>(a);
+        return 0;
+    }
+
+    // Append the CG iterations to the capture under way on stream_: a conditional WHILE node whose body (one
+    // iteration) is captured on the side stream; the body's last kernel sets the condition and ends the loop
+    // after at most CG_MAX_ITERATIONS + 1 passes.
+    int capture_cg_loop(const StepArgs<T>& a)
+    {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g;
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* edges = nullptr;
+        size_t nd = 0;
+        ZR_CUDA(cudaStreamGetCaptureInfo(stream_, &cs, nullptr, &g, &deps, &edges, &nd));
+        cudaGraphConditionalHandle h;
+        ZR_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {}; // reserved fields zero
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        ZR_CUDA(cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        ZR_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        ZR_CUDA(cudaStreamBeginCaptureToGraph(side_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        k_dmg_group<T, 1><<<nsm_ * occ_dmg_[1], 128, 0, side_>>>(a);
+        k_cg_nodes<T, 1><<<nsm_ * 8, 256, 0, side_>>>(a);
+        k_cg_nodes<T, 2><<<nsm_ * 8, 256, 0, side_>>>(a);
+        k_cg_nodes<T, 3><<<nsm_ * 8, 256, 0, side_>>>(a);
+        k_cg_scalars<T, 1><<<1, 256, 0, side_>>>(a, n_scenes(), h);
+        cudaGraph_t out = nullptr;
+        const cudaError_t le = cudaGetLastError();
+        ZR_CUDA(cudaStreamEndCapture(side_, &out));
+        ZR_CUDA(le);
+        return 0;
+    }
+
+    // the damage solve's vectors and scalars (the vectors follow the grid's block capacity)
+    int ensure_cg()
+    {
+        if (!implicit_ || cg_) return 0;
+        const size_t bytes = sizeof(T) * CG_NF * (size_t)b_cap_ * L::nodes;
+        if (alloc((void**)&cg_, bytes)) return ZR_ERR_CUDA_;
+        ZR_CUDA(cudaMemsetAsync(cg_, 0, bytes, stream_));
         return 0;
     }
 
@@ -979,6 +1104,8 @@ private:
 
     void drop_graphs()
     {
+        if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+        cg_exec_ = nullptr;
         for (int p = 0; p < 2; p++) {
             if (g1_[p]) cudaGraphExecDestroy(g1_[p]);
             if (gk_[p]) cudaGraphExecDestroy(gk_[p]);
@@ -1137,6 +1264,7 @@ private:
         if (aborted_out) {
             ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
             ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+            if (cg_) ZR_CUDA(cudaMemsetAsync(cg_, 0, sizeof(T) * CG_NF * (size_t)b_cap_ * L::nodes, stream_));
         }
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
@@ -1261,7 +1389,7 @@ private:
     {
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
-            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_ };
+            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1280,6 +1408,9 @@ private:
         stage_bytes_ = 0;
         pay_ = nullptr;
         pstride_ = 0;
+        cg_ = nullptr;
+        cgs_ = nullptr;
+        implicit_ = false;
         scenes_backup_ = nullptr;
         scenes_backup_bytes_ = 0;
         ck_pool_ = ck_pid_ = ck_scenes_ = nullptr;
@@ -1307,6 +1438,8 @@ private:
         hst_ = nullptr;
         if (stream_) cudaStreamDestroy(stream_);
         stream_ = nullptr;
+        if (side_) cudaStreamDestroy(side_);
+        side_ = nullptr;
     }
 };
 

@@ -44,7 +44,7 @@ constexpr uint64_t HASH_EMPTY = ~0ULL;
 constexpr int HASH_PROBES = 64;
 
 // particle pool: field k of storage slot i at f[k * stride + i]
-enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_NF = 28 };
+enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_MDT = 28, P_NF = 29 };
 
 template <class T>
 struct Pool {
@@ -74,6 +74,16 @@ struct KeyLayout {
     __host__ __device__ uint32_t orig(uint64_t k) const { return (uint32_t)(k & ((1ULL << ib) - 1)); }
 };
 
+// per-scene state of the implicit damage solve's conjugate gradients (ConjugateGradient.h), kept on the device
+struct CgScalars {
+    double zr; // r . z
+    double zr_new;
+    double pAp; // p . A p
+    double tol; // min(|r0|_z, 1e-6)
+    int32_t iter, done;
+    int32_t pad0, pad1;
+};
+
 template <class T>
 struct StepArgs {
     const uint64_t* keys_sorted;
@@ -82,8 +92,10 @@ struct StepArgs {
     Pool<T> pin, pout;
     const uint32_t* g_start;
     int32_t* g_nbr;
-    T* pay; // P2G payload, NPAY fields of pstride elements
+    T* pay; // P2G payload, NPAY fields of pstride elements (also the implicit damage solve's particle scratch)
     int64_t pstride;
+    T* cg; // implicit damage solve: CG_NF node vectors of b_cap * nodes
+    CgScalars* cgs; // per scene
     uint64_t* b_key;
     T* acc;
     T* vel;
@@ -980,7 +992,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             // Separable gather: the stencil weight is wx_i wy_j wz_k, so sums over k, then j, then i give
             //   pv = sum w v,  M_rc = sum w v_r delta_c,  G_rc = sum v_r (grad w)_c dx,
             // and the APIC moment sum w v (x_i - x_p)^T = dx (M - pv fr^T) because x_i - x_p = (delta - fr) dx.
-            T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0;
+            T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0, pw = 0;
             const T* nv0 = tv + (l[0] * TY + l[1]) * TZ + l[2];
 #pragma unroll
             for (int ii = 0; ii < 3; ii++) {
@@ -1034,7 +1046,10 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                 }
                 // the reference's 3D Laplacian weights every term with d2w(i) = (1,-2,1)(i) (MpmGrid.h:607-613):
                 // sum_jk pf * d2w_i (wy_j wz_k + wx_i wz_k + wx_i wy_j)
-                if (damage) lap += (ii == 1 ? (T)-2 : (T)1) * (lA + wi * (lB + lC));
+                if (damage) {
+                    lap += (ii == 1 ? (T)-2 : (T)1) * (lA + wi * (lB + lC));
+                    pw += wi * lA; // sum w times the node field (the damage change of an implicit solve)
+                }
             }
             lap *= inv_dx * inv_dx;
             T Bm[9];
@@ -1093,14 +1108,24 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
             Q.pid[i] = pid;
+            Q.f[P_MDT * Q.stride + i] = P.f[P_MDT * P.stride + j]; // the implicit damage solve's history travels with the particle
             if (damage) {
                 // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
                 const uint32_t mat = pid >> L::index_bits;
                 const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
                 if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
-                    bool fb = false;
-                    dd = damage_update(mt, F, dd, lap, sc, dt, fb);
-                    if (fb) atomicAdd(&a.st->fallback, 1u);
+                    if (sp.implicit) {
+                        // damageG2P (AnisoFractureSimulation.h:578-610): the grid holds the solve's change of the
+                        // nodal phase field; damage never decreases and stays <= 1
+                        const T nd = dd + pw;
+                        dd = nd > dd ? nd : dd;
+                        dd = dd < (T)1 ? dd : (T)1;
+                    }
+                    else {
+                        bool fb = false;
+                        dd = damage_update(mt, F, dd, lap, sc, dt, fb);
+                        if (fb) atomicAdd(&a.st->fallback, 1u);
+                    }
                     if (!isfinite(dd)) flags |= FLAG_NONFINITE;
                 }
                 Q.f[P_D * Q.stride + i] = dd;
@@ -1109,6 +1134,331 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
         }
         if (flags) raise_flag(a.st, flags);
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Implicit damage solve (AnisoFractureSimulation::solveDamageSystem, AnisoFractureSimulation.h:437-626), run
+// between the grid update and G2P for scenes that ask for it. Unknowns: the nodal phase field x on the nodes
+// that damageable particles reach. With per-particle vol = V0 det F, the damage drive history
+// D~ = max(D~, zeta <phi - 1>) (updateDTilde, :285-340), c_p = vol (1 + dt/eta (D~ + 1)) and
+// e_p = vol dt/eta l0^2:
+//   rhs_i = sum_p (dt D~/eta + pf_i) vol w_ip          (pf: the normalised nodal damage of this substep)
+//   (A x)_i = diag_i x_i + sum_p (e_p sum_j x_j grad w_jp) . grad w_ip,   diag_i = sum_p c_p w_ip
+// solved by Jacobi-preconditioned conjugate gradients from x = 0 as ConjugateGradient::solve does (stop when
+// sqrt(r.z) <= min(sqrt(r0.z0), 1e-6), at most 100 iterations). Dot products are per scene, so every scene of a
+// batch runs the iterations it would run alone. G2P then adds sum_i w_ip (x_i - pf_i) to the damage.
+// ---------------------------------------------------------------------------------------------------
+enum { CG_SA = 0, CG_SV, CG_DIAG, CG_X, CG_R, CG_Z, CG_P, CG_AP, CG_NF }; // node vectors
+enum { DS_F = 0, DS_A = 3, DS_VOL = 4, DS_C = 5, DS_E = 6 }; // particle scratch fields in the payload buffer
+constexpr int CG_MAX_ITERATIONS = 100;
+
+template <class T>
+__device__ __forceinline__ T* cgv(const StepArgs<T>& a, int f, uint32_t slot) { return a.cg + ((size_t)f * a.b_cap + slot) * LayoutOf<T>::type::nodes; }
+
+// per sorted particle: D~ history, vol, the solve's coefficients and the fractional position
+template <class T>
+__global__ void k_dmg_prep(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const KeyLayout kl = a.kl;
+    const int64_t S = a.pstride;
+    const Pool<T>& P = a.pin;
+    uint32_t fallbacks = 0;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
+        const SceneParams<T>& sp = a.scenes[kl.scene(kl.at(a.keys_sorted, q))];
+        if (!sp.implicit) continue;
+        const uint32_t j = a.vals_sorted[q];
+        T* y = a.pay + pay_pos(q);
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+            const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
+            y[(DS_F + e) * S] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
+        }
+        const uint32_t mat = P.pid[j] >> L::index_bits;
+        const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+        T av = 0, vol = 0, c = 0, ev = 0;
+        if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
+            T F[9];
+#pragma unroll
+            for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
+            vol = P.f[P_V0 * P.stride + j] * det3(F);
+            bool fb = false;
+            const T drive = damage_drive(mt, F, P.f[P_SC * P.stride + j], fb);
+            if (fb) fallbacks++;
+            T hist = P.f[P_MDT * P.stride + j];
+            hist = drive > hist ? drive : hist;
+            P.f[P_MDT * P.stride + j] = hist;
+            const T dt = sp.dt;
+            av = ((dt * hist) / mt.eta) * vol;
+            c = vol * ((T)1 + ((dt / mt.eta) * (hist + (T)1)));
+            ev = vol * (dt / mt.eta) * mt.l0 * mt.l0;
+        }
+        y[DS_A * S] = av;
+        y[DS_VOL * S] = vol;
+        y[DS_C * S] = c;
+        y[DS_E * S] = ev;
+    }
+    if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
+}
+
+// quadratic B-spline weights and derivatives (per unit cell) of the three nodes from a fractional position
+template <class T>
+__device__ __forceinline__ void weights_of(const T* y, int64_t S, T (&w)[3][3], T (&dw)[3][3])
+{
+#pragma unroll
+    for (int e = 0; e < 3; e++) bspline_w(y[(DS_F + e) * S], 0, w[e], dw[e]);
+}
+
+// node tile of a group (its block plus 2 nodes on the + side): index of node (lx, ly, lz)
+template <class L>
+__device__ __forceinline__ int tile_index(int lx, int ly, int lz) { return (lx * (L::sy + 2) + ly) * (L::sz + 2) + lz; }
+
+// tile -> the node vectors of the 8 neighbouring blocks (atomics), then cleared; nf fields, vector f0 + f
+template <class T, class L>
+__device__ void flush_tile_cg(const StepArgs<T>& a, T* tile, const int32_t* nbr, int nf, const int* f_of, int tid, int nthreads)
+{
+    constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
+    for (int q = tid; q < nf * TN; q += nthreads) {
+        const int f = q / TN, node = q % TN;
+        const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
+        const T v = tile[q];
+        if (v == (T)0) continue;
+        tile[q] = (T)0;
+        const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+        const int slot = nbr[ax * 4 + ay * 2 + az];
+        if (slot < 0 || (uint32_t)slot >= a.b_cap) {
+            check_failed(a.st, 7);
+            continue;
+        }
+        atomicAdd(cgv(a, f_of[f], slot) + L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz), v);
+    }
+}
+
+// MODE 0: scatter vol D~ dt/eta, vol and c_p with the weights (right-hand side parts, diagonal);
+// MODE 1: the operator's particle part, sum_p (e_p sum_j p_j grad w_jp) . grad w_ip, into A p
+template <class T, int MODE>
+__global__ void __launch_bounds__(128) k_dmg_group(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    constexpr int NT = 128, TN = (L::sx + 2) * (L::sy + 2) * (L::sz + 2), NF = MODE == 0 ? 3 : 1;
+    constexpr int TY = L::sy + 2, TZ = L::sz + 2;
+    __shared__ T tile[NF * TN];
+    __shared__ T ptile[MODE == 1 ? TN : 1];
+    __shared__ int s_g, s_skip;
+    __shared__ int32_t s_nbr[8];
+    if (aborted_cta(a.st)) return;
+    const uint32_t G = a.st->n_groups;
+    const KeyLayout kl = a.kl;
+    const int64_t S = a.pstride;
+    for (int q = threadIdx.x; q < NF * TN; q += NT) tile[q] = (T)0;
+    uint32_t* counter = MODE == 0 ? &a.st->work_dmg : &a.st->work_cg;
+    for (;;) {
+        if (threadIdx.x == 0) s_g = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int g = s_g;
+        if (g >= (int)G) break;
+        const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
+        if (threadIdx.x < 8) s_nbr[threadIdx.x] = a.g_nbr[g * 8 + threadIdx.x];
+        if (threadIdx.x == 0) {
+            const uint32_t sc = kl.scene(kl.at(a.keys_sorted, start));
+            s_skip = !a.scenes[sc].implicit || (MODE == 1 && a.cgs[sc].done);
+        }
+        __syncthreads();
+        if (s_skip) {
+            __syncthreads();
+            continue;
+        }
+        if (MODE == 1) { // stage p on the tile
+            for (int q = threadIdx.x; q < TN; q += NT) {
+                const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
+                const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+                const int slot = s_nbr[ax * 4 + ay * 2 + az];
+                ptile[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? cgv(a, CG_P, slot)[L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)] : (T)0;
+            }
+            __syncthreads();
+        }
+        const T inv_dx = a.scenes[kl.scene(kl.at(a.keys_sorted, start))].inv_dx;
+        for (uint32_t q = start + threadIdx.x; q < end; q += NT) {
+            const T* y = a.pay + pay_pos(q);
+            const T c = y[DS_C * S];
+            if (c == (T)0) continue; // not damageable
+            const int e = (int)((kl.at(a.keys_sorted, q) >> kl.ib) & (L::nodes - 1));
+            const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
+            const int base = tile_index<L>(lx, ly, lz);
+            T w[3][3], dw[3][3];
+            weights_of(y, S, w, dw);
+            if (MODE == 0) {
+                const T av = y[DS_A * S], vol = y[DS_VOL * S];
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            const T wijk = w[0][i] * w[1][j] * w[2][k];
+                            T* t = tile + base + (i * TY + j) * TZ + k;
+                            atomicAdd(t, wijk * av);
+                            atomicAdd(t + TN, wijk * vol);
+                            atomicAdd(t + 2 * TN, wijk * c);
+                        }
+            }
+            else {
+                const T ev = y[DS_E * S];
+                T gc[3] = { 0, 0, 0 };
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            const T pj = ptile[base + (i * TY + j) * TZ + k];
+                            gc[0] += pj * (dw[0][i] * w[1][j] * w[2][k]);
+                            gc[1] += pj * (w[0][i] * dw[1][j] * w[2][k]);
+                            gc[2] += pj * (w[0][i] * w[1][j] * dw[2][k]);
+                        }
+                const T sgc = ev * inv_dx * inv_dx; // both gradients carry 1/dx
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            const T v = sgc * (gc[0] * (dw[0][i] * w[1][j] * w[2][k]) + gc[1] * (w[0][i] * dw[1][j] * w[2][k])
+                                                  + gc[2] * (w[0][i] * w[1][j] * dw[2][k]));
+                            atomicAdd(tile + base + (i * TY + j) * TZ + k, v);
+                        }
+            }
+        }
+        __syncthreads();
+        const int f0[3] = { CG_SA, CG_SV, CG_DIAG }, f1[1] = { CG_AP };
+        flush_tile_cg<T, L>(a, tile, s_nbr, NF, MODE == 0 ? f0 : f1, threadIdx.x, NT);
+        __syncthreads();
+    }
+}
+
+// per scene of a node, with the warp's nodes all of one block (and so of one scene)
+template <class T>
+__device__ __forceinline__ void scene_sum(double v, int scene, double* dst)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int s0 = __shfl_sync(0xffffffffu, scene, 0);
+    if ((threadIdx.x & 31) == 0 && s0 >= 0 && v != 0.0) atomicAdd(dst + (size_t)s0 * (sizeof(CgScalars) / sizeof(double)), v);
+}
+
+// node kernels: STAGE 0 init (r = rhs, z = r/diag, p = z, r.z), 1 A p += diag p and p.Ap, 2 x, r, z update
+// and r.z, 3 p = z + beta p and A p = 0, 4 finish (the grid's phase field becomes x - pf)
+template <class T, int STAGE>
+__global__ void k_cg_nodes(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const uint32_t B = min(a.st->n_blocks, a.b_cap);
+    const uint32_t total = B * L::nodes;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ((total + 31) & ~31u); t += gridDim.x * blockDim.x) {
+        double acc = 0;
+        int scene = -1;
+        if (t < total) {
+            const uint32_t b = t / L::nodes, e = t % L::nodes;
+            const int sc = (int)(a.b_key[b] >> 40);
+            const SceneParams<T>& sp = a.scenes[sc];
+            CgScalars& cs = a.cgs[sc];
+            if (sp.implicit && (STAGE == 0 || STAGE == 4 || !cs.done)) {
+                scene = sc;
+                T* dg = cgv(a, CG_DIAG, b) + e;
+                const T diag = *dg;
+                T* x = cgv(a, CG_X, b) + e;
+                T* r = cgv(a, CG_R, b) + e;
+                T* z = cgv(a, CG_Z, b) + e;
+                T* p = cgv(a, CG_P, b) + e;
+                T* Ap = cgv(a, CG_AP, b) + e;
+                T* pf = a.vel + (size_t)b * NVEL * L::nodes + 3 * L::nodes + e;
+                const bool on = diag > (T)0;
+                if (STAGE == 0) {
+                    const T rhs = on ? cgv(a, CG_SA, b)[e] + *pf * cgv(a, CG_SV, b)[e] : (T)0;
+                    const T zz = on ? rhs / diag : (T)0;
+                    *x = 0;
+                    *r = rhs;
+                    *z = zz;
+                    *p = zz;
+                    *Ap = 0;
+                    acc = (double)rhs * (double)zz;
+                }
+                else if (STAGE == 1) {
+                    const T ap = on ? *Ap + diag * *p : (T)0;
+                    *Ap = ap;
+                    acc = (double)ap * (double)*p;
+                }
+                else if (STAGE == 2) {
+                    const T alpha = (T)(cs.zr / cs.pAp);
+                    const T xn = *x + *p * alpha, rn = *r - *Ap * alpha, zn = on ? rn / diag : (T)0;
+                    *x = xn;
+                    *r = rn;
+                    *z = zn;
+                    acc = (double)zn * (double)rn;
+                }
+                else if (STAGE == 3) {
+                    const T beta = (T)(cs.zr_new / cs.zr);
+                    *p = *z + beta * *p;
+                    *Ap = 0;
+                }
+                else {
+                    *pf = on ? *x - *pf : (T)0;
+                    // the solve's vectors start from zero next time
+                    cgv(a, CG_SA, b)[e] = 0;
+                    cgv(a, CG_SV, b)[e] = 0;
+                    *dg = 0;
+                    *Ap = 0;
+                }
+            }
+        }
+        if (STAGE == 0 || STAGE == 2) scene_sum<T>(acc, scene, STAGE == 0 ? &a.cgs[0].zr : &a.cgs[0].zr_new);
+        if (STAGE == 1) scene_sum<T>(acc, scene, &a.cgs[0].pAp);
+    }
+}
+
+// per-scene CG bookkeeping (one block): STAGE 0 after init, 1 after an iteration. STAGE 1 runs as the last
+// kernel of the loop body and sets the loop's condition: some scene unfinished, and never more than
+// CG_MAX_ITERATIONS + 1 passes (each scene stops itself at CG_MAX_ITERATIONS, so the loop always ends).
+template <class T, int STAGE>
+__global__ void k_cg_scalars(StepArgs<T> a, int n_scenes, cudaGraphConditionalHandle loop)
+{
+    __shared__ uint32_t s_active;
+    if (threadIdx.x == 0) s_active = 0;
+    __syncthreads();
+    const bool ab = aborted(a.st);
+    for (int s = threadIdx.x; s < n_scenes; s += blockDim.x) {
+        CgScalars& cs = a.cgs[s];
+        if (!a.scenes[s].implicit) {
+            cs.done = 1;
+            continue;
+        }
+        if (STAGE == 0) {
+            const double res = sqrt(cs.zr);
+            cs.tol = res < 1e-6 ? res : 1e-6;
+            cs.iter = 0;
+            cs.done = res <= cs.tol;
+        }
+        else if (!cs.done) {
+            cs.zr = cs.zr_new;
+            cs.iter++;
+            cs.done = sqrt(cs.zr) <= cs.tol || cs.iter >= CG_MAX_ITERATIONS;
+        }
+        cs.pAp = 0;
+        cs.zr_new = 0;
+        if (ab) cs.done = 1;
+        if (!cs.done) atomicAdd(&s_active, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a.st->work_cg = 0;
+        if (STAGE == 0)
+            a.st->cg_loops = 0;
+        else {
+            const uint32_t loops = ++a.st->cg_loops;
+            cudaGraphSetConditional(loop, (s_active > 0 && loops <= (uint32_t)CG_MAX_ITERATIONS) ? 1u : 0u);
+        }
     }
 }
 
@@ -1123,6 +1473,7 @@ __global__ void k_step_end(SceneParams<T>* scenes, int n_scenes, DevStatus* st)
         st->n_blocks = 0;
         st->work_p2g = 0;
         st->work_g2p = 0;
+        st->work_dmg = 0;
     }
 }
 

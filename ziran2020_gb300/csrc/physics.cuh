@@ -531,12 +531,12 @@ ZR_HD T degradation(T d, T k)
     return (((T)1 - d) * ((T)1 - d)) * ((T)1 - k) + k;
 }
 
-// Explicit AnisoMPM damage update of one particle (AnisoFractureSimulation.h:210-283, :365-391) with one
-// structural director a0 = e1 rotated by the polar R of F. Returns the new damage.
+// The damage drive D~ = zeta <phi - 1> of one particle, phi = (A sigma+) : (sigma+ A) / sigma_c^2 with the
+// undegraded Cauchy stress's tensile part sigma+ and the structural tensor A = I + alpha (R e1)(R e1)^T
+// (AnisoFractureSimulation.h:224-270; updateDTildeHelper :292-333 for the implicit solve).
 template <class T>
-ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, T dt, bool& fallback)
+ZR_HD T damage_drive(const Material<T>& mt, const T* F, T sigma_c, bool& fallback)
 {
-    T geo = d - mt.l0 * mt.l0 * lap;
     T tau[9], invJ;
     if (mt.model == MODEL_QR_STABLE_NEOHOOKEAN) {
         invJ = (T)1 / tau_qrnh(mt, F, (T)1, tau, true); // cauchy = P F^T / J with J from the QR (QRStableNeoHookean.h:86-96)
@@ -562,7 +562,16 @@ ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, 
     for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) contraction += M[3 * r + c] * M[3 * c + r];
     T phi = contraction / (sigma_c * sigma_c);
-    T dtilde = mt.zeta * (phi > (T)1 ? phi - (T)1 : (T)0);
+    return mt.zeta * (phi > (T)1 ? phi - (T)1 : (T)0);
+}
+
+// Explicit AnisoMPM damage update of one particle (AnisoFractureSimulation.h:210-283, :365-391) with one
+// structural director a0 = e1 rotated by the polar R of F. Returns the new damage.
+template <class T>
+ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, T dt, bool& fallback)
+{
+    T geo = d - mt.l0 * mt.l0 * lap;
+    T dtilde = damage_drive(mt, F, sigma_c, fallback);
     T diff = ((T)1 - d) * dtilde - geo;
     T nd = d + (dt / mt.eta) * (diff > (T)0 ? diff : (T)0);
     return nd < (T)1 ? nd : (T)1;
