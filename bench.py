@@ -31,12 +31,15 @@ WORKLOADS = {
     "elastic_box_dx64": (0, dict()),
     # the same slab with the QR-stable Neo-Hookean model and fibre stiffness 10 mu (examples/tubepull.h:104-107)
     "aniso_slab_qr_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256, model=2, fiber_stiffness=10.0)),
+    # the same slab with the implicit damage solve (AnisoFractureSimulation.h:437-626) instead of the explicit update
+    "aniso_slab_implicit_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256, implicit_damage=1)),
 }
 # CPU sample: the same slab at the same resolution, cropped to a 0.125 x 0.1 x 0.125 m piece
 CPU_SAMPLE = {"aniso_slab_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125)),
               "aniso_slab_dx128": dict(size=(0.25, 0.1, 0.25)),
               "elastic_box_dx64": dict(),
-              "aniso_slab_qr_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), model=2, fiber_stiffness=10.0)}
+              "aniso_slab_qr_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), model=2, fiber_stiffness=10.0),
+              "aniso_slab_implicit_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), implicit_damage=1)}
 
 
 def parse():
@@ -255,7 +258,7 @@ def _desc_for(kind, over, scenes):
     if kind == 1:
         dx = over.get("dx", 1 / 128)
         return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345, model=over.get("model") or None,
-                                 fiber=over.get("fiber_stiffness", 0.0))
+                                 fiber=over.get("fiber_stiffness", 0.0), implicit=bool(over.get("implicit_damage")))
     return scenes.elastic_box(size=over.get("size", 0.25), dx=over.get("dx", 1 / 64), seed=12345)
 
 
@@ -479,6 +482,7 @@ def run_ours(args, world, rank):
                "what": "per step: zr_scene_set_state from pinned FP32 host memory (x,v,C,F,d), zr_scene_step(1), zr_scene_get_state"}
     except Exception as ex:  # pinned memory needs torch; report instead of failing the line
         e2e = {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None, "error": str(ex)}
+    cg_iterations = s.cg_iterations
     del s
 
     # plain FP64 GPU path on the same workload
@@ -542,6 +546,10 @@ def run_ours(args, world, rank):
     cfg["active_blocks"] = int(blocks)
     cfg["particle_groups"] = int(groups)
     cfg["schedule"] = schedule
+    if over.get("implicit_damage"):
+        # the CG loop runs as a conditional node of the substep graph: 5 kernels per iteration, not counted in
+        # kernels_per_substep; the phase "grid" includes the whole damage solve
+        cfg["damage_solve"] = {"cg_iterations_last_substep": cg_iterations, "kernels_per_cg_iteration": 5}
     line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded recipe)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,

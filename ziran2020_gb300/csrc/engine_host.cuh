@@ -359,6 +359,7 @@ public:
             k_import<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const float*)stage_, nc, 0);
         else
             k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const double*)stage_, nc, 0);
+        if (field == FIELD_F || field == FIELD_SIGMA_C) ZR_CUDA(forget_drive(s));
         if (field == FIELD_X) return rekey();
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
@@ -398,6 +399,7 @@ public:
             else
                 k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (const double*)stage_, 25, offs[q]);
         }
+        ZR_CUDA(forget_drive(s));
         return rekey();
     }
 
@@ -452,6 +454,12 @@ public:
         ck_host_scenes_ = h_scenes_;
         ck_valid_ = true;
         return 0;
+    }
+
+    // the cached damage drive of scene s's particles no longer matches their F (all-ones bytes: NaN)
+    cudaError_t forget_drive(int s)
+    {
+        return cudaMemsetAsync(pool_[cur_] + (size_t)P_DRV * cap_ + h_scenes_[s].first, 0xff, sizeof(T) * h_scenes_[s].count, stream_);
     }
 
     int cg_iterations(int s, int* out) override
@@ -750,7 +758,7 @@ private:
         int rc;
         if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
             || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1))
-            || (rc = put(P_MDT, 1, sd.dtilde_max, 0, 0)))
+            || (rc = put(P_MDT, 1, sd.dtilde_max, 0, 0)) || (rc = put(P_DRV, 1, {}, NAN, NAN)))
             return rc;
         const uint8_t* mp = nullptr;
         if (!sd.material.empty()) {
@@ -784,8 +792,8 @@ private:
             init_err_ = fail(ZR_ERR_CUDA_, "stream/pinned allocation failed");
             return;
         }
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[0], k_dmg_group<T, 0>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[1], k_dmg_group<T, 1>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[0], k_dmg_rhs<T>, DmgShape<T>::NT, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_dmg_[1], k_dmg_apply<T>, DmgShape<T>::NT, 0);
         occ_dmg_[0] = std::max(1, occ_dmg_[0]);
         occ_dmg_[1] = std::max(1, occ_dmg_[1]);
         scatter_setup<0>();
@@ -1002,8 +1010,7 @@ private:
     int enqueue_damage_solve(const StepArgs<T>& a)
     {
         ZR_CUDA(cudaMemsetAsync(cgs_, 0, sizeof(CgScalars) * h_scenes_.size(), stream_));
-        k_dmg_prep<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
-        k_dmg_group<T, 0><<<nsm_ * occ_dmg_[0], 128, 0, stream_>>>(a);
+        k_dmg_rhs<T><<<nsm_ * occ_dmg_[0], DmgShape<T>::NT, 0, stream_>>>(a);
         k_cg_nodes<T, 0><<<nsm_ * 8, 256, 0, stream_>>>(a);
         k_cg_scalars<T, 0><<<1, 256, 0, stream_>>>(a, n_scenes(), cudaGraphConditionalHandle{});
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1053,7 +1060,7 @@ private:
         cudaGraph_t body = np.conditional.phGraph_out[0];
         ZR_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
         ZR_CUDA(cudaStreamBeginCaptureToGraph(side_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-        k_dmg_group<T, 1><<<nsm_ * occ_dmg_[1], 128, 0, side_>>>(a);
+        k_dmg_apply<T><<<nsm_ * occ_dmg_[1], DmgShape<T>::NT, 0, side_>>>(a);
         k_cg_nodes<T, 1><<<nsm_ * 8, 256, 0, side_>>>(a);
         k_cg_nodes<T, 2><<<nsm_ * 8, 256, 0, side_>>>(a);
         k_cg_nodes<T, 3><<<nsm_ * 8, 256, 0, side_>>>(a);

@@ -44,7 +44,9 @@ constexpr uint64_t HASH_EMPTY = ~0ULL;
 constexpr int HASH_PROBES = 64;
 
 // particle pool: field k of storage slot i at f[k * stride + i]
-enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_MDT = 28, P_NF = 29 };
+// P_MDT: the implicit damage solve's D~ history; P_DRV: the damage drive of the particle's current F, filled by
+// G2P for implicit scenes (NaN = not known: recomputed from F)
+enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_MDT = 28, P_DRV = 29, P_NF = 30 };
 
 template <class T>
 struct Pool {
@@ -1120,6 +1122,14 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                         const T nd = dd + pw;
                         dd = nd > dd ? nd : dd;
                         dd = dd < (T)1 ? dd : (T)1;
+                        // the next substep's solve folds the drive of the new F into the history: computed here,
+                        // where the explicit update would evaluate the drive of the old F
+                        T Fn[9];
+#pragma unroll
+                        for (int c = 0; c < 9; c++) Fn[c] = Q.f[(P_F + c) * Q.stride + i];
+                        bool fb = false;
+                        Q.f[P_DRV * Q.stride + i] = damage_drive(mt, Fn, sc, fb);
+                        if (fb) atomicAdd(&a.st->fallback, 1u);
                     }
                     else {
                         bool fb = false;
@@ -1150,72 +1160,69 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 // batch runs the iterations it would run alone. G2P then adds sum_i w_ip (x_i - pf_i) to the damage.
 // ---------------------------------------------------------------------------------------------------
 enum { CG_SA = 0, CG_SV, CG_DIAG, CG_X, CG_R, CG_Z, CG_P, CG_AP, CG_NF }; // node vectors
-enum { DS_F = 0, DS_A = 3, DS_VOL = 4, DS_C = 5, DS_E = 6 }; // particle scratch fields in the payload buffer
+enum { DS_F = 0, DS_E = 3 }; // particle scratch fields in the payload buffer (fractional position, e_p)
 constexpr int CG_MAX_ITERATIONS = 100;
 
 template <class T>
 __device__ __forceinline__ T* cgv(const StepArgs<T>& a, int f, uint32_t slot) { return a.cg + ((size_t)f * a.b_cap + slot) * LayoutOf<T>::type::nodes; }
 
-// per sorted particle: D~ history, vol, the solve's coefficients and the fractional position
+// Per sorted particle q of an implicit scene: the D~ history; v gets the fractional position, vol D~ dt/eta,
+// vol and c_p; the fractional position and e_p go to the particle scratch for the operator. The drive of the
+// particle's F comes from the cache G2P filled (P_DRV) unless a state write invalidated it (NaN).
+// the drive of a particle whose cached value was invalidated (after a state write): out of line, so the
+// group kernel keeps the registers of its common path
 template <class T>
-__global__ void k_dmg_prep(StepArgs<T> a)
+__device__ __noinline__ T drive_uncached(const Material<T>& mt, const T* F, T sigma_c, uint32_t* fallbacks)
 {
-    using L = typename LayoutOf<T>::type;
-    if (aborted(a.st)) return;
-    const KeyLayout kl = a.kl;
-    const int64_t S = a.pstride;
-    const Pool<T>& P = a.pin;
-    uint32_t fallbacks = 0;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
-        const SceneParams<T>& sp = a.scenes[kl.scene(kl.at(a.keys_sorted, q))];
-        if (!sp.implicit) continue;
-        const uint32_t j = a.vals_sorted[q];
-        T* y = a.pay + pay_pos(q);
-#pragma unroll
-        for (int e = 0; e < 3; e++) {
-            const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
-            y[(DS_F + e) * S] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
-        }
-        const uint32_t mat = P.pid[j] >> L::index_bits;
-        const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
-        T av = 0, vol = 0, c = 0, ev = 0;
-        if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
-            T F[9];
-#pragma unroll
-            for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
-            vol = P.f[P_V0 * P.stride + j] * det3(F);
-            bool fb = false;
-            const T drive = damage_drive(mt, F, P.f[P_SC * P.stride + j], fb);
-            if (fb) fallbacks++;
-            T hist = P.f[P_MDT * P.stride + j];
-            hist = drive > hist ? drive : hist;
-            P.f[P_MDT * P.stride + j] = hist;
-            const T dt = sp.dt;
-            av = ((dt * hist) / mt.eta) * vol;
-            c = vol * ((T)1 + ((dt / mt.eta) * (hist + (T)1)));
-            ev = vol * (dt / mt.eta) * mt.l0 * mt.l0;
-        }
-        y[DS_A * S] = av;
-        y[DS_VOL * S] = vol;
-        y[DS_C * S] = c;
-        y[DS_E * S] = ev;
-    }
-    if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
+    bool fb = false;
+    const T d = damage_drive(mt, F, sigma_c, fb);
+    if (fb) atomicAdd(fallbacks, 1u);
+    return d;
 }
 
-// quadratic B-spline weights and derivatives (per unit cell) of the three nodes from a fractional position
 template <class T>
-__device__ __forceinline__ void weights_of(const T* y, int64_t S, T (&w)[3][3], T (&dw)[3][3])
+__device__ __forceinline__ void dmg_prep_particle(const StepArgs<T>& a, const SceneParams<T>& sp, uint32_t q, T (&v)[6])
 {
+    using L = typename LayoutOf<T>::type;
+    const int64_t S = a.pstride;
+    const Pool<T>& P = a.pin;
+    const uint32_t j = a.vals_sorted[q];
+    T* y = a.pay + pay_pos(q);
 #pragma unroll
-    for (int e = 0; e < 3; e++) bspline_w(y[(DS_F + e) * S], 0, w[e], dw[e]);
+    for (int e = 0; e < 3; e++) {
+        const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
+        v[e] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
+        y[(DS_F + e) * S] = v[e];
+    }
+    const uint32_t mat = P.pid[j] >> L::index_bits;
+    const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+    T av = 0, vol = 0, c = 0, ev = 0;
+    if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
+        T F[9];
+#pragma unroll
+        for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
+        vol = P.f[P_V0 * P.stride + j] * det3(F);
+        T drive = P.f[P_DRV * P.stride + j];
+        if (!(drive >= (T)0)) drive = drive_uncached(mt, F, P.f[P_SC * P.stride + j], &a.st->fallback);
+        T hist = P.f[P_MDT * P.stride + j];
+        hist = drive > hist ? drive : hist;
+        P.f[P_MDT * P.stride + j] = hist;
+        const T dt = sp.dt;
+        av = ((dt * hist) / mt.eta) * vol;
+        c = vol * ((T)1 + ((dt / mt.eta) * (hist + (T)1)));
+        ev = vol * (dt / mt.eta) * mt.l0 * mt.l0;
+    }
+    v[3] = av;
+    v[4] = vol;
+    v[5] = c;
+    y[DS_E * S] = ev;
 }
 
 // node tile of a group (its block plus 2 nodes on the + side): index of node (lx, ly, lz)
 template <class L>
 __device__ __forceinline__ int tile_index(int lx, int ly, int lz) { return (lx * (L::sy + 2) + ly) * (L::sz + 2) + lz; }
 
-// tile -> the node vectors of the 8 neighbouring blocks (atomics), then cleared; nf fields, vector f0 + f
+// tile -> the node vectors of the 8 neighbouring blocks (atomics), then cleared; nf fields, vector f_of[f]
 template <class T, class L>
 __device__ void flush_tile_cg(const StepArgs<T>& a, T* tile, const int32_t* nbr, int nf, const int* f_of, int tid, int nthreads)
 {
@@ -1236,104 +1243,243 @@ __device__ void flush_tile_cg(const StepArgs<T>& a, T* tile, const int32_t* nbr,
     }
 }
 
-// MODE 0: scatter vol D~ dt/eta, vol and c_p with the weights (right-hand side parts, diagonal);
-// MODE 1: the operator's particle part, sum_p (e_p sum_j p_j grad w_jp) . grad w_ip, into A p
-template <class T, int MODE>
-__global__ void __launch_bounds__(128) k_dmg_group(StepArgs<T> a)
+// Claim the next group of an implicit scene for a damage-solve kernel (thread 0 claims, all threads get the same
+// answer): the group's particle range and neighbour blocks. Returns the scene, or -1 when the groups are exhausted.
+template <class T>
+__device__ int dmg_claim(const StepArgs<T>& a, uint32_t* counter, bool need_unfinished, uint32_t& start, uint32_t& end, int32_t* s_nbr, int* s_g,
+    int* s_skip)
+{
+    const KeyLayout kl = a.kl;
+    const uint32_t G = a.st->n_groups;
+    for (;;) {
+        if (threadIdx.x == 0) *s_g = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int g = *s_g;
+        if (g >= (int)G) return -1;
+        start = a.g_start[g];
+        end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
+        const uint32_t sc = kl.scene(kl.at(a.keys_sorted, start));
+        if (threadIdx.x == 0) *s_skip = !a.scenes[sc].implicit || (need_unfinished && a.cgs[sc].done);
+        if (threadIdx.x < 8) s_nbr[threadIdx.x] = a.g_nbr[g * 8 + threadIdx.x];
+        __syncthreads();
+        if (!*s_skip) return (int)sc;
+        __syncthreads(); // every thread has read *s_skip before thread 0 claims again
+    }
+}
+
+// threads and particle chunk of the damage solve's group kernels: one thread per (in-block cell, stencil x-offset);
+// a chunk's per-particle values are staged in shared memory for the per-cell sums
+template <class T>
+struct DmgShape {
+    using L = typename LayoutOf<T>::type;
+    static constexpr int NT = 3 * L::nodes;
+    static constexpr int CHUNK = 512;
+    static constexpr int NS = 6; // staged values per particle
+    static constexpr int MINB = 4; // CTAs per SM the registers are cut for: these kernels wait on memory
+};
+
+// cell ranges of a staged chunk: particles of one cell are contiguous (sorted by cell inside the block)
+template <int NC>
+__device__ __forceinline__ void chunk_cells(const uint8_t* cellof, int cnt, int16_t* cfirst, int16_t* clast, int tid, int nt)
+{
+    for (int q = tid; q < cnt; q += nt) {
+        const int e = cellof[q];
+        if (q == 0 || cellof[q - 1] != e) cfirst[e] = (int16_t)q;
+        if (q == cnt - 1 || cellof[q + 1] != e) clast[e] = (int16_t)(q + 1);
+    }
+}
+
+// Right-hand side parts and the preconditioner's diagonal. Per chunk: the particles' coefficients (phase 1,
+// staged in shared memory with the fractional positions), then one thread per (in-block cell, x-offset) sums the
+// 9 (y, z) nodes over its cell's particles in registers (phase 2) and adds them to the group's shared node tile;
+// the tile goes to the node vectors CG_SA, CG_SV, CG_DIAG.
+template <class T>
+__global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    constexpr int NT = 128, TN = (L::sx + 2) * (L::sy + 2) * (L::sz + 2), NF = MODE == 0 ? 3 : 1;
-    constexpr int TY = L::sy + 2, TZ = L::sz + 2;
-    __shared__ T tile[NF * TN];
-    __shared__ T ptile[MODE == 1 ? TN : 1];
+    using D = DmgShape<T>;
+    constexpr int NC = L::nodes, NT = D::NT, CHUNK = D::CHUNK, TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
+    __shared__ T tile[3 * TN];
+    __shared__ T st[D::NS][CHUNK]; // fr x3, vol D~ dt/eta, vol, c
+    __shared__ uint8_t cellof[CHUNK];
+    __shared__ int16_t cfirst[NC], clast[NC];
     __shared__ int s_g, s_skip;
     __shared__ int32_t s_nbr[8];
     if (aborted_cta(a.st)) return;
-    const uint32_t G = a.st->n_groups;
+    const KeyLayout kl = a.kl;
+    const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
+    const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    for (int q = tid; q < 3 * TN; q += NT) tile[q] = (T)0;
+    const int f_of[3] = { CG_SA, CG_SV, CG_DIAG };
+    for (;;) {
+        uint32_t start, end;
+        const int sc = dmg_claim<T>(a, &a.st->work_dmg, false, start, end, s_nbr, &s_g, &s_skip);
+        if (sc < 0) break;
+        const SceneParams<T>& sp = a.scenes[sc];
+        bool any = false;
+        for (uint32_t c0 = start; c0 < end; c0 += CHUNK) {
+            const int cnt = (int)min((uint32_t)CHUNK, end - c0);
+            if (tid < NC) {
+                cfirst[tid] = 0;
+                clast[tid] = 0;
+            }
+            for (int q = tid; q < cnt; q += NT) {
+                T v[D::NS];
+                dmg_prep_particle(a, sp, c0 + q, v);
+#pragma unroll
+                for (int f = 0; f < D::NS; f++) st[f][q] = v[f];
+                cellof[q] = (uint8_t)((kl.at(a.keys_sorted, c0 + q) >> kl.ib) & (NC - 1));
+            }
+            __syncthreads();
+            chunk_cells<NC>(cellof, cnt, cfirst, clast, tid, NT);
+            __syncthreads();
+            T acc[9][3];
+#pragma unroll
+            for (int n = 0; n < 9; n++) acc[n][0] = acc[n][1] = acc[n][2] = (T)0;
+            const int qa = cfirst[c], qb = clast[c];
+            for (int q = qa; q < qb; q++) {
+                const T cc = st[5][q];
+                if (cc == (T)0) continue; // not damageable
+                const T av = st[3][q], vol = st[4][q];
+                T w[3][3], dw[3][3];
+#pragma unroll
+                for (int e = 0; e < 3; e++) bspline_w(st[e][q], 0, w[e], dw[e]);
+                const T wx = w[0][ii];
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        const T wijk = wx * w[1][j] * w[2][k];
+                        acc[j * 3 + k][0] += wijk * av;
+                        acc[j * 3 + k][1] += wijk * vol;
+                        acc[j * 3 + k][2] += wijk * cc;
+                    }
+            }
+            if (qb > qa) {
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        T* t = tile + tile_index<L>(cx + ii, cy + j, cz + k);
+                        atomicAdd(t, acc[j * 3 + k][0]);
+                        atomicAdd(t + TN, acc[j * 3 + k][1]);
+                        atomicAdd(t + 2 * TN, acc[j * 3 + k][2]);
+                    }
+            }
+            any = true;
+            __syncthreads();
+        }
+        if (any) flush_tile_cg<T, L>(a, tile, s_nbr, 3, f_of, tid, NT);
+        __syncthreads();
+    }
+}
+
+// The operator's particle part for the search direction p. Per chunk: per particle gc = e_p / dx^2 sum_j p_j
+// grad w_jp (gradients per unit cell; phase 1, from p staged on the group's tile), staged with the fractional
+// position; then per (cell, x-offset) thread the sums gc . grad w over its cell's particles for its 9 nodes
+// (phase 2) into the tile, which goes to A p (CG_AP).
+template <class T>
+__global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_apply(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    using D = DmgShape<T>;
+    constexpr int NC = L::nodes, NT = D::NT, CHUNK = D::CHUNK, TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
+    __shared__ T tile[TN];
+    __shared__ T ptile[TN];
+    __shared__ T st[D::NS][CHUNK]; // fr x3, gc x3
+    __shared__ uint8_t cellof[CHUNK];
+    __shared__ int16_t cfirst[NC], clast[NC];
+    __shared__ int s_g, s_skip;
+    __shared__ int32_t s_nbr[8];
+    if (aborted_cta(a.st)) return;
     const KeyLayout kl = a.kl;
     const int64_t S = a.pstride;
-    for (int q = threadIdx.x; q < NF * TN; q += NT) tile[q] = (T)0;
-    uint32_t* counter = MODE == 0 ? &a.st->work_dmg : &a.st->work_cg;
+    const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
+    const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    for (int q = tid; q < TN; q += NT) tile[q] = (T)0;
+    const int f_of[1] = { CG_AP };
     for (;;) {
-        if (threadIdx.x == 0) s_g = (int)atomicAdd(counter, 1u);
-        __syncthreads();
-        const int g = s_g;
-        if (g >= (int)G) break;
-        const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
-        if (threadIdx.x < 8) s_nbr[threadIdx.x] = a.g_nbr[g * 8 + threadIdx.x];
-        if (threadIdx.x == 0) {
-            const uint32_t sc = kl.scene(kl.at(a.keys_sorted, start));
-            s_skip = !a.scenes[sc].implicit || (MODE == 1 && a.cgs[sc].done);
+        uint32_t start, end;
+        const int sc = dmg_claim<T>(a, &a.st->work_cg, true, start, end, s_nbr, &s_g, &s_skip);
+        if (sc < 0) break;
+        for (int q = tid; q < TN; q += NT) {
+            const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
+            const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+            const int slot = s_nbr[ax * 4 + ay * 2 + az];
+            ptile[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? cgv(a, CG_P, slot)[L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)] : (T)0;
         }
         __syncthreads();
-        if (s_skip) {
-            __syncthreads();
-            continue;
-        }
-        if (MODE == 1) { // stage p on the tile
-            for (int q = threadIdx.x; q < TN; q += NT) {
-                const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
-                const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
-                const int slot = s_nbr[ax * 4 + ay * 2 + az];
-                ptile[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? cgv(a, CG_P, slot)[L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)] : (T)0;
+        const T inv_dx = a.scenes[sc].inv_dx;
+        for (uint32_t c0 = start; c0 < end; c0 += CHUNK) {
+            const int cnt = (int)min((uint32_t)CHUNK, end - c0);
+            if (tid < NC) {
+                cfirst[tid] = 0;
+                clast[tid] = 0;
             }
-            __syncthreads();
-        }
-        const T inv_dx = a.scenes[kl.scene(kl.at(a.keys_sorted, start))].inv_dx;
-        for (uint32_t q = start + threadIdx.x; q < end; q += NT) {
-            const T* y = a.pay + pay_pos(q);
-            const T c = y[DS_C * S];
-            if (c == (T)0) continue; // not damageable
-            const int e = (int)((kl.at(a.keys_sorted, q) >> kl.ib) & (L::nodes - 1));
-            const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
-            const int base = tile_index<L>(lx, ly, lz);
-            T w[3][3], dw[3][3];
-            weights_of(y, S, w, dw);
-            if (MODE == 0) {
-                const T av = y[DS_A * S], vol = y[DS_VOL * S];
-#pragma unroll
-                for (int i = 0; i < 3; i++)
-#pragma unroll
-                    for (int j = 0; j < 3; j++)
-#pragma unroll
-                        for (int k = 0; k < 3; k++) {
-                            const T wijk = w[0][i] * w[1][j] * w[2][k];
-                            T* t = tile + base + (i * TY + j) * TZ + k;
-                            atomicAdd(t, wijk * av);
-                            atomicAdd(t + TN, wijk * vol);
-                            atomicAdd(t + 2 * TN, wijk * c);
-                        }
-            }
-            else {
+            for (int q = tid; q < cnt; q += NT) {
+                const T* y = a.pay + pay_pos(c0 + q);
                 const T ev = y[DS_E * S];
-                T gc[3] = { 0, 0, 0 };
+                const int e = (int)((kl.at(a.keys_sorted, c0 + q) >> kl.ib) & (NC - 1));
+                cellof[q] = (uint8_t)e;
+                T fr[3], w[3][3], dw[3][3];
 #pragma unroll
-                for (int i = 0; i < 3; i++)
+                for (int f = 0; f < 3; f++) {
+                    fr[f] = y[(DS_F + f) * S];
+                    st[f][q] = fr[f];
+                    bspline_w(fr[f], 0, w[f], dw[f]);
+                }
+                T g0 = 0, g1 = 0, g2 = 0;
+                if (ev != (T)0) {
+                    const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
+                    const T* pt = ptile + tile_index<L>(lx, ly, lz);
 #pragma unroll
-                    for (int j = 0; j < 3; j++)
+                    for (int i = 0; i < 3; i++)
 #pragma unroll
-                        for (int k = 0; k < 3; k++) {
-                            const T pj = ptile[base + (i * TY + j) * TZ + k];
-                            gc[0] += pj * (dw[0][i] * w[1][j] * w[2][k]);
-                            gc[1] += pj * (w[0][i] * dw[1][j] * w[2][k]);
-                            gc[2] += pj * (w[0][i] * w[1][j] * dw[2][k]);
-                        }
-                const T sgc = ev * inv_dx * inv_dx; // both gradients carry 1/dx
+                        for (int j = 0; j < 3; j++)
 #pragma unroll
-                for (int i = 0; i < 3; i++)
-#pragma unroll
-                    for (int j = 0; j < 3; j++)
-#pragma unroll
-                        for (int k = 0; k < 3; k++) {
-                            const T v = sgc * (gc[0] * (dw[0][i] * w[1][j] * w[2][k]) + gc[1] * (w[0][i] * dw[1][j] * w[2][k])
-                                                  + gc[2] * (w[0][i] * w[1][j] * dw[2][k]));
-                            atomicAdd(tile + base + (i * TY + j) * TZ + k, v);
-                        }
+                            for (int k = 0; k < 3; k++) {
+                                const T pj = pt[(i * TY + j) * TZ + k];
+                                g0 += pj * (dw[0][i] * w[1][j] * w[2][k]);
+                                g1 += pj * (w[0][i] * dw[1][j] * w[2][k]);
+                                g2 += pj * (w[0][i] * w[1][j] * dw[2][k]);
+                            }
+                    const T sgc = ev * inv_dx * inv_dx; // both gradients carry 1/dx
+                    g0 *= sgc;
+                    g1 *= sgc;
+                    g2 *= sgc;
+                }
+                st[3][q] = g0;
+                st[4][q] = g1;
+                st[5][q] = g2;
             }
+            __syncthreads();
+            chunk_cells<NC>(cellof, cnt, cfirst, clast, tid, NT);
+            __syncthreads();
+            T acc[9];
+#pragma unroll
+            for (int n = 0; n < 9; n++) acc[n] = (T)0;
+            const int qa = cfirst[c], qb = clast[c];
+            for (int q = qa; q < qb; q++) {
+                const T g0 = st[3][q], g1 = st[4][q], g2 = st[5][q];
+                if (g0 == (T)0 && g1 == (T)0 && g2 == (T)0) continue;
+                T w[3][3], dw[3][3];
+#pragma unroll
+                for (int e = 0; e < 3; e++) bspline_w(st[e][q], 0, w[e], dw[e]);
+                const T a0 = g0 * dw[0][ii], a1 = g1 * w[0][ii], a2 = g2 * w[0][ii];
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) acc[j * 3 + k] += (a0 * w[1][j] + a1 * dw[1][j]) * w[2][k] + a2 * (w[1][j] * dw[2][k]);
+            }
+            if (qb > qa) {
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) atomicAdd(tile + tile_index<L>(cx + ii, cy + j, cz + k), acc[j * 3 + k]);
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        const int f0[3] = { CG_SA, CG_SV, CG_DIAG }, f1[1] = { CG_AP };
-        flush_tile_cg<T, L>(a, tile, s_nbr, NF, MODE == 0 ? f0 : f1, threadIdx.x, NT);
+        flush_tile_cg<T, L>(a, tile, s_nbr, 1, f_of, tid, NT);
         __syncthreads();
     }
 }
