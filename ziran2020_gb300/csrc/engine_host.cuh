@@ -194,6 +194,7 @@ public:
         models_ = 0;
         any_damage_ = false;
         implicit_ = false;
+        drive_stale_ = true;
         for (auto& sp : h_scenes_) {
             for (int k = 0; k < sp.n_materials; k++) models_ |= 1 << sp.materials[k].model;
             any_damage_ = any_damage_ || sp.damage;
@@ -269,6 +270,7 @@ public:
     // An aborted substep is retried after growing the grid (capacity) or reported with the state left at its start.
     int run_steps(int nsteps, StepReport& r, int& done)
     {
+        if (int rc = refresh_drive()) return rc;
         const int target = done + nsteps;
         int grow_rounds = 0;
         while (done < target) {
@@ -456,10 +458,19 @@ public:
         return 0;
     }
 
-    // the cached damage drive of scene s's particles no longer matches their F (all-ones bytes: NaN)
-    cudaError_t forget_drive(int s)
+    // the cached damage drive (P_DRV) no longer matches F: refilled before the next substep
+    cudaError_t forget_drive(int)
     {
-        return cudaMemsetAsync(pool_[cur_] + (size_t)P_DRV * cap_ + h_scenes_[s].first, 0xff, sizeof(T) * h_scenes_[s].count, stream_);
+        drive_stale_ = true;
+        return cudaSuccess;
+    }
+    int refresh_drive()
+    {
+        if (!implicit_ || !drive_stale_) return 0;
+        k_dmg_drive<T><<<nsm_ * 8, 256, 0, stream_>>>(args(cur_), keys_in_);
+        ZR_CUDA(cudaGetLastError());
+        drive_stale_ = false;
+        return 0;
     }
 
     int cg_iterations(int s, int* out) override
@@ -632,6 +643,7 @@ private:
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
     bool implicit_ = false; // some scene solves its damage implicitly
+    bool drive_stale_ = true; // P_DRV must be refilled from F before the next substep
     T* cg_ = nullptr; // the damage solve's node vectors (CG_NF x b_cap_ blocks), allocated when implicit_
     CgScalars* cgs_ = nullptr; // per scene (scene_cap_)
     cudaStream_t side_ = nullptr; // captures the damage solve's loop body
@@ -758,7 +770,7 @@ private:
         int rc;
         if ((rc = put(P_X, 3, sd.x, 0, 0)) || (rc = put(P_V, 3, sd.v, 0, 0)) || (rc = put(P_C, 9, sd.C, 0, 0)) || (rc = put(P_F, 9, sd.F, 1, 0))
             || (rc = put(P_M, 1, sd.m, 0, 0)) || (rc = put(P_V0, 1, sd.V0, 0, 0)) || (rc = put(P_D, 1, sd.d, 0, 0)) || (rc = put(P_SC, 1, sd.sigma_c, 1, 1))
-            || (rc = put(P_MDT, 1, sd.dtilde_max, 0, 0)) || (rc = put(P_DRV, 1, {}, NAN, NAN)))
+            || (rc = put(P_MDT, 1, sd.dtilde_max, 0, 0)))
             return rc;
         const uint8_t* mp = nullptr;
         if (!sd.material.empty()) {
@@ -1010,6 +1022,7 @@ private:
     int enqueue_damage_solve(const StepArgs<T>& a)
     {
         ZR_CUDA(cudaMemsetAsync(cgs_, 0, sizeof(CgScalars) * h_scenes_.size(), stream_));
+        k_dmg_prep<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
         k_dmg_rhs<T><<<nsm_ * occ_dmg_[0], DmgShape<T>::NT, 0, stream_>>>(a);
         k_cg_nodes<T, 0><<<nsm_ * 8, 256, 0, stream_>>>(a);
         k_cg_scalars<T, 0><<<1, 256, 0, stream_>>>(a, n_scenes(), cudaGraphConditionalHandle{});
@@ -1252,6 +1265,7 @@ private:
     // one trial substep with schedule sc on the current state; p2g / g2p milliseconds; state rolled back
     int trial(const Schedule& sc, float& p2g_ms, float& g2p_ms, bool& aborted_out)
     {
+        if (int rc = refresh_drive()) return rc;
         sched_ = sc;
         if ((int)ev_.size() < 6) {
             size_t old = ev_.size();

@@ -44,8 +44,8 @@ constexpr uint64_t HASH_EMPTY = ~0ULL;
 constexpr int HASH_PROBES = 64;
 
 // particle pool: field k of storage slot i at f[k * stride + i]
-// P_MDT: the implicit damage solve's D~ history; P_DRV: the damage drive of the particle's current F, filled by
-// G2P for implicit scenes (NaN = not known: recomputed from F)
+// P_MDT: the implicit damage solve's D~ history; P_DRV: the damage drive of the particle's current F (implicit
+// scenes), kept by G2P and refilled after state writes
 enum { P_X = 0, P_V = 3, P_C = 6, P_F = 15, P_M = 24, P_V0 = 25, P_D = 26, P_SC = 27, P_MDT = 28, P_DRV = 29, P_NF = 30 };
 
 template <class T>
@@ -1160,62 +1160,82 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 // batch runs the iterations it would run alone. G2P then adds sum_i w_ip (x_i - pf_i) to the damage.
 // ---------------------------------------------------------------------------------------------------
 enum { CG_SA = 0, CG_SV, CG_DIAG, CG_X, CG_R, CG_Z, CG_P, CG_AP, CG_NF }; // node vectors
-enum { DS_F = 0, DS_E = 3 }; // particle scratch fields in the payload buffer (fractional position, e_p)
+enum { DS_F = 0, DS_A = 3, DS_VOL = 4, DS_C = 5, DS_E = 6 }; // particle scratch fields in the payload buffer
 constexpr int CG_MAX_ITERATIONS = 100;
 
 template <class T>
 __device__ __forceinline__ T* cgv(const StepArgs<T>& a, int f, uint32_t slot) { return a.cg + ((size_t)f * a.b_cap + slot) * LayoutOf<T>::type::nodes; }
 
-// Per sorted particle q of an implicit scene: the D~ history; v gets the fractional position, vol D~ dt/eta,
-// vol and c_p; the fractional position and e_p go to the particle scratch for the operator. The drive of the
-// particle's F comes from the cache G2P filled (P_DRV) unless a state write invalidated it (NaN).
-// the drive of a particle whose cached value was invalidated (after a state write): out of line, so the
-// group kernel keeps the registers of its common path
+// The damage drive of every particle of the implicit scenes from its current F, in storage order (the scene from
+// the particle's current key): fills the cache P_DRV after a state write made it stale; G2P keeps it afterwards.
 template <class T>
-__device__ __noinline__ T drive_uncached(const Material<T>& mt, const T* F, T sigma_c, uint32_t* fallbacks)
-{
-    bool fb = false;
-    const T d = damage_drive(mt, F, sigma_c, fb);
-    if (fb) atomicAdd(fallbacks, 1u);
-    return d;
-}
-
-template <class T>
-__device__ __forceinline__ void dmg_prep_particle(const StepArgs<T>& a, const SceneParams<T>& sp, uint32_t q, T (&v)[6])
+__global__ void k_dmg_drive(StepArgs<T> a, const uint64_t* keys)
 {
     using L = typename LayoutOf<T>::type;
+    const Pool<T>& P = a.pin;
+    uint32_t fallbacks = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_total; i += gridDim.x * blockDim.x) {
+        const SceneParams<T>& sp = a.scenes[a.kl.scene(a.kl.at(keys, i))];
+        if (!sp.implicit) continue;
+        const uint32_t mat = P.pid[i] >> L::index_bits;
+        const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+        T drive = 0;
+        if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
+            T F[9];
+#pragma unroll
+            for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + i];
+            bool fb = false;
+            drive = damage_drive(mt, F, P.f[P_SC * P.stride + i], fb);
+            if (fb) fallbacks++;
+        }
+        P.f[P_DRV * P.stride + i] = drive;
+    }
+    if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
+}
+
+// Per sorted particle of an implicit scene (one thread each, no barriers): the D~ history folded with the drive
+// of the particle's F (cached in P_DRV), and into the particle scratch the fractional position, vol D~ dt/eta,
+// vol, c_p and e_p.
+template <class T>
+__global__ void k_dmg_prep(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    if (aborted(a.st)) return;
+    const KeyLayout kl = a.kl;
     const int64_t S = a.pstride;
     const Pool<T>& P = a.pin;
-    const uint32_t j = a.vals_sorted[q];
-    T* y = a.pay + pay_pos(q);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
+        const SceneParams<T>& sp = a.scenes[kl.scene(kl.at(a.keys_sorted, q))];
+        if (!sp.implicit) continue;
+        const uint32_t j = a.vals_sorted[q];
+        T* y = a.pay + pay_pos(q);
 #pragma unroll
-    for (int e = 0; e < 3; e++) {
-        const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
-        v[e] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
-        y[(DS_F + e) * S] = v[e];
-    }
-    const uint32_t mat = P.pid[j] >> L::index_bits;
-    const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
-    T av = 0, vol = 0, c = 0, ev = 0;
-    if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
-        T F[9];
+        for (int e = 0; e < 3; e++) {
+            const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
+            y[(DS_F + e) * S] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
+        }
+        const uint32_t mat = P.pid[j] >> L::index_bits;
+        const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+        T av = 0, vol = 0, c = 0, ev = 0;
+        if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
+            T F[9];
 #pragma unroll
-        for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
-        vol = P.f[P_V0 * P.stride + j] * det3(F);
-        T drive = P.f[P_DRV * P.stride + j];
-        if (!(drive >= (T)0)) drive = drive_uncached(mt, F, P.f[P_SC * P.stride + j], &a.st->fallback);
-        T hist = P.f[P_MDT * P.stride + j];
-        hist = drive > hist ? drive : hist;
-        P.f[P_MDT * P.stride + j] = hist;
-        const T dt = sp.dt;
-        av = ((dt * hist) / mt.eta) * vol;
-        c = vol * ((T)1 + ((dt / mt.eta) * (hist + (T)1)));
-        ev = vol * (dt / mt.eta) * mt.l0 * mt.l0;
+            for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
+            vol = P.f[P_V0 * P.stride + j] * det3(F);
+                const T drive = P.f[P_DRV * P.stride + j];
+            T hist = P.f[P_MDT * P.stride + j];
+            hist = drive > hist ? drive : hist;
+            P.f[P_MDT * P.stride + j] = hist;
+            const T dt = sp.dt;
+            av = ((dt * hist) / mt.eta) * vol;
+            c = vol * ((T)1 + ((dt / mt.eta) * (hist + (T)1)));
+            ev = vol * (dt / mt.eta) * mt.l0 * mt.l0;
+        }
+        y[DS_A * S] = av;
+        y[DS_VOL * S] = vol;
+        y[DS_C * S] = c;
+        y[DS_E * S] = ev;
     }
-    v[3] = av;
-    v[4] = vol;
-    v[5] = c;
-    y[DS_E * S] = ev;
 }
 
 // node tile of a group (its block plus 2 nodes on the + side): index of node (lx, ly, lz)
@@ -1289,10 +1309,10 @@ __device__ __forceinline__ void chunk_cells(const uint8_t* cellof, int cnt, int1
     }
 }
 
-// Right-hand side parts and the preconditioner's diagonal. Per chunk: the particles' coefficients (phase 1,
-// staged in shared memory with the fractional positions), then one thread per (in-block cell, x-offset) sums the
-// 9 (y, z) nodes over its cell's particles in registers (phase 2) and adds them to the group's shared node tile;
-// the tile goes to the node vectors CG_SA, CG_SV, CG_DIAG.
+// Right-hand side parts and the preconditioner's diagonal. Per chunk: the particles' scratch values staged in
+// shared memory (phase 1), then one thread per (in-block cell, x-offset) sums the 9 (y, z) nodes over its cell's
+// particles in registers (phase 2) and adds them to the group's shared node tile; the tile goes to the node
+// vectors CG_SA, CG_SV, CG_DIAG.
 template <class T>
 __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(StepArgs<T> a)
 {
@@ -1307,6 +1327,7 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
     __shared__ int32_t s_nbr[8];
     if (aborted_cta(a.st)) return;
     const KeyLayout kl = a.kl;
+    const int64_t S = a.pstride;
     const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
     for (int q = tid; q < 3 * TN; q += NT) tile[q] = (T)0;
@@ -1315,7 +1336,6 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
         uint32_t start, end;
         const int sc = dmg_claim<T>(a, &a.st->work_dmg, false, start, end, s_nbr, &s_g, &s_skip);
         if (sc < 0) break;
-        const SceneParams<T>& sp = a.scenes[sc];
         bool any = false;
         for (uint32_t c0 = start; c0 < end; c0 += CHUNK) {
             const int cnt = (int)min((uint32_t)CHUNK, end - c0);
@@ -1324,10 +1344,9 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
                 clast[tid] = 0;
             }
             for (int q = tid; q < cnt; q += NT) {
-                T v[D::NS];
-                dmg_prep_particle(a, sp, c0 + q, v);
+                const T* y = a.pay + pay_pos(c0 + q);
 #pragma unroll
-                for (int f = 0; f < D::NS; f++) st[f][q] = v[f];
+                for (int f = 0; f < D::NS; f++) st[f][q] = y[(DS_F + f) * S];
                 cellof[q] = (uint8_t)((kl.at(a.keys_sorted, c0 + q) >> kl.ib) & (NC - 1));
             }
             __syncthreads();
