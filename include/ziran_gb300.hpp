@@ -122,6 +122,9 @@ public:
     T apic_rpic_ratio = (T)1;
     T cfl = (T).6;
     int domain_cells = 0;
+    // AnisoFractureSimulation::implicit (AnisoFractureSimulation.h:59-70, the driver's --implicit_damage):
+    // solve the phase field implicitly; read at the first substep
+    bool implicit = false;
 
     MpmSimulation()
     {
@@ -189,6 +192,13 @@ public:
         return restarts;
     }
     int64_t particleCount() const { return zr_scene_count(h_); }
+    // conjugate-gradient iterations of the last substep's implicit damage solve
+    int cgIterations() const
+    {
+        int it = 0;
+        check(zr_scene_cg_iterations(h_, &it));
+        return it;
+    }
 
 private:
     friend class ParticleHandle<T>;
@@ -209,7 +219,10 @@ private:
             p.apic_rpic_ratio = apic_rpic_ratio;
             p.cfl = cfl;
             p.domain_cells = domain_cells;
-            if (zr_scene_set_params(h_, &p) == ZR_OK) return;
+            if (zr_scene_set_params(h_, &p) == ZR_OK) {
+                check(zr_scene_set_implicit_damage(h_, implicit ? 1 : 0));
+                return;
+            }
             pushed_ = true; // parameters froze at the first substep; later changes of dt go through set_dt
         }
         check(zr_scene_set_dt(h_, dt));

@@ -39,35 +39,39 @@ int main()
 
     // An AnisoMPM piece the way examples/tubepull.h builds one: QRStableNeoHookean with fibre stiffness
     // 10 mu along the material x axis and anisotropic damage, pulled apart by two sticky plates.
-    ziran_gb300::MpmSimulation<T> tear;
-    tear.dx = (T)1 / 128;
-    tear.dt = (T)5e-5;
-    tear.apic_rpic_ratio = 0;
-    tear.domain_cells = 132;
-    std::vector<double> xs, ms, vs, Fs;
-    const double h = 1.0 / 128, vh = h * h * h / 8;
-    for (int i = 0; i < 12; i++)
-        for (int j = 0; j < 4; j++)
-            for (int k = 0; k < 4; k++)
-                for (int s = 0; s < 8; s++) {
-                    int sub[3] = { s >> 2, (s >> 1) & 1, s & 1 }, c[3] = { 58 + i, 62 + j, 62 + k };
-                    for (int a = 0; a < 3; a++) xs.push_back((c[a] + (sub[a] + U(g)) * 0.5) * h);
-                    ms.push_back(800 * vh);
-                }
-    const size_t n2 = ms.size();
-    std::vector<double> V2(n2, vh);
-    ziran_gb300::QRStableNeoHookean<T> model(5e4f, 0.25f);
-    model.setExtraFiberStiffness(0, 10);
-    auto piece = tear.addParticles(xs, ms, V2);
-    piece.addFBasedMpmForce(model);
-    std::vector<T> sc(n2, model.getSigmaCrit((T)0.01));
-    piece.addFBasedMpmForceWithAnisotropicPhaseField((T)-1, (T)(0.5 * h), model, (T)0.1, (T)1, (T)0.01, sc);
-    tear.addCollisionObject(ziran_gb300::HalfSpace<T>{ { (T)(60 * h), 0, 0 }, { 1, 0, 0 } }, ziran_gb300::STICKY, 0, { (T)-1, 0, 0 });
-    tear.addCollisionObject(ziran_gb300::HalfSpace<T>{ { (T)(68 * h), 0, 0 }, { -1, 0, 0 } }, ziran_gb300::STICKY, 0, { (T)1, 0, 0 });
-    tear.advance(30);
-    std::vector<double> dmg = tear.field(ZR_FIELD_D);
-    double dmax = 0;
-    for (double v : dmg) dmax = v > dmax ? v : dmax;
-    std::printf("qr_particles %lld max_damage %.6f\n", (long long)tear.particleCount(), dmax);
+    // run twice: the explicit damage update, then AnisoFractureSimulation's implicit solve (sim.implicit)
+    for (int implicit = 0; implicit < 2; implicit++) {
+        ziran_gb300::MpmSimulation<T> tear;
+        tear.implicit = implicit != 0;
+        tear.dx = (T)1 / 128;
+        tear.dt = (T)5e-5;
+        tear.apic_rpic_ratio = 0;
+        tear.domain_cells = 132;
+        std::vector<double> xs, ms, vs, Fs;
+        const double h = 1.0 / 128, vh = h * h * h / 8;
+        for (int i = 0; i < 12; i++)
+            for (int j = 0; j < 4; j++)
+                for (int k = 0; k < 4; k++)
+                    for (int s = 0; s < 8; s++) {
+                        int sub[3] = { s >> 2, (s >> 1) & 1, s & 1 }, c[3] = { 58 + i, 62 + j, 62 + k };
+                        for (int a = 0; a < 3; a++) xs.push_back((c[a] + (sub[a] + U(g)) * 0.5) * h);
+                        ms.push_back(800 * vh);
+                    }
+        const size_t n2 = ms.size();
+        std::vector<double> V2(n2, vh);
+        ziran_gb300::QRStableNeoHookean<T> model(5e4f, 0.25f);
+        model.setExtraFiberStiffness(0, 10);
+        auto piece = tear.addParticles(xs, ms, V2);
+        piece.addFBasedMpmForce(model);
+        std::vector<T> sc(n2, model.getSigmaCrit((T)0.01));
+        piece.addFBasedMpmForceWithAnisotropicPhaseField((T)-1, (T)(0.5 * h), model, (T)0.1, (T)1, (T)0.01, sc);
+        tear.addCollisionObject(ziran_gb300::HalfSpace<T>{ { (T)(60 * h), 0, 0 }, { 1, 0, 0 } }, ziran_gb300::STICKY, 0, { (T)-1, 0, 0 });
+        tear.addCollisionObject(ziran_gb300::HalfSpace<T>{ { (T)(68 * h), 0, 0 }, { -1, 0, 0 } }, ziran_gb300::STICKY, 0, { (T)1, 0, 0 });
+        tear.advance(30);
+        std::vector<double> dmg = tear.field(ZR_FIELD_D);
+        double dmax = 0;
+        for (double v : dmg) dmax = v > dmax ? v : dmax;
+        std::printf("qr_particles %lld max_damage %.6f cg %d\n", (long long)tear.particleCount(), dmax, tear.cgIterations());
+    }
     return 0;
 }

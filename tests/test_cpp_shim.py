@@ -38,3 +38,6 @@ def test_shim_demo_runs(tmp_path):
     n2, dmax = int(out[7]), float(out[9])
     assert n2 == 12 * 4 * 4 * 8
     assert 0 < dmax <= 1
+    # the same piece with the implicit damage solve (sim.implicit = true): damage grows, the CG iterated
+    n3, dmax3, cg3 = int(out[13]), float(out[15]), int(out[17])
+    assert n3 == n2 and 0 < dmax3 <= 1 and cg3 > 0
