@@ -113,9 +113,10 @@ enum : uint32_t {
     FLAG_CAPACITY = 1u << 4, // active-block table or grid storage full
     FLAG_TIMEOUT = 1u << 5, // a bounded wait on a copy barrier gave up
     FLAG_CHECK = 1u << 6, // an internal consistency check failed (status.check_code says which); the access was skipped
+    FLAG_SORT = 1u << 7, // more particles changed cell than the incremental sort's mover buffer holds (the host grows it)
     FLAG_ABORT = 1u << 31, // processing stopped at status.abort_step; later substeps were no-ops
 };
-constexpr uint32_t ABORTING = FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_CAPACITY | FLAG_TIMEOUT | FLAG_CHECK;
+constexpr uint32_t ABORTING = FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_CAPACITY | FLAG_TIMEOUT | FLAG_CHECK | FLAG_SORT;
 
 struct DevStatus {
     uint32_t flags;
@@ -133,7 +134,7 @@ struct DevStatus {
     uint32_t work_dmg; // work counters of the implicit damage solve's group kernels
     uint32_t work_cg;
     uint32_t cg_loops; // iterations of the damage solve's loop in this substep (any scene)
-    uint32_t pad;
+    uint32_t max_movers; // most particles that changed cell in one substep (incremental sort)
 };
 
 constexpr int MAX_OBJECTS = 8;

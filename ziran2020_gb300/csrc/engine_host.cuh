@@ -133,7 +133,8 @@ public:
                 ZR_CUDA(cudaMemcpyAsync(grown_pid[0] + np[q].first, old_pid + src_first[q], 4 * np[q].count, cudaMemcpyDeviceToDevice, stream_));
             }
             ZR_CUDA(cudaStreamSynchronize(stream_));
-            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_, pay_ };
+            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_, pay_,
+                inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
             for (void* p : olds)
                 if (p) cudaFree(p);
             pool_[0] = grown_pool[0];
@@ -142,11 +143,18 @@ public:
             pid_[1] = grown_pid[1];
             cap_ = (uint64_t)cap;
             pay_ = nullptr;
+            inc_stay_ = inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
+            inc_cnt_ = nullptr;
             // P2G payload: NPAY fields of sorted particles at q + q/8, plus the copy granularity at the end
             pstride_ = (int64_t)((pay_pos((uint64_t)cap) + 64 + 63) & ~(uint64_t)63);
+            // keys_sorted_ (as 32-bit words) and vals_sorted_ take the incremental merge's n + mcap <= 2 cap items
             if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
-                || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_))
+                || alloc((void**)&vals_sorted_, 8 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_)
+                || alloc((void**)&inc_stay_, 4 * cap) || alloc((void**)&inc_move_, 4 * cap) || alloc((void**)&inc_mkeys_, 4 * cap)
+                || alloc((void**)&inc_mvals_, 4 * cap) || alloc((void**)&inc_mkeys2_, 4 * cap) || alloc((void**)&inc_mvals2_, 4 * cap)
+                || alloc((void**)&inc_cnt_, 16))
                 return ZR_ERR_CUDA_;
+            mcap_ = std::min<int64_t>(cap, std::max<int64_t>(MCAP_MIN, cap / 16));
             ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
             k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
             size_t sb = 0, sb32 = 0, se = 0;
@@ -154,6 +162,7 @@ public:
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb32, (uint32_t*)keys_in_, (uint32_t*)keys_sorted_, iota_, vals_sorted_, cap, 0, 32,
                 stream_));
             sb = std::max(sb, sb32); // the key width follows the batch: room for either
+            sb = std::max(sb, inc_sort_bytes(cap)); // and for the incremental sort's passes
             ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, (uint32_t*)nullptr, cap,
                 GroupHead{ keys_sorted_, kl }, stream_));
             sort_bytes_ = sb;
@@ -202,6 +211,7 @@ public:
         }
         tuned_ = false;
         sorted_storage_ = false;
+        sort_base_stale_ = true;
         ck_valid_ = false;
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         ZR_CUDA(cudaMemsetAsync(grid_mass_, 0, 8 * scene_cap_, stream_));
@@ -278,7 +288,7 @@ public:
             const int cur0 = cur_;
             int todo = target - done;
             if (!timing_ && graphs_on_) {
-                int rcg = prepare_graphs(todo);
+                int rcg = prepare_graphs(todo - (sort_base_stale_ ? 1 : 0));
                 if (rcg) return rcg;
             }
             ZR_CUDA(cudaEventRecord(t0_, stream_));
@@ -299,8 +309,17 @@ public:
                 cur_ = (cur0 + todo) & 1;
                 done += todo;
                 sorted_storage_ = true;
+                sort_base_stale_ = false;
+                // the mover buffer follows the movers seen: shrink to 4x the most seen when it is 16x too large
+                // (graphs are re-captured); a substep with more movers than it holds is repeated after growing it
+                const int64_t mm = (int64_t)hst_->max_movers;
+                if (inc_sort_usable() && todo >= 8 && mm > 0 && 16 * mm < mcap_ && mcap_ > MCAP_MIN) {
+                    mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(MCAP_MIN, 4 * mm));
+                    drop_graphs();
+                }
                 break;
             }
+            sort_base_stale_ = true; // the aborted substep's sort overwrote the base
             const int k = hst_->abort_step;
             done += k;
             cur_ = (cur0 + k) & 1;
@@ -313,6 +332,12 @@ public:
             k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
             ZR_CUDA(cudaStreamSynchronize(stream_));
             const uint32_t f = hst_->flags;
+            if ((f & FLAG_SORT) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK | FLAG_CAPACITY)) && mcap_ < (int64_t)cap_) {
+                const int64_t mm = (int64_t)hst_->max_movers;
+                mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(2 * mcap_, mm + mm / 2));
+                drop_graphs();
+                continue; // repeat the substep (a full sort) with room for more movers next time
+            }
             if ((f & FLAG_CAPACITY) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK)) && grow_rounds < 6) {
                 grow_rounds++;
                 int rc2 = alloc_grid(b_cap_ * 2);
@@ -656,6 +681,15 @@ private:
     bool tuned_ = false;
     bool fixed_schedule_ = false;
     bool sorted_storage_ = false; // particles sit in the sorted order of their last substep (after one G2P)
+    // incremental sort: keys_sorted_ holds the keys the current storage order was sorted by (false after state
+    // writes, aborts and autotuner trials: the next substep sorts in full)
+    bool sort_base_stale_ = true;
+    bool inc_sort_on_ = true; // ZR_SORT=full turns the incremental sort off
+    static constexpr int64_t MCAP_MIN = 4096;
+    // stayer indices; mover indices, keys and storage indices before and after their sort
+    uint32_t *inc_stay_ = nullptr, *inc_move_ = nullptr, *inc_mkeys_ = nullptr, *inc_mvals_ = nullptr, *inc_mkeys2_ = nullptr, *inc_mvals2_ = nullptr;
+    int64_t* inc_cnt_ = nullptr; // stayers, movers
+    int64_t mcap_ = 0; // movers the incremental sort takes per substep
     void *ck_pool_ = nullptr, *ck_pid_ = nullptr, *ck_scenes_ = nullptr; // device checkpoint
     uint64_t ck_cap_ = 0;
     size_t ck_scenes_n_ = 0;
@@ -681,6 +715,43 @@ private:
             return cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, keys_in_, keys_sorted_, iota_, vals_sorted_, n, 0, kl_.total(), stream_);
         return cub::DeviceRadixSort::SortPairs(sort_tmp_, sort_bytes_, (uint32_t*)keys_in_, (uint32_t*)keys_sorted_, iota_, vals_sorted_, n, 0,
             kl_.total(), stream_);
+    }
+
+    // temporary storage of the incremental sort's CUB passes for up to cap particles
+    size_t inc_sort_bytes(int64_t cap)
+    {
+        size_t a = 0, b = 0, c = 0;
+        auto keys = thrust::make_transform_iterator(inc_stay_, KeyOfIndex{ nullptr, 0 });
+        cub::DevicePartition::If(nullptr, a, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, cap,
+            KeptCell{ nullptr, nullptr }, AnyItem{}, stream_);
+        cub::DeviceRadixSort::SortPairs(nullptr, b, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, cap, 0, 32, stream_);
+        cub::DeviceMerge::MergePairs(nullptr, c, keys, inc_stay_, cap, inc_mkeys2_, inc_mvals2_, cap, (uint32_t*)keys_sorted_, vals_sorted_,
+            ::cuda::std::less<uint32_t>{}, stream_);
+        return std::max(a, std::max(b, c));
+    }
+    bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_stay_; }
+
+    // The sorted keys and storage indices of keys_in_ from the previous substep's sorted keys (keys_sorted_):
+    // split stayers / movers (one pass, both in storage order), pad the stayers and gather the movers' keys,
+    // sort the movers (stable), merge into keys_sorted_ / vals_sorted_ (n real items, then mcap padding).
+    cudaError_t sort_keys_incremental(int64_t n)
+    {
+        const uint32_t* nk = (const uint32_t*)keys_in_;
+        const uint32_t* ok = (const uint32_t*)keys_sorted_;
+        size_t tb = sort_bytes_;
+        cudaError_t e = cub::DevicePartition::If(sort_tmp_, tb, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, n,
+            KeptCell{ nk, ok }, AnyItem{}, stream_);
+        if (e != cudaSuccess) return e;
+        k_inc_prep<<<nsm_ * 4, 256, 0, stream_>>>(inc_stay_, inc_move_, nk, inc_mkeys_, inc_mvals_, inc_cnt_, n, mcap_, st_);
+        tb = sort_bytes_;
+        e = cub::DeviceRadixSort::SortPairs(sort_tmp_, tb, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, mcap_, 0, 32, stream_);
+        if (e != cudaSuccess) return e;
+        tb = sort_bytes_;
+        auto keys = thrust::make_transform_iterator(inc_stay_, KeyOfIndex{ nk, (uint32_t)n });
+        e = cub::DeviceMerge::MergePairs(sort_tmp_, tb, keys, inc_stay_, n, inc_mkeys2_, inc_mvals2_, mcap_, (uint32_t*)keys_sorted_, vals_sorted_,
+            ::cuda::std::less<uint32_t>{}, stream_);
+        if (e != cudaSuccess) return e;
+        return cudaGetLastError();
     }
 
     int params_from_desc(const SceneDesc& sdr, SceneParams<T>& sp)
@@ -836,6 +907,7 @@ private:
         sched_.scatter_ctas_per_sm = occ_scatter_[0];
         sched_.tuned = 0;
         if (const char* e = std::getenv("ZR_AUTOTUNE")) autotune_mode_ = std::atoi(e);
+        if (const char* e = std::getenv("ZR_SORT")) inc_sort_on_ = std::string(e) != "full";
     }
 
     int alloc(void** p, size_t bytes)
@@ -905,6 +977,7 @@ private:
     int rekey()
     {
         sorted_storage_ = false; // new positions: the storage order may no longer follow the cells
+        sort_base_stale_ = true;
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
         ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
@@ -960,12 +1033,15 @@ private:
 
     // Enqueue one substep reading buffer `parity`. With ev != nullptr, events are recorded between the
     // phases (sort+groups | activate | p2g | grid | g2p+end).
-    int enqueue_step(int parity, cudaEvent_t* ev)
+    int enqueue_step(int parity, cudaEvent_t* ev, bool full_sort = false)
     {
         StepArgs<T> a = args(parity);
         const int64_t n = N_;
         if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
-        ZR_CUDA(sort_keys(n));
+        if (full_sort || !inc_sort_usable())
+            ZR_CUDA(sort_keys(n));
+        else
+            ZR_CUDA(sort_keys_incremental(n));
         ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
@@ -1133,32 +1209,33 @@ private:
         }
     }
 
+    // Substeps from buffer cur_. The first one sorts in full when the sort base is stale; the others (and the
+    // captured graphs) sort incrementally.
     int launch_steps(int nsteps)
     {
-        if (timing_) {
-            if ((int)ev_.size() < 6 * nsteps) {
-                size_t old = ev_.size();
-                ev_.resize(6 * (size_t)nsteps);
-                for (size_t i = old; i < ev_.size(); i++) ZR_CUDA(cudaEventCreate(&ev_[i]));
-            }
-            for (int s = 0; s < nsteps; s++) {
-                int rc = enqueue_step((cur_ + s) & 1, &ev_[6 * (size_t)s]);
+        if (timing_ && (int)ev_.size() < 6 * nsteps) {
+            size_t old = ev_.size();
+            ev_.resize(6 * (size_t)nsteps);
+            for (size_t i = old; i < ev_.size(); i++) ZR_CUDA(cudaEventCreate(&ev_[i]));
+        }
+        int s0 = 0;
+        if (nsteps > 0 && sort_base_stale_) {
+            int rc = enqueue_step(cur_ & 1, timing_ ? &ev_[0] : nullptr, true);
+            if (rc) return rc;
+            s0 = 1;
+        }
+        if (timing_ || !graphs_on_) {
+            for (int s = s0; s < nsteps; s++) {
+                int rc = enqueue_step((cur_ + s) & 1, timing_ ? &ev_[6 * (size_t)s] : nullptr);
                 if (rc) return rc;
             }
             return 0;
         }
-        if (!graphs_on_) {
-            for (int s = 0; s < nsteps; s++) {
-                int rc = enqueue_step((cur_ + s) & 1, nullptr);
-                if (rc) return rc;
-            }
-            return 0;
-        }
-        int rc = prepare_graphs(nsteps);
+        int rc = prepare_graphs(nsteps - s0);
         if (rc) return rc;
-        int par = cur_;
-        int s = 0;
-        if (nsteps >= GRAPH_K)
+        int par = (cur_ + s0) & 1;
+        int s = s0;
+        if (nsteps - s0 >= GRAPH_K)
             for (; s + GRAPH_K <= nsteps; s += GRAPH_K) ZR_CUDA(cudaGraphLaunch(gk_[par], stream_)); // GRAPH_K even: parity unchanged
         for (; s < nsteps; s++) {
             ZR_CUDA(cudaGraphLaunch(g1_[par], stream_));
@@ -1273,7 +1350,8 @@ private:
             for (size_t i = old; i < ev_.size(); i++) ZR_CUDA(cudaEventCreate(&ev_[i]));
         }
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
-        int rc = enqueue_step(cur_, ev_.data());
+        int rc = enqueue_step(cur_, ev_.data(), sort_base_stale_);
+        sort_base_stale_ = true; // the trial's sort overwrote the base
         if (rc) return rc;
         ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
@@ -1410,7 +1488,8 @@ private:
     {
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
-            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_ };
+            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
+            inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1432,6 +1511,10 @@ private:
         cg_ = nullptr;
         cgs_ = nullptr;
         implicit_ = false;
+        inc_stay_ = inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
+        inc_cnt_ = nullptr;
+        mcap_ = 0;
+        sort_base_stale_ = true;
         scenes_backup_ = nullptr;
         scenes_backup_bytes_ = 0;
         ck_pool_ = ck_pid_ = ck_scenes_ = nullptr;

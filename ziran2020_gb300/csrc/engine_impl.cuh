@@ -29,6 +29,7 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 #include <thrust/iterator/counting_iterator.h>
+#include <thrust/iterator/transform_iterator.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -229,6 +230,53 @@ struct GroupHead {
     KeyLayout kl;
     __device__ bool operator()(uint32_t i) const { return i == 0 || kl.group(kl.at(k, i)) != kl.group(kl.at(k, i - 1)); }
 };
+
+// ---------------------------------------------------------------------------------------------------
+// Incremental sort (32-bit keys). The storage order is the previous substep's sorted order, so the particles
+// whose cell did not change ("stayers") are already sorted; only the particles that changed cell ("movers",
+// ~2% per substep at the slab's speeds) need sorting: partition the storage indices (both parts keep storage
+// order), sort the movers by key (stable), merge the two key-sorted sequences straight into the sorted keys and
+// indices. Particles of one cell may come out in another order than a full stable sort gives (a mover after the
+// cell's stayers); any order of a cell's particles is a valid binning.
+// ---------------------------------------------------------------------------------------------------
+struct KeptCell { // the new key equals the one the particle was sorted by in the previous substep
+    const uint32_t* knew;
+    const uint32_t* kold;
+    __host__ __device__ bool operator()(uint32_t i) const { return knew[i] == kold[i]; }
+};
+struct AnyItem {
+    __host__ __device__ bool operator()(uint32_t) const { return true; }
+};
+struct KeyOfIndex { // the key of a stayer; padding (index ~0, or any index past n) sorts last
+    const uint32_t* k;
+    uint32_t n;
+    __host__ __device__ uint32_t operator()(uint32_t i) const { return i < n ? k[i] : ~0u; }
+};
+
+// Pad the stayers to n indices and gather the movers' keys, padded to mcap items with the largest key (padding
+// merges and sorts last; real keys have at most 31 bits). More than mcap movers abort the substep with FLAG_SORT
+// (the host grows the buffer and repeats it with a full sort); the lists are then filled with padding only, so
+// the sort and merge that still run read no index.
+static __global__ void k_inc_prep(uint32_t* stay, const uint32_t* move_idx, const uint32_t* keys, uint32_t* move_keys, uint32_t* move_vals,
+    const int64_t* cnt, int64_t n, int64_t mcap, DevStatus* st)
+{
+    int64_t S = cnt[0], M = cnt[1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&st->max_movers, (uint32_t)(M >= 0 && M < 0xffffffffLL ? M : 0xffffffffLL));
+    if (S < 0 || M < 0 || S + M != n || M > mcap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise_flag(st, FLAG_SORT);
+        S = 0;
+        M = 0;
+    }
+    const int64_t lim = n > mcap ? n : mcap;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < lim; t += (int64_t)gridDim.x * blockDim.x) {
+        if (t >= S && t < n) stay[t] = ~0u;
+        if (t < mcap) {
+            const uint32_t i = t < M ? move_idx[t] : ~0u;
+            move_keys[t] = i < (uint64_t)n ? keys[i] : ~0u;
+            move_vals[t] = i;
+        }
+    }
+}
 
 template <class T>
 __global__ void k_activate(StepArgs<T> a)
