@@ -262,3 +262,34 @@ def test_qrnh_damage_update_matches_reference_formula(shim):
         phi = np.sum((A @ sp) * (sp @ A)) / sc ** 2
         want = min(d + dt / eta * max((1 - d) * zeta * max(phi - 1, 0) - (d - l0 * l0 * lap), 0), 1)
         assert abs(got - want) < 1e-10, t
+
+
+@pytest.mark.parametrize("alpha", [-1.0, 0.5, 2.0])
+def test_damage_drive_zero_bound_changes_nothing(shim, alpha):
+    """The drive skips the tensile split and the polar decomposition when max(1, (1+alpha)^2) |sigma|_F^2 is at
+    most 0.999 sigma_c^2 (then phi <= 1 exactly). Critical stresses straddling that bound within +-10% give the
+    reference formula's damage either way."""
+    rng = np.random.default_rng(21)
+    E, nu, l0, eta, zeta, k = 5e4, 0.25, 0.002, 0.1, 1.0, 0.01
+    skipped = computed = 0
+    for t in range(300):
+        F = np.ascontiguousarray(np.eye(3) + 0.01 * rng.normal(size=(3, 3)))
+        J = np.linalg.det(F)
+        S = tau_reference(1, E, nu, F, 1.0) / J
+        bound = max(1.0, (1 + alpha) ** 2) * np.sum(S * S)
+        sc = np.sqrt(bound / 0.999) * rng.uniform(0.9, 1.1)
+        d, lap, dt = rng.uniform(0, 0.5), rng.normal() * 100, 5e-5
+        got = shim.shim_damage(E, nu, alpha, l0, eta, zeta, k, p(F), d, lap, sc, dt)
+        w, Q = np.linalg.eigh((S + S.T) / 2)
+        sp = Q @ np.diag(np.maximum(w, 0)) @ Q.T
+        a = oracle_R(8, F)[:, 0]
+        A = np.eye(3) + alpha * np.outer(a, a)
+        phi = np.sum((A @ sp) * (sp @ A)) / sc ** 2
+        want = min(d + dt / eta * max((1 - d) * zeta * max(phi - 1, 0) - (d - l0 * l0 * lap), 0), 1)
+        assert abs(got - want) < 1e-10, (t, phi)
+        if bound <= 0.999 * sc * sc:
+            skipped += 1
+            assert phi <= 1.0
+        else:
+            computed += 1
+    assert skipped > 50 and computed > 50

@@ -356,76 +356,101 @@ public:
         return 0;
     }
 
-    int get_field(int s, int field, void* out, int f32) override
+    // Rows of scene s between the pool and a caller's row-major buffer (rf: which fields). A buffer in pinned host
+    // memory is read or written by the kernel itself over the host link; any other goes through the staging buffer
+    // with one copy. Synchronises.
+    int transfer_rows(int s, const RowFields& rf, void* host, int f32, bool exporting)
     {
-        int f0, nc;
-        if (!field_range(field, f0, nc)) return arg("unknown field");
-        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
         const int64_t n = h_scenes_[s].count;
-        int rc = ensure_stage((size_t)n * nc * (f32 ? 4 : 8));
-        if (rc) return rc;
-        if (f32)
-            k_export<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (float*)stage_, nc, 0);
-        else
-            k_export<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (double*)stage_, nc, 0);
-        ZR_CUDA(cudaMemcpyAsync(out, stage_, (size_t)n * nc * (f32 ? 4 : 8), cudaMemcpyDeviceToHost, stream_));
+        const size_t bytes = (size_t)n * rf.W * (f32 ? 4 : 8);
+        if (!inv_ || inv_cap_ < cap_) {
+            void* old = inv_;
+            dfree(old);
+            inv_ = nullptr;
+            inv_cap_ = 0;
+            if (alloc((void**)&inv_, 4 * (size_t)cap_)) return ZR_ERR_CUDA_;
+            inv_cap_ = cap_;
+        }
+        k_inv<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, inv_);
+        cudaPointerAttributes at;
+        void* dev = nullptr;
+        if (cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) dev = at.devicePointer;
+        cudaGetLastError(); // an unknown pointer only means: stage it
+        if (!dev) {
+            int rc = ensure_stage(bytes);
+            if (rc) return rc;
+            dev = stage_;
+            if (!exporting) ZR_CUDA(cudaMemcpyAsync(stage_, host, bytes, cudaMemcpyHostToDevice, stream_));
+        }
+        const int grid = (int)std::min<int64_t>((n + IO_ROWS - 1) / IO_ROWS, (int64_t)nsm_ * 16);
+        const size_t sm = (size_t)IO_ROWS * rf.W * (f32 ? 4 : 8);
+        if (grid > 0) {
+            if (f32) {
+                if (exporting)
+                    k_rows<T, float, true><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (float*)dev);
+                else
+                    k_rows<T, float, false><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (float*)dev);
+            }
+            else {
+                if (exporting)
+                    k_rows<T, double, true><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (double*)dev);
+                else
+                    k_rows<T, double, false><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (double*)dev);
+            }
+        }
+        ZR_CUDA(cudaGetLastError());
+        if (exporting && dev == stage_) ZR_CUDA(cudaMemcpyAsync(host, stage_, bytes, cudaMemcpyDeviceToHost, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
+    }
+    static RowFields state_fields()
+    {
+        RowFields rf{};
+        const int f0s[5] = { P_X, P_V, P_C, P_F, P_D }, ncs[5] = { 3, 3, 9, 9, 1 };
+        for (int q = 0; q < 5; q++) {
+            rf.f0[q] = f0s[q];
+            rf.nc[q] = ncs[q];
+        }
+        rf.count = 5;
+        rf.W = 25;
+        return rf;
+    }
+
+    int get_field(int s, int field, void* out, int f32) override
+    {
+        RowFields rf{};
+        if (!field_range(field, rf.f0[0], rf.nc[0])) return arg("unknown field");
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        rf.count = 1;
+        rf.W = rf.nc[0];
+        return transfer_rows(s, rf, out, f32, true);
     }
 
     int set_field(int s, int field, const void* in, int f32) override
     {
-        int f0, nc;
-        if (!field_range(field, f0, nc)) return arg("unknown field");
+        RowFields rf{};
+        if (!field_range(field, rf.f0[0], rf.nc[0])) return arg("unknown field");
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
-        const int64_t n = h_scenes_[s].count;
-        int rc = ensure_stage((size_t)n * nc * (f32 ? 4 : 8));
+        rf.count = 1;
+        rf.W = rf.nc[0];
+        int rc = transfer_rows(s, rf, const_cast<void*>(in), f32, false);
         if (rc) return rc;
-        ZR_CUDA(cudaMemcpyAsync(stage_, in, (size_t)n * nc * (f32 ? 4 : 8), cudaMemcpyHostToDevice, stream_));
-        if (f32)
-            k_import<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const float*)stage_, nc, 0);
-        else
-            k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0, nc, (const double*)stage_, nc, 0);
         if (field == FIELD_F || field == FIELD_SIGMA_C) ZR_CUDA(forget_drive(s));
         if (field == FIELD_X) return rekey();
-        ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
     }
 
     int get_state(int s, void* out, int f32) override
     {
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
-        const int64_t n = h_scenes_[s].count;
-        const size_t es = f32 ? 4 : 8;
-        int rc = ensure_stage((size_t)n * 25 * es);
-        if (rc) return rc;
-        const int f0s[5] = { P_X, P_V, P_C, P_F, P_D }, ncs[5] = { 3, 3, 9, 9, 1 }, offs[5] = { 0, 3, 6, 15, 24 };
-        for (int q = 0; q < 5; q++) {
-            if (f32)
-                k_export<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (float*)stage_, 25, offs[q]);
-            else
-                k_export<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (double*)stage_, 25, offs[q]);
-        }
-        ZR_CUDA(cudaMemcpyAsync(out, stage_, (size_t)n * 25 * es, cudaMemcpyDeviceToHost, stream_));
-        ZR_CUDA(cudaStreamSynchronize(stream_));
-        return 0;
+        return transfer_rows(s, state_fields(), out, f32, true);
     }
 
     int set_state(int s, const void* in, int f32) override
     {
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
-        const int64_t n = h_scenes_[s].count;
-        const size_t es = f32 ? 4 : 8;
-        int rc = ensure_stage((size_t)n * 25 * es);
+        int rc = transfer_rows(s, state_fields(), const_cast<void*>(in), f32, false);
         if (rc) return rc;
-        ZR_CUDA(cudaMemcpyAsync(stage_, in, (size_t)n * 25 * es, cudaMemcpyHostToDevice, stream_));
-        const int f0s[5] = { P_X, P_V, P_C, P_F, P_D }, ncs[5] = { 3, 3, 9, 9, 1 }, offs[5] = { 0, 3, 6, 15, 24 };
-        for (int q = 0; q < 5; q++) {
-            if (f32)
-                k_import<T, float><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (const float*)stage_, 25, offs[q]);
-            else
-                k_import<T, double><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, f0s[q], ncs[q], (const double*)stage_, 25, offs[q]);
-        }
         ZR_CUDA(forget_drive(s));
         return rekey();
     }
@@ -674,6 +699,8 @@ private:
     cudaStream_t side_ = nullptr; // captures the damage solve's loop body
     cudaGraphExec_t cg_exec_ = nullptr; // the damage solve's loop alone, for substeps launched outside graphs
     int occ_dmg_[2] = { 1, 1 };
+    uint32_t* inv_ = nullptr; // storage slot of each particle of a scene in the caller's order (row transfers)
+    uint64_t inv_cap_ = 0;
     T* pay_ = nullptr;
     int64_t pstride_ = 0;
     Schedule sched_{ 0, VAR_CHUNK[0], VAR_NBUF[0], 2, 128, 0, 0 };
@@ -977,7 +1004,8 @@ private:
     int rekey()
     {
         sorted_storage_ = false; // new positions: the storage order may no longer follow the cells
-        sort_base_stale_ = true;
+        // the sort base (keys_sorted_) stays a sorted array of the same keys' layout, which is all the incremental
+        // sort needs to be correct: particles whose key matches it at their slot form a sorted subsequence
         ZR_CUDA(cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_));
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
         ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
@@ -1489,7 +1517,7 @@ private:
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
             d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
-            inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
+            inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_, inv_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1514,6 +1542,8 @@ private:
         inc_stay_ = inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
         inc_cnt_ = nullptr;
         mcap_ = 0;
+        inv_ = nullptr;
+        inv_cap_ = 0;
         sort_base_stale_ = true;
         scenes_backup_ = nullptr;
         scenes_backup_bytes_ = 0;

@@ -1699,25 +1699,60 @@ __global__ void k_zero_grid_mass(double* gm, int n)
 // ---------------------------------------------------------------------------------------------------
 // host <-> device field transfer (caller order <-> storage order via the original index)
 // ---------------------------------------------------------------------------------------------------
-template <class T, class O>
-__global__ void k_export(Pool<T> p, int64_t first, int64_t n, int f0, int nc, O* out, int out_stride, int out_off)
+// Storage slot of every particle of a scene in the caller's order (inv[orig] = slot), for the row transfers.
+template <class T>
+__global__ void k_inv(Pool<T> p, int64_t first, int64_t n, uint32_t* inv)
 {
     using L = typename LayoutOf<T>::type;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = first + i;
-        const uint32_t orig = p.pid[s] & ((1u << L::index_bits) - 1);
-        for (int c = 0; c < nc; c++) out[(int64_t)orig * out_stride + out_off + c] = (O)p.f[(f0 + c) * p.stride + s];
+        const uint32_t orig = p.pid[first + i] & ((1u << L::index_bits) - 1);
+        if (orig < (uint64_t)n) inv[orig] = (uint32_t)(first + i);
     }
 }
 
-template <class T, class I>
-__global__ void k_import(Pool<T> p, int64_t first, int64_t n, int f0, int nc, const I* in, int in_stride, int in_off)
+// Field groups of a row transfer: rows of W = sum nc values in the caller's order, fields f0[k] .. f0[k]+nc[k]-1.
+struct RowFields {
+    int f0[8], nc[8], count, W;
+};
+constexpr int IO_ROWS = 128; // rows per CTA (one per thread)
+
+// Rows of a scene between the particle pool and a row-major buffer (host memory mapped into the device, or a
+// staging buffer). A CTA moves IO_ROWS consecutive rows: pool <-> shared memory per row (thread per row, slot from
+// inv), shared memory <-> buffer as one contiguous run of IO_ROWS * W values (coalesced, whole lines over the
+// host link).
+template <class T, class O, bool EXPORT>
+__global__ void __launch_bounds__(IO_ROWS) k_rows(Pool<T> p, const uint32_t* inv, int64_t n, RowFields rf, O* buf)
 {
-    using L = typename LayoutOf<T>::type;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = first + i;
-        const uint32_t orig = p.pid[s] & ((1u << L::index_bits) - 1);
-        for (int c = 0; c < nc; c++) p.f[(f0 + c) * p.stride + s] = (T)in[(int64_t)orig * in_stride + in_off + c];
+    extern __shared__ __align__(16) unsigned char rows_dyn[];
+    O* sm = reinterpret_cast<O*>(rows_dyn);
+    const int W = rf.W;
+    for (int64_t base = (int64_t)blockIdx.x * IO_ROWS; base < n; base += (int64_t)gridDim.x * IO_ROWS) {
+        const int rows = (int)min((int64_t)IO_ROWS, n - base);
+        O* run = buf + base * W;
+        if (!EXPORT) {
+            for (int q = threadIdx.x; q < rows * W; q += IO_ROWS) sm[q] = run[q];
+            __syncthreads();
+        }
+        if (threadIdx.x < rows) {
+            const uint32_t slot = inv[base + threadIdx.x];
+            O* r = sm + threadIdx.x * W;
+            int c0 = 0;
+            for (int k = 0; k < rf.count; k++) {
+                for (int c = 0; c < rf.nc[k]; c++) {
+                    T* f = p.f + (int64_t)(rf.f0[k] + c) * p.stride + slot;
+                    if (EXPORT)
+                        r[c0 + c] = (O)*f;
+                    else
+                        *f = (T)r[c0 + c];
+                }
+                c0 += rf.nc[k];
+            }
+        }
+        __syncthreads();
+        if (EXPORT) {
+            for (int q = threadIdx.x; q < rows * W; q += IO_ROWS) run[q] = sm[q];
+            __syncthreads();
+        }
     }
 }
 

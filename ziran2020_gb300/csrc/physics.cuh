@@ -545,8 +545,19 @@ ZR_HD T damage_drive(const Material<T>& mt, const T* F, T sigma_c, bool& fallbac
         tau_nhb(mt, F, (T)1, tau);
         invJ = (T)1 / det3(F);
     }
-    T S[9], sp[9];
-    for (int i = 0; i < 9; i++) S[i] = tau[i] * invJ; // undegraded Cauchy stress
+    T S[9], sp[9], s2 = 0;
+    for (int i = 0; i < 9; i++) {
+        S[i] = tau[i] * invJ; // undegraded Cauchy stress
+        s2 += S[i] * S[i];
+    }
+    // phi sigma_c^2 = tr((A sigma+)^2) <= |A|_2^2 |sigma+|_F^2 <= max(1, (1 + alpha)^2) |sigma|_F^2 (A = I + alpha a a^T
+    // with |a| = 1; sigma+ keeps a subset of sigma's eigenvalues). Below that bound, with a margin far above
+    // rounding, the drive is exactly zero: skip the eigen split and the polar decomposition.
+    const T ap1 = (T)1 + mt.alpha, anorm2 = ap1 * ap1 > (T)1 ? ap1 * ap1 : (T)1;
+    if (s2 * anorm2 <= (T)0.999 * sigma_c * sigma_c) {
+        fallback = false;
+        return (T)0;
+    }
     tension_part(S, sp); // sum of Macaulay-bracketed principal stresses times their projectors
     T R[9];
     fallback = polar_rotation(F, R);
