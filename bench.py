@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--eager", action="store_true", help="with --profile-only: launch kernels one at a time, not as graphs")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
     ap.add_argument("--schedule", default="auto",
                     help="auto (the autotuner), or fused:CTAS:G2P[:TIGHT], fused2:CTAS:G2P[:TIGHT] or split:CHUNK:BUFFERS:CTAS:G2P[:TIGHT] "
@@ -422,6 +423,8 @@ def run_ours(args, world, rank):
     s.from_recipe(r)
     apply_schedule(s, args.schedule)
     if args.profile_only:
+        if args.eager:  # substeps launched one kernel at a time (ncu lists no kernel of a graph holding a conditional loop)
+            s.set_timing(True)
         s.step(args.warmup)
         s.step(args.steps)
         g, b = s.last_grid()

@@ -1158,7 +1158,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
             Q.pid[i] = pid;
-            Q.f[P_MDT * Q.stride + i] = P.f[P_MDT * P.stride + j]; // the implicit damage solve's history travels with the particle
+            if (sp.implicit) Q.f[P_MDT * Q.stride + i] = P.f[P_MDT * P.stride + j]; // the implicit damage solve's history travels with the particle
             if (damage) {
                 // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
                 const uint32_t mat = pid >> L::index_bits;
