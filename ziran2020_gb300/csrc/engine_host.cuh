@@ -1104,7 +1104,7 @@ private:
                 launch_scatter<2>(a, sctas);
         }
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
-        k_grid<T><<<nsm_ * 8, 256, 0, stream_>>>(a);
+        k_grid<T><<<nsm_ * 8, GRID_NT, 0, stream_>>>(a);
         if (implicit_) {
             int rc = enqueue_damage_solve(a);
             if (rc) return rc;

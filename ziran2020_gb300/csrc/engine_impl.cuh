@@ -905,15 +905,21 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
 // ---------------------------------------------------------------------------------------------------
 // grid update
 // ---------------------------------------------------------------------------------------------------
+constexpr int GRID_NT = 256; // threads per CTA of the grid update
+
 template <class T>
-__global__ void k_grid(StepArgs<T> a)
+__global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
+    __shared__ double s_mass[GRID_NT / 32];
+    __shared__ int s_msc[GRID_NT / 32];
     if (aborted_cta(a.st)) return;
     const uint32_t B = min(a.st->n_blocks, a.b_cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_blocks_seen = max(a.st->max_blocks_seen, B);
     const uint32_t total = B * L::nodes;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ((total + 31) & ~31u); t += gridDim.x * blockDim.x) {
+    // every thread of the CTA runs the same iterations (the loop holds barriers)
+    for (uint32_t base = blockIdx.x * GRID_NT; base < total; base += gridDim.x * GRID_NT) {
+        const uint32_t t = base + threadIdx.x;
         T gm = 0;
         int scene = -1;
         if (t < total) {
@@ -949,11 +955,31 @@ __global__ void k_grid(StepArgs<T> a)
                 V[0] = V[L::nodes] = V[2 * L::nodes] = V[3 * L::nodes] = (T)0;
             }
         }
-        // grid mass per scene: nodes of one warp share a block (and so a scene) whenever L::nodes >= 32
+        // grid mass per scene: nodes of one warp share a block (and so a scene) whenever L::nodes >= 32; the
+        // CTA's warps then combine their sums, one atomic per run of warps of one scene (a single scene would
+        // otherwise send every warp's atomic to the same address)
         double s = (double)gm;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        int sc0 = __shfl_sync(0xffffffffu, scene, 0);
-        if ((threadIdx.x & 31) == 0 && sc0 >= 0) atomicAdd(&a.grid_mass[sc0], s);
+        const int sc0 = __shfl_sync(0xffffffffu, scene, 0);
+        if ((threadIdx.x & 31) == 0) {
+            s_mass[threadIdx.x >> 5] = s;
+            s_msc[threadIdx.x >> 5] = sc0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double run = 0;
+            int rsc = -1;
+            for (int w = 0; w < GRID_NT / 32; w++) {
+                if (s_msc[w] != rsc) {
+                    if (rsc >= 0 && run != 0.0) atomicAdd(&a.grid_mass[rsc], run);
+                    rsc = s_msc[w];
+                    run = 0;
+                }
+                run += s_mass[w];
+            }
+            if (rsc >= 0 && run != 0.0) atomicAdd(&a.grid_mass[rsc], run);
+        }
+        __syncthreads();
     }
     // the hash table is used only by activate and P2G: clear it for the next substep
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= a.h_mask; h += gridDim.x * blockDim.x) a.h_keys[h] = HASH_EMPTY;
