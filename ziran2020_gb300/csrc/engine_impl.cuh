@@ -478,14 +478,48 @@ __device__ inline void flush_column(T* dst, const T* src, int n)
     }
 }
 
+// Paired arithmetic: Blackwell issues two FP32 FMAs as one instruction on float2 operands (__ffma2_rn rounds each
+// lane as fmaf does). The accumulators of a (cell, x-offset) thread are kept as pairs so that every update of
+// two fields is one instruction; FP64 keeps scalar FMAs.
 template <class T>
-__device__ __forceinline__ void zero_acc(T (&acc)[9][NACC])
+struct PairOf;
+template <>
+struct PairOf<float> {
+    using type = float2;
+};
+template <>
+struct PairOf<double> {
+    using type = double2;
+};
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) { return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y)); }
+template <class P, class T>
+__device__ __forceinline__ P pmake(T x, T y)
 {
-#pragma unroll
-    for (int n = 0; n < 9; n++)
-#pragma unroll
-        for (int f = 0; f < NACC; f++) acc[n][f] = (T)0;
+    P r;
+    r.x = x;
+    r.y = y;
+    return r;
 }
+
+// The 9 nodes (jj, kk) x NACC fields of a (cell, stencil x-offset ii) thread, as pairs (p_x, p_y), (p_z, m), (d w, w)
+template <class T>
+struct NodeAcc {
+    using P = typename PairOf<T>::type;
+    P a[9][3];
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int n = 0; n < 9; n++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) a[n][k] = pmake<P>((T)0, (T)0);
+    }
+    // field f of node n: 0 mass, 1-3 momentum, 4 d w, 5 w (the accumulator order of the grid)
+    __device__ __forceinline__ T field(int n, int f) const
+    {
+        return f == 0 ? a[n][1].y : f == 1 ? a[n][0].x : f == 2 ? a[n][0].y : f == 3 ? a[n][1].x : f == 4 ? a[n][2].x : a[n][2].y;
+    }
+};
 
 // One particle's contribution to the 9 nodes (ii, jj, kk) of a (cell, stencil x-offset ii) thread; y points
 // at the particle's payload, fields STRIDE apart. Weights from the fractional position (BSplines.h:73-100).
@@ -493,8 +527,9 @@ __device__ __forceinline__ void zero_acc(T (&acc)[9][NACC])
 //   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
 //   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
 template <class T, int STRIDE>
-__device__ __forceinline__ void accumulate_particle(T (&acc)[9][NACC], const T* y, int ii, bool damage)
+__device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y, int ii, bool damage)
 {
+    using P = typename NodeAcc<T>::P;
     T w[3][3], dw[3][3];
 #pragma unroll
     for (int e = 0; e < 3; e++) {
@@ -531,25 +566,34 @@ __device__ __forceinline__ void accumulate_particle(T (&acc)[9][NACC], const T* 
             be[r] = c0 * B2[r];
             ga[r] = c0 * K2[r];
         }
-        const T mc = mass * c0, dc = dd * c0;
+        // (p_x, p_y) and (p_z, m): the mass lane takes wz_k m c0 and zero for the other two terms
+        const P AL0 = pmake<P>(al[0], al[1]), AL1 = pmake<P>(al[2], mass * c0);
+        const P BE0 = pmake<P>(be[0], be[1]), BE1 = pmake<P>(be[2], (T)0);
+        const P GA0 = pmake<P>(ga[0], ga[1]), GA1 = pmake<P>(ga[2], (T)0);
+        const P DW = pmake<P>(dd * c0, c0);
 #pragma unroll
         for (int kk = 0; kk < 3; kk++) {
             const T wk = w[2][kk], dwk = dw[2][kk];
-            T* ac = acc[jj * 3 + kk];
-            ac[0] += mc * wk;
-#pragma unroll
-            for (int r = 0; r < 3; r++) ac[1 + r] += wk * al[r] + (kk ? ((T)kk * wk) * be[r] : (T)0) + dwk * ga[r];
-            if (damage) {
-                ac[4] += dc * wk;
-                ac[5] += c0 * wk;
+            const P W = pmake<P>(wk, wk), DWK = pmake<P>(dwk, dwk);
+            P* ac = acc.a[jj * 3 + kk];
+            ac[0] = pfma(W, AL0, ac[0]);
+            ac[1] = pfma(W, AL1, ac[1]);
+            if (kk) {
+                const T kw = (T)kk * wk;
+                const P KW = pmake<P>(kw, kw);
+                ac[0] = pfma(KW, BE0, ac[0]);
+                ac[1] = pfma(KW, BE1, ac[1]);
             }
+            ac[0] = pfma(DWK, GA0, ac[0]);
+            ac[1] = pfma(DWK, GA1, ac[1]);
+            if (damage) ac[2] = pfma(W, DW, ac[2]);
         }
     }
 }
 
 // registers -> shared node tile of the block plus its +2 halo (distinct nodes within a warp: no contention)
 template <class T, class L>
-__device__ __forceinline__ void add_to_tile(const T (&acc)[9][NACC], T* tile, int cx, int cy, int cz, int ii, int nf)
+__device__ __forceinline__ void add_to_tile(const NodeAcc<T>& acc, T* tile, int cx, int cy, int cz, int ii, int nf)
 {
     constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
 #pragma unroll
@@ -557,10 +601,9 @@ __device__ __forceinline__ void add_to_tile(const T (&acc)[9][NACC], T* tile, in
 #pragma unroll
         for (int kk = 0; kk < 3; kk++) {
             T* t = tile + ((cx + ii) * TY + (cy + jj)) * TZ + (cz + kk);
-            const T* ac = acc[jj * 3 + kk];
 #pragma unroll
             for (int f = 0; f < NACC; f++)
-                if (f < nf) atomicAdd(t + f * TN, ac[f]);
+                if (f < nf) atomicAdd(t + f * TN, acc.field(jj * 3 + kk, f));
         }
 }
 
@@ -780,8 +823,8 @@ __global__ void __launch_bounds__(ScatterShape<T, CHUNK, NBUF>::NT, MIN_CTAS) k_
         const bool damage = nf == NACC;
         if ((fl & ITEM_LAST) && tid < 8) s_nbr[tid] = it.nbr[tid]; // read before this warp releases the item
         // per (cell, stencil x-offset): register accumulators of the thread's 9 nodes
-        T acc[9][NACC];
-        zero_acc(acc);
+        NodeAcc<T> acc;
+        acc.zero();
         // decided once: after the release below, faster warps may already mark the next chunk
         const bool mine = !(fl & ITEM_BAD) && ctag[b][c] == seq;
         if (mine) {
@@ -889,8 +932,8 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
             }
             __syncthreads();
             // ---- phases 2 and 3
-            T acc[9][NACC];
-            zero_acc(acc);
+            NodeAcc<T> acc;
+            acc.zero();
             const int qa = cfirst[c], qb = clast[c];
             for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD>(acc, pay + (q + (q >> 3)), ii, nf == NACC);
             if (qb > qa) add_to_tile<T, L>(acc, tile, cx, cy, cz, ii, nf);
@@ -1070,45 +1113,54 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             // and the APIC moment sum w v (x_i - x_p)^T = dx (M - pv fr^T) because x_i - x_p = (delta - fr) dx.
             T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0, pw = 0;
             const T* nv0 = tv + (l[0] * TY + l[1]) * TZ + l[2];
+            // the z and y sums run on pairs (two fields per instruction): velocity lanes (x, y) and (z, phase field)
+            using PT = typename PairOf<T>::type;
+            const PT Z = pmake<PT>((T)0, (T)0);
 #pragma unroll
             for (int ii = 0; ii < 3; ii++) {
-                T Si[3] = { 0, 0, 0 }, Ji[3] = { 0, 0, 0 }, Ki[3] = { 0, 0, 0 }, Ui[3] = { 0, 0, 0 }, Ti[3] = { 0, 0, 0 };
-                T lA = 0, lB = 0, lC = 0;
+                // (S_x, S_y) (S_z, lA) (U_x, U_y) (U_z, lB) (T_x, T_y) (T_z, lC) (K_x, K_y) (K_z, -) (J_x, J_y) (J_z, -)
+                PT S01 = Z, S2A = Z, U01 = Z, U2B = Z, T01 = Z, T2C = Z, K01 = Z, K2 = Z, J01 = Z, J2 = Z;
 #pragma unroll
                 for (int jj = 0; jj < 3; jj++) {
-                    T sj[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 }, pz = 0, p1 = 0;
+                    // (s_x, s_y) (s_z, pz) (t_x, t_y) (t_z, p1) (u_x, u_y) (u_z, -)
+                    PT s01 = Z, s2z = Z, t01 = Z, t2p = Z, u01 = Z, u2 = Z;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
                         const T* nv = nv0 + (ii * TY + jj) * TZ + kk;
                         const T wk = w[2][kk], dwk = dw[2][kk];
-#pragma unroll
-                        for (int r = 0; r < 3; r++) {
-                            const T vr = nv[r * TN];
-                            sj[r] += wk * vr;
-                            tj[r] += dwk * vr;
-                            if (kk) uj[r] += ((T)kk * wk) * vr;
-                        }
-                        if (damage) {
-                            const T pf = nv[3 * TN];
-                            pz += wk * pf;
-                            p1 += pf;
+                        const PT v01 = pmake<PT>(nv[0], nv[TN]), v2f = pmake<PT>(nv[2 * TN], damage ? nv[3 * TN] : (T)0);
+                        const PT W = pmake<PT>(wk, wk);
+                        s01 = pfma(W, v01, s01);
+                        s2z = pfma(W, v2f, s2z);
+                        t01 = pfma(pmake<PT>(dwk, dwk), v01, t01);
+                        t2p = pfma(pmake<PT>(dwk, (T)1), v2f, t2p);
+                        if (kk) {
+                            const T kw = (T)kk * wk;
+                            const PT KW = pmake<PT>(kw, kw);
+                            u01 = pfma(KW, v01, u01);
+                            u2 = pfma(KW, v2f, u2);
                         }
                     }
                     const T wj = w[1][jj], dwj = dw[1][jj];
-#pragma unroll
-                    for (int r = 0; r < 3; r++) {
-                        Si[r] += wj * sj[r];
-                        Ui[r] += dwj * sj[r];
-                        Ti[r] += wj * tj[r];
-                        Ki[r] += wj * uj[r];
-                        if (jj) Ji[r] += ((T)jj * wj) * sj[r];
-                    }
-                    if (damage) {
-                        lA += wj * pz;
-                        lB += pz;
-                        lC += wj * p1;
+                    const PT WJ = pmake<PT>(wj, wj);
+                    S01 = pfma(WJ, s01, S01);
+                    S2A = pfma(WJ, s2z, S2A);
+                    U01 = pfma(pmake<PT>(dwj, dwj), s01, U01);
+                    U2B = pfma(pmake<PT>(dwj, (T)1), s2z, U2B);
+                    T01 = pfma(WJ, t01, T01);
+                    T2C = pfma(WJ, t2p, T2C);
+                    K01 = pfma(WJ, u01, K01);
+                    K2 = pfma(WJ, u2, K2);
+                    if (jj) {
+                        const T jw = (T)jj * wj;
+                        const PT JW = pmake<PT>(jw, jw);
+                        J01 = pfma(JW, s01, J01);
+                        J2 = pfma(JW, s2z, J2);
                     }
                 }
+                const T Si[3] = { S01.x, S01.y, S2A.x }, Ui[3] = { U01.x, U01.y, U2B.x }, Ti[3] = { T01.x, T01.y, T2C.x };
+                const T Ki[3] = { K01.x, K01.y, K2.x }, Ji[3] = { J01.x, J01.y, J2.x };
+                const T lA = S2A.y, lB = U2B.y, lC = T2C.y;
                 const T wi = w[0][ii], dwi = dw[0][ii];
 #pragma unroll
                 for (int r = 0; r < 3; r++) {
