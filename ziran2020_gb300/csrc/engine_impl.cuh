@@ -1041,7 +1041,13 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
     constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
     __shared__ T tv[NVEL * TN];
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
+    __shared__ uint16_t s_map[TN]; // tile node -> (neighbour block 0-7) << 8 | element in that block
     if (aborted_cta(a.st)) return;
+    for (int node = threadIdx.x; node < TN; node += NT) {
+        const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
+        const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+        s_map[node] = (uint16_t)(((ax * 4 + ay * 2 + az) << 8) | L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz));
+    }
     const uint32_t G = a.st->n_groups;
     const KeyLayout kl = a.kl;
     for (;;) {
@@ -1063,15 +1069,13 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             }
         }
         __syncthreads();
-        // stage the tile from the 8 neighbouring blocks
-        for (int q = threadIdx.x; q < NVEL * TN; q += NT) {
-            const int f = q / TN, node = q % TN;
-            const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
-            const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
-            const int slot = s_nbr[ax * 4 + ay * 2 + az];
-            tv[q] = (slot >= 0 && (uint32_t)slot < a.b_cap)
-                ? a.vel[((size_t)slot * NVEL + f) * L::nodes + L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)]
-                : (T)0;
+        // stage the tile from the 8 neighbouring blocks (s_map was built before the first barrier)
+        for (int node = threadIdx.x; node < TN; node += NT) {
+            const int m = s_map[node], slot = s_nbr[m >> 8];
+            const bool ok = slot >= 0 && (uint32_t)slot < a.b_cap;
+            const T* src = a.vel + (size_t)(ok ? slot : 0) * NVEL * L::nodes + (m & 0xff);
+#pragma unroll
+            for (int f = 0; f < NVEL; f++) tv[f * TN + node] = ok ? src[f * L::nodes] : (T)0;
         }
         __syncthreads();
         const SceneParams<T>& sp = a.scenes[s_scene];
@@ -1231,7 +1235,11 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                     flags |= FLAG_OUT_OF_DOMAIN;
                     nb[0] = nb[1] = nb[2] = 0;
                 }
-                kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
+                // a particle that stays in its cell keeps the key it was sorted by
+                if (nb[0] == b[0] && nb[1] == b[1] && nb[2] == b[2])
+                    kl.put(a.keys_next, i, kl.at(a.keys_sorted, i));
+                else
+                    kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
             }
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
