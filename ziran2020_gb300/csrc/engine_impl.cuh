@@ -526,8 +526,8 @@ struct NodeAcc {
 // Node (ii, jj, kk) receives, per momentum component r,
 //   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
 //   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
-template <class T, int STRIDE>
-__device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y, int ii, bool damage)
+template <class T, int STRIDE, bool DAMAGE>
+__device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y, int ii)
 {
     using P = typename NodeAcc<T>::P;
     T w[3][3], dw[3][3];
@@ -545,7 +545,7 @@ __device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y,
     const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
     const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
     const T mass = y[Y_M * STRIDE];
-    const T dd = y[Y_D * STRIDE];
+    const T dd = DAMAGE ? y[Y_D * STRIDE] : (T)0;
     T Ai[3], B1[3], B2[3], K0[3], K1[3], K2[3];
 #pragma unroll
     for (int r = 0; r < 3; r++) {
@@ -586,7 +586,7 @@ __device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y,
             }
             ac[0] = pfma(DWK, GA0, ac[0]);
             ac[1] = pfma(DWK, GA1, ac[1]);
-            if (damage) ac[2] = pfma(W, DW, ac[2]);
+            if (DAMAGE) ac[2] = pfma(W, DW, ac[2]);
         }
     }
 }
@@ -829,7 +829,10 @@ __global__ void __launch_bounds__(ScatterShape<T, CHUNK, NBUF>::NT, MIN_CTAS) k_
         const bool mine = !(fl & ITEM_BAD) && ctag[b][c] == seq;
         if (mine) {
             const uint32_t qa = q0 + cfirst[b][c], qb = q0 + clast[b][c];
-            for (uint32_t q = qa; q < qb; q++) accumulate_particle<T, WIN>(acc, buf + (pay_pos(q) - base), ii, damage);
+            if (damage)
+                for (uint32_t q = qa; q < qb; q++) accumulate_particle<T, WIN, true>(acc, buf + (pay_pos(q) - base), ii);
+            else
+                for (uint32_t q = qa; q < qb; q++) accumulate_particle<T, WIN, false>(acc, buf + (pay_pos(q) - base), ii);
         }
         // the chunk's payload is no longer needed: release the buffer (and the item) to the producer
         __syncwarp();
@@ -935,7 +938,10 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
             NodeAcc<T> acc;
             acc.zero();
             const int qa = cfirst[c], qb = clast[c];
-            for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD>(acc, pay + (q + (q >> 3)), ii, nf == NACC);
+            if (nf == NACC)
+                for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, true>(acc, pay + (q + (q >> 3)), ii);
+            else
+                for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, false>(acc, pay + (q + (q >> 3)), ii);
             if (qb > qa) add_to_tile<T, L>(acc, tile, cx, cy, cz, ii, nf);
             __syncthreads();
         }
