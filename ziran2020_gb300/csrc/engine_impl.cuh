@@ -492,6 +492,11 @@ struct PairOf<double> {
     using type = double2;
 };
 __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// four values of one grid node read with one shared-memory access (velocity x, y, z and the phase field)
+template <class T>
+struct alignas(4 * sizeof(T)) Quad {
+    T x, y, z, w;
+};
 __device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) { return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y)); }
 template <class P, class T>
 __device__ __forceinline__ P pmake(T x, T y)
@@ -1045,7 +1050,8 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
     // the grid velocities around the group's block as one dense node tile (the block plus 2 nodes on the
     // + side of every axis, the reach of the quadratic stencil): every stencil read is a fixed offset
     constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
-    __shared__ T tv[NVEL * TN];
+    static_assert(NVEL == 4, "one Quad per tile node");
+    __shared__ Quad<T> tq[TN]; // node-major: the 4 fields of a node in one access
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
     __shared__ uint16_t s_map[TN]; // tile node -> (neighbour block 0-7) << 8 | element in that block
     if (aborted_cta(a.st)) return;
@@ -1080,8 +1086,12 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             const int m = s_map[node], slot = s_nbr[m >> 8];
             const bool ok = slot >= 0 && (uint32_t)slot < a.b_cap;
             const T* src = a.vel + (size_t)(ok ? slot : 0) * NVEL * L::nodes + (m & 0xff);
-#pragma unroll
-            for (int f = 0; f < NVEL; f++) tv[f * TN + node] = ok ? src[f * L::nodes] : (T)0;
+            Quad<T> qv;
+            qv.x = ok ? src[0] : (T)0;
+            qv.y = ok ? src[L::nodes] : (T)0;
+            qv.z = ok ? src[2 * L::nodes] : (T)0;
+            qv.w = ok ? src[3 * L::nodes] : (T)0;
+            tq[node] = qv;
         }
         __syncthreads();
         const SceneParams<T>& sp = a.scenes[s_scene];
@@ -1122,7 +1132,7 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             //   pv = sum w v,  M_rc = sum w v_r delta_c,  G_rc = sum v_r (grad w)_c dx,
             // and the APIC moment sum w v (x_i - x_p)^T = dx (M - pv fr^T) because x_i - x_p = (delta - fr) dx.
             T pv[3] = { 0, 0, 0 }, M[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, Gv[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 }, lap = 0, pw = 0;
-            const T* nv0 = tv + (l[0] * TY + l[1]) * TZ + l[2];
+            const Quad<T>* nq0 = tq + (l[0] * TY + l[1]) * TZ + l[2];
             // the z and y sums run on pairs (two fields per instruction): velocity lanes (x, y) and (z, phase field)
             using PT = typename PairOf<T>::type;
             const PT Z = pmake<PT>((T)0, (T)0);
@@ -1136,9 +1146,9 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                     PT s01 = Z, s2z = Z, t01 = Z, t2p = Z, u01 = Z, u2 = Z;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
-                        const T* nv = nv0 + (ii * TY + jj) * TZ + kk;
+                        const Quad<T> nv = nq0[(ii * TY + jj) * TZ + kk];
                         const T wk = w[2][kk], dwk = dw[2][kk];
-                        const PT v01 = pmake<PT>(nv[0], nv[TN]), v2f = pmake<PT>(nv[2 * TN], damage ? nv[3 * TN] : (T)0);
+                        const PT v01 = pmake<PT>(nv.x, nv.y), v2f = pmake<PT>(nv.z, damage ? nv.w : (T)0);
                         const PT W = pmake<PT>(wk, wk);
                         s01 = pfma(W, v01, s01);
                         s2z = pfma(W, v2f, s2z);
