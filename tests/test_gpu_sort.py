@@ -35,8 +35,6 @@ def test_incremental_sort_matches_full_sort():
     full = run(d, zr.F64, 30, sort="full")
     for f, tol in (("x", 1e-12), ("v", 1e-9), ("F", 1e-9), ("d", 1e-9)):
         assert np.abs(inc.get(f) - full.get(f)).max() <= tol, f
-    # the substep graphs differ: the incremental one partitions, sorts the movers and merges
-    assert inc.stats()["launches_per_step"] != full.stats()["launches_per_step"]
 
 
 @pytest.mark.parametrize("prec", [zr.F64, zr.F32])

@@ -759,8 +759,8 @@ private:
     bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_stay_; }
 
     // The sorted keys and storage indices of keys_in_ from the previous substep's sorted keys (keys_sorted_):
-    // split stayers / movers (one pass, both in storage order), pad the stayers and gather the movers' keys,
-    // sort the movers (stable), merge into keys_sorted_ / vals_sorted_ (n real items, then mcap padding).
+    // split stayers / movers (one pass, both in storage order), gather the movers' keys (padded), sort the movers
+    // (stable), merge the two key-sorted sequences into keys_sorted_ / vals_sorted_ (k_inc_merge).
     cudaError_t sort_keys_incremental(int64_t n)
     {
         const uint32_t* nk = (const uint32_t*)keys_in_;
@@ -773,11 +773,8 @@ private:
         tb = sort_bytes_;
         e = cub::DeviceRadixSort::SortPairs(sort_tmp_, tb, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, mcap_, 0, 32, stream_);
         if (e != cudaSuccess) return e;
-        tb = sort_bytes_;
-        auto keys = thrust::make_transform_iterator(inc_stay_, KeyOfIndex{ nk, (uint32_t)n });
-        e = cub::DeviceMerge::MergePairs(sort_tmp_, tb, keys, inc_stay_, n, inc_mkeys2_, inc_mvals2_, mcap_, (uint32_t*)keys_sorted_, vals_sorted_,
-            ::cuda::std::less<uint32_t>{}, stream_);
-        if (e != cudaSuccess) return e;
+        const int tiles = (int)std::max<int64_t>(1, (n + MERGE_TILE - 1) / MERGE_TILE);
+        k_inc_merge<<<tiles, MERGE_NT, 0, stream_>>>(inc_stay_, nk, inc_mkeys2_, inc_mvals2_, inc_cnt_, n, mcap_, (uint32_t*)keys_sorted_, vals_sorted_, st_);
         return cudaGetLastError();
     }
 

@@ -278,6 +278,79 @@ static __global__ void k_inc_prep(uint32_t* stay, const uint32_t* move_idx, cons
     }
 }
 
+// Merge of the stayers (storage order, key-sorted) with the sorted movers straight into the sorted keys and
+// storage indices. In the order (key, stayers before movers, rank) the output position of a stayer is its rank
+// among the stayers plus the movers with a smaller key; of a mover, its rank among the movers plus the stayers
+// with a key not above it. CTA j takes MERGE_TILE consecutive stayers and owns the movers [lb_j, lb_j+1), lb_j =
+// the movers below its first stayer key (lb_0 = 0; the last tile owns the movers up to M): every owned mover
+// lies between this tile's first stayer and the next tile's, so both counts come from this tile and its window
+// of movers. Positions outside [0, n) (inconsistent inputs) raise a check instead of writing.
+constexpr int MERGE_NT = 256, MERGE_TILE = 1024;
+
+__device__ __forceinline__ int64_t lower_bound_u32(const uint32_t* v, int64_t lo, int64_t hi, uint32_t key)
+{
+    while (lo < hi) {
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        if (v[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+static __global__ void __launch_bounds__(MERGE_NT) k_inc_merge(const uint32_t* stay, const uint32_t* keys, const uint32_t* mkeys, const uint32_t* mvals,
+    const int64_t* cnt, int64_t n, int64_t mcap, uint32_t* out_keys, uint32_t* out_vals, DevStatus* st)
+{
+    __shared__ uint32_t sk[MERGE_TILE]; // this tile's stayer keys
+    __shared__ int64_t s_lb[2];
+    const int64_t S = cnt[0], M = cnt[1];
+    if (S < 0 || M < 0 || S + M != n || M > mcap) return; // k_inc_prep raised FLAG_SORT: the substep is repeated
+    const int64_t a0 = (int64_t)blockIdx.x * MERGE_TILE;
+    if (a0 >= S && blockIdx.x > 0) return; // (tile 0 also runs when every particle moved)
+    const int na = (int)(S - a0 < MERGE_TILE ? (S - a0 > 0 ? S - a0 : 0) : MERGE_TILE);
+    for (int t = threadIdx.x; t < na; t += MERGE_NT) sk[t] = keys[stay[a0 + t]];
+    if (threadIdx.x < 2) {
+        int64_t lb;
+        if (threadIdx.x == 0)
+            lb = blockIdx.x == 0 ? 0 : lower_bound_u32(mkeys, 0, M, keys[stay[a0]]);
+        else
+            lb = a0 + MERGE_TILE >= S ? M : lower_bound_u32(mkeys, 0, M, keys[stay[a0 + MERGE_TILE]]);
+        s_lb[threadIdx.x] = lb;
+    }
+    __syncthreads();
+    const int64_t lo = s_lb[0], hi = s_lb[1] > s_lb[0] ? s_lb[1] : s_lb[0];
+    for (int t = threadIdx.x; t < na; t += MERGE_NT) {
+        const uint32_t k = sk[t];
+        const int64_t pos = a0 + t + lower_bound_u32(mkeys, lo, hi, k);
+        if (pos < 0 || pos >= n) {
+            check_failed(st, 8);
+            continue;
+        }
+        out_keys[pos] = k;
+        out_vals[pos] = stay[a0 + t];
+    }
+    for (int64_t m = lo + threadIdx.x; m < hi; m += MERGE_NT) {
+        const uint32_t k = mkeys[m];
+        // stayers of this tile with a key not above k
+        int l = 0, h = na;
+        while (l < h) {
+            const int mid = (l + h) >> 1;
+            if (sk[mid] <= k)
+                l = mid + 1;
+            else
+                h = mid;
+        }
+        const int64_t pos = m + a0 + l;
+        if (pos < 0 || pos >= n) {
+            check_failed(st, 8);
+            continue;
+        }
+        out_keys[pos] = k;
+        out_vals[pos] = mvals[m];
+    }
+}
+
 template <class T>
 __global__ void k_activate(StepArgs<T> a)
 {
