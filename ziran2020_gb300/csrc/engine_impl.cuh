@@ -299,6 +299,23 @@ __device__ __forceinline__ int64_t lower_bound_u32(const uint32_t* v, int64_t lo
     return lo;
 }
 
+// lower bound of key in the sorted v[lo, hi) by a whole warp: 32 probes per step narrow the range 32-fold, so a
+// search over 2^17 values takes four dependent loads instead of seventeen. Every lane must call it.
+__device__ __forceinline__ int64_t warp_lower_bound(const uint32_t* v, int64_t lo, int64_t hi, uint32_t key)
+{
+    const int lane = threadIdx.x & 31;
+    while (hi - lo > 32) { // the answer lies in [lo, hi]
+        const int64_t step = (hi - lo + 31) / 32, p = lo + lane * step;
+        const int c = __popc(__ballot_sync(0xffffffffu, p < hi && v[p] < key)); // probes below the answer
+        const int64_t nlo = c == 0 ? lo : lo + (int64_t)(c - 1) * step + 1;
+        const int64_t nhi = c == 32 ? hi : (lo + (int64_t)c * step < hi ? lo + (int64_t)c * step : hi);
+        lo = nlo;
+        hi = nhi;
+    }
+    const int64_t p = lo + lane;
+    return lo + __popc(__ballot_sync(0xffffffffu, p < hi && v[p] < key));
+}
+
 static __global__ void __launch_bounds__(MERGE_NT) k_inc_merge(const uint32_t* stay, const uint32_t* keys, const uint32_t* mkeys, const uint32_t* mvals,
     const int64_t* cnt, int64_t n, int64_t mcap, uint32_t* out_keys, uint32_t* out_vals, DevStatus* st)
 {
@@ -310,13 +327,14 @@ static __global__ void __launch_bounds__(MERGE_NT) k_inc_merge(const uint32_t* s
     if (a0 >= S && blockIdx.x > 0) return; // (tile 0 also runs when every particle moved)
     const int na = (int)(S - a0 < MERGE_TILE ? (S - a0 > 0 ? S - a0 : 0) : MERGE_TILE);
     for (int t = threadIdx.x; t < na; t += MERGE_NT) sk[t] = keys[stay[a0 + t]];
-    if (threadIdx.x < 2) {
+    const int warp = threadIdx.x >> 5;
+    if (warp < 2) { // warp 0: this tile's first mover, warp 1: the next tile's (both warp-uniform branches)
         int64_t lb;
-        if (threadIdx.x == 0)
-            lb = blockIdx.x == 0 ? 0 : lower_bound_u32(mkeys, 0, M, keys[stay[a0]]);
+        if (warp == 0)
+            lb = blockIdx.x == 0 ? 0 : warp_lower_bound(mkeys, 0, M, keys[stay[a0]]);
         else
-            lb = a0 + MERGE_TILE >= S ? M : lower_bound_u32(mkeys, 0, M, keys[stay[a0 + MERGE_TILE]]);
-        s_lb[threadIdx.x] = lb;
+            lb = a0 + MERGE_TILE >= S ? M : warp_lower_bound(mkeys, 0, M, keys[stay[a0 + MERGE_TILE]]);
+        if ((threadIdx.x & 31) == 0) s_lb[warp] = lb;
     }
     __syncthreads();
     const int64_t lo = s_lb[0], hi = s_lb[1] > s_lb[0] ? s_lb[1] : s_lb[0];
