@@ -54,7 +54,7 @@ def test_budget_bounds_the_resident_set_and_refuses_oversized_requests():
     rng = np.random.default_rng(5)
     reqs = [(workloads.elastic_family(rng, 8000), 12) for _ in range(6)]  # equal sizes: the bound is exact
     n = zr.recipe_count(reqs[0][0])
-    per_scene = n * (2 * (30 * 4 + 4) + 28 + 27 * 4 * 9 / 8 + 40) + 8 * (n / 256 + 64) * (10 * 64 * 4 + 64)  # the server's estimate
+    per_scene = n * (2 * (30 * 4 + 4) + 28 + 27 * 4 * 9 / 8 + 24) + 8 * (n / 256 + 64) * (10 * 64 * 4 + 64)  # the server's estimate
     sv = zr.Server(zr.F32, budget_bytes=2.5 * per_scene, tick_substeps=5, max_scenes=64)
     for r, steps in reqs:
         sv.submit(r, steps)

@@ -1145,8 +1145,8 @@ double scene_bytes(int precision, int64_t n)
 {
     const double s = precision == ZR_F64 ? 8 : 4, nodes = precision == ZR_F64 ? 32 : 64;
     // two pool copies (30 fields and the id), keys (in, sorted), sort values, iota, group starts, the P2G payload
-    // (27 fields at 9/8 density) and the incremental sort's stayers, movers, sorted movers and merged items
-    const double per_particle = 2 * (30 * s + 4) + 8 + 8 + 4 + 4 + 4 + 27 * s * 9 / 8 + 8 + 8 + 8 + 16;
+    // (27 fields at 9/8 density) and the incremental sort's six index and key lists
+    const double per_particle = 2 * (30 * s + 4) + 8 + 8 + 4 + 4 + 4 + 27 * s * 9 / 8 + 6 * 4;
     const double groups = (double)n / (nodes * 4) + 64;
     return n * per_particle + 8 * groups * (10 * nodes * s + 64);
 }

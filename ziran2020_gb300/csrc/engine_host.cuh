@@ -147,14 +147,13 @@ public:
             inc_cnt_ = nullptr;
             // P2G payload: NPAY fields of sorted particles at q + q/8, plus the copy granularity at the end
             pstride_ = (int64_t)((pay_pos((uint64_t)cap) + 64 + 63) & ~(uint64_t)63);
-            // keys_sorted_ (as 32-bit words) and vals_sorted_ take the incremental merge's n + mcap <= 2 cap items
             if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
-                || alloc((void**)&vals_sorted_, 8 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_)
+                || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_)
                 || alloc((void**)&inc_stay_, 4 * cap) || alloc((void**)&inc_move_, 4 * cap) || alloc((void**)&inc_mkeys_, 4 * cap)
                 || alloc((void**)&inc_mvals_, 4 * cap) || alloc((void**)&inc_mkeys2_, 4 * cap) || alloc((void**)&inc_mvals2_, 4 * cap)
                 || alloc((void**)&inc_cnt_, 16))
                 return ZR_ERR_CUDA_;
-            mcap_ = std::min<int64_t>(cap, std::max<int64_t>(MCAP_MIN, cap / 16));
+            mcap_ = std::min<int64_t>(cap, std::max<int64_t>(MCAP_MIN, cap / 32));
             ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
             k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
             size_t sb = 0, sb32 = 0, se = 0;
@@ -310,11 +309,11 @@ public:
                 done += todo;
                 sorted_storage_ = true;
                 sort_base_stale_ = false;
-                // the mover buffer follows the movers seen: shrink to 4x the most seen when it is 16x too large
+                // the mover buffer follows the movers seen: shrink to 3x the most seen when it is 8x too large
                 // (graphs are re-captured); a substep with more movers than it holds is repeated after growing it
                 const int64_t mm = (int64_t)hst_->max_movers;
-                if (inc_sort_usable() && todo >= 8 && mm > 0 && 16 * mm < mcap_ && mcap_ > MCAP_MIN) {
-                    mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(MCAP_MIN, 4 * mm));
+                if (inc_sort_usable() && todo >= 8 && mm > 0 && 8 * mm < mcap_ && mcap_ > MCAP_MIN) {
+                    mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(MCAP_MIN, 3 * mm));
                     drop_graphs();
                 }
                 break;
@@ -747,14 +746,11 @@ private:
     // temporary storage of the incremental sort's CUB passes for up to cap particles
     size_t inc_sort_bytes(int64_t cap)
     {
-        size_t a = 0, b = 0, c = 0;
-        auto keys = thrust::make_transform_iterator(inc_stay_, KeyOfIndex{ nullptr, 0 });
+        size_t a = 0, b = 0;
         cub::DevicePartition::If(nullptr, a, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, cap,
             KeptCell{ nullptr, nullptr }, AnyItem{}, stream_);
         cub::DeviceRadixSort::SortPairs(nullptr, b, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, cap, 0, 32, stream_);
-        cub::DeviceMerge::MergePairs(nullptr, c, keys, inc_stay_, cap, inc_mkeys2_, inc_mvals2_, cap, (uint32_t*)keys_sorted_, vals_sorted_,
-            ::cuda::std::less<uint32_t>{}, stream_);
-        return std::max(a, std::max(b, c));
+        return std::max(a, b);
     }
     bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_stay_; }
 
@@ -769,7 +765,7 @@ private:
         cudaError_t e = cub::DevicePartition::If(sort_tmp_, tb, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, n,
             KeptCell{ nk, ok }, AnyItem{}, stream_);
         if (e != cudaSuccess) return e;
-        k_inc_prep<<<nsm_ * 4, 256, 0, stream_>>>(inc_stay_, inc_move_, nk, inc_mkeys_, inc_mvals_, inc_cnt_, n, mcap_, st_);
+        k_inc_prep<<<nsm_ * 4, 256, 0, stream_>>>(inc_move_, nk, inc_mkeys_, inc_mvals_, inc_cnt_, n, mcap_, st_);
         tb = sort_bytes_;
         e = cub::DeviceRadixSort::SortPairs(sort_tmp_, tb, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, mcap_, 0, 32, stream_);
         if (e != cudaSuccess) return e;

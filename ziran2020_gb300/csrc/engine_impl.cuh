@@ -29,7 +29,6 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 #include <thrust/iterator/counting_iterator.h>
-#include <thrust/iterator/transform_iterator.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -247,34 +246,23 @@ struct KeptCell { // the new key equals the one the particle was sorted by in th
 struct AnyItem {
     __host__ __device__ bool operator()(uint32_t) const { return true; }
 };
-struct KeyOfIndex { // the key of a stayer; padding (index ~0, or any index past n) sorts last
-    const uint32_t* k;
-    uint32_t n;
-    __host__ __device__ uint32_t operator()(uint32_t i) const { return i < n ? k[i] : ~0u; }
-};
-
-// Pad the stayers to n indices and gather the movers' keys, padded to mcap items with the largest key (padding
-// merges and sorts last; real keys have at most 31 bits). More than mcap movers abort the substep with FLAG_SORT
-// (the host grows the buffer and repeats it with a full sort); the lists are then filled with padding only, so
-// the sort and merge that still run read no index.
-static __global__ void k_inc_prep(uint32_t* stay, const uint32_t* move_idx, const uint32_t* keys, uint32_t* move_keys, uint32_t* move_vals,
-    const int64_t* cnt, int64_t n, int64_t mcap, DevStatus* st)
+// Gather the movers' keys, padded to mcap items with the largest key (padding sorts last; real keys have at most
+// 31 bits). More than mcap movers abort the substep with FLAG_SORT (the host grows the buffer and repeats it with
+// a full sort); the movers' list is then padding only, so the sort that still runs reads no index.
+static __global__ void k_inc_prep(const uint32_t* move_idx, const uint32_t* keys, uint32_t* move_keys, uint32_t* move_vals, const int64_t* cnt,
+    int64_t n, int64_t mcap, DevStatus* st)
 {
-    int64_t S = cnt[0], M = cnt[1];
+    const int64_t S = cnt[0];
+    int64_t M = cnt[1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&st->max_movers, (uint32_t)(M >= 0 && M < 0xffffffffLL ? M : 0xffffffffLL));
     if (S < 0 || M < 0 || S + M != n || M > mcap) {
         if (blockIdx.x == 0 && threadIdx.x == 0) raise_flag(st, FLAG_SORT);
-        S = 0;
         M = 0;
     }
-    const int64_t lim = n > mcap ? n : mcap;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < lim; t += (int64_t)gridDim.x * blockDim.x) {
-        if (t >= S && t < n) stay[t] = ~0u;
-        if (t < mcap) {
-            const uint32_t i = t < M ? move_idx[t] : ~0u;
-            move_keys[t] = i < (uint64_t)n ? keys[i] : ~0u;
-            move_vals[t] = i;
-        }
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < mcap; t += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = t < M ? move_idx[t] : ~0u;
+        move_keys[t] = i < (uint64_t)n ? keys[i] : ~0u;
+        move_vals[t] = i;
     }
 }
 
