@@ -571,6 +571,11 @@ struct PairOf<double> {
     using type = double2;
 };
 __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// 16 bytes of consecutive values (4 FP32 or 2 FP64), moved with one access
+template <class T>
+struct alignas(16) Vec16 {
+    T v[16 / sizeof(T)];
+};
 // four values of one grid node read with one shared-memory access (velocity x, y, z and the phase field)
 template <class T>
 struct alignas(4 * sizeof(T)) Quad {
@@ -1049,44 +1054,56 @@ __global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
     if (aborted_cta(a.st)) return;
     const uint32_t B = min(a.st->n_blocks, a.b_cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_blocks_seen = max(a.st->max_blocks_seen, B);
-    const uint32_t total = B * L::nodes;
+    // GV consecutive nodes of one block per thread: every field moves as one 16-byte access
+    constexpr int GV = (int)(16 / sizeof(T));
+    static_assert(L::nodes % GV == 0, "a block holds whole vectors");
+    const uint32_t total = B * (L::nodes / GV);
     // every thread of the CTA runs the same iterations (the loop holds barriers)
     for (uint32_t base = blockIdx.x * GRID_NT; base < total; base += gridDim.x * GRID_NT) {
         const uint32_t t = base + threadIdx.x;
         T gm = 0;
         int scene = -1;
         if (t < total) {
-            const uint32_t b = t / L::nodes, e = t % L::nodes;
+            const uint32_t b = t / (L::nodes / GV), e0 = (t % (L::nodes / GV)) * GV;
             const uint64_t hk = a.b_key[b];
             scene = (int)(hk >> 40);
             const SceneParams<T>& sp = a.scenes[scene];
-            T* A = a.acc + (size_t)b * NACC * L::nodes + e;
-            T m = A[0];
-            T P[3] = { A[L::nodes], A[2 * L::nodes], A[3 * L::nodes] };
-            T pf = A[4 * L::nodes], pfm = A[5 * L::nodes];
+            Vec16<T>* A = reinterpret_cast<Vec16<T>*>(a.acc + (size_t)b * NACC * L::nodes + e0);
+            constexpr int FS = L::nodes / GV; // field stride in vectors
+            const Vec16<T> m = A[0], P0 = A[FS], P1 = A[2 * FS], P2 = A[3 * FS], pf = A[4 * FS], pfm = A[5 * FS];
+            Vec16<T> zero;
 #pragma unroll
-            for (int q = 0; q < NACC; q++) A[q * L::nodes] = (T)0;
-            T* V = a.vel + (size_t)b * NVEL * L::nodes + e;
-            gm = m;
-            if (m != (T)0) {
-                uint32_t bi, bj, bk;
-                L::block_of_page(hk & ((1ULL << 40) - 1), bi, bj, bk);
-                const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
-                const T xi[3] = { (T)(bi * L::sx + lx) * sp.dx, (T)(bj * L::sy + ly) * sp.dx, (T)(bk * L::sz + lz) * sp.dx };
-                const T dt = sp.dt;
-                T vi[3];
-                // P = m v + dt f: v + g dt + f dt / m (MpmSimulationBase.cpp:1204-1210)
+            for (int k = 0; k < GV; k++) zero.v[k] = (T)0;
 #pragma unroll
-                for (int c = 0; c < 3; c++) vi[c] = P[c] / m + sp.gravity[c] * dt;
-                collide(sp, (T)sp.time, xi, vi);
-                V[0] = vi[0];
-                V[L::nodes] = vi[1];
-                V[2 * L::nodes] = vi[2];
-                V[3 * L::nodes] = pfm != (T)0 ? pf / pfm : (T)0;
+            for (int q = 0; q < NACC; q++) A[q * FS] = zero;
+            Vec16<T> o0, o1, o2, o3;
+            uint32_t bi, bj, bk;
+            L::block_of_page(hk & ((1ULL << 40) - 1), bi, bj, bk);
+            const T dt = sp.dt;
+#pragma unroll
+            for (int k = 0; k < GV; k++) {
+                const T mk = m.v[k];
+                gm += mk;
+                if (mk != (T)0) {
+                    const int e = (int)e0 + k;
+                    const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
+                    const T xi[3] = { (T)(bi * L::sx + lx) * sp.dx, (T)(bj * L::sy + ly) * sp.dx, (T)(bk * L::sz + lz) * sp.dx };
+                    // P = m v + dt f: v + g dt + f dt / m (MpmSimulationBase.cpp:1204-1210)
+                    T vi[3] = { P0.v[k] / mk + sp.gravity[0] * dt, P1.v[k] / mk + sp.gravity[1] * dt, P2.v[k] / mk + sp.gravity[2] * dt };
+                    collide(sp, (T)sp.time, xi, vi);
+                    o0.v[k] = vi[0];
+                    o1.v[k] = vi[1];
+                    o2.v[k] = vi[2];
+                    o3.v[k] = pfm.v[k] != (T)0 ? pf.v[k] / pfm.v[k] : (T)0;
+                }
+                else
+                    o0.v[k] = o1.v[k] = o2.v[k] = o3.v[k] = (T)0;
             }
-            else {
-                V[0] = V[L::nodes] = V[2 * L::nodes] = V[3 * L::nodes] = (T)0;
-            }
+            Vec16<T>* V = reinterpret_cast<Vec16<T>*>(a.vel + (size_t)b * NVEL * L::nodes + e0);
+            V[0] = o0;
+            V[FS] = o1;
+            V[2 * FS] = o2;
+            V[3 * FS] = o3;
         }
         // grid mass per scene: nodes of one warp share a block (and so a scene) whenever L::nodes >= 32; the
         // CTA's warps then combine their sums, one atomic per run of warps of one scene (a single scene would
