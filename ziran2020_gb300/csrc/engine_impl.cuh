@@ -1656,22 +1656,26 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_appl
     __shared__ int16_t cfirst[NC], clast[NC];
     __shared__ int s_g, s_skip;
     __shared__ int32_t s_nbr[8];
+    __shared__ uint16_t s_map[TN]; // tile node -> (neighbour block 0-7) << 8 | element in that block
     if (aborted_cta(a.st)) return;
     const KeyLayout kl = a.kl;
     const int64_t S = a.pstride;
     const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
-    for (int q = tid; q < TN; q += NT) tile[q] = (T)0;
+    for (int q = tid; q < TN; q += NT) {
+        tile[q] = (T)0;
+        const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
+        const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
+        s_map[q] = (uint16_t)(((ax * 4 + ay * 2 + az) << 8) | L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz));
+    }
     const int f_of[1] = { CG_AP };
     for (;;) {
         uint32_t start, end;
         const int sc = dmg_claim<T>(a, &a.st->work_cg, true, start, end, s_nbr, &s_g, &s_skip);
         if (sc < 0) break;
-        for (int q = tid; q < TN; q += NT) {
-            const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
-            const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
-            const int slot = s_nbr[ax * 4 + ay * 2 + az];
-            ptile[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? cgv(a, CG_P, slot)[L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz)] : (T)0;
+        for (int q = tid; q < TN; q += NT) { // (s_map was built before the claim's first barrier)
+            const int m = s_map[q], slot = s_nbr[m >> 8];
+            ptile[q] = (slot >= 0 && (uint32_t)slot < a.b_cap) ? cgv(a, CG_P, slot)[m & 0xff] : (T)0;
         }
         __syncthreads();
         const T inv_dx = a.scenes[sc].inv_dx;
@@ -1697,17 +1701,27 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_appl
                 if (ev != (T)0) {
                     const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
                     const T* pt = ptile + tile_index<L>(lx, ly, lz);
+                    // separable sums of p against the gradient weights: over z, then y, then x
 #pragma unroll
-                    for (int i = 0; i < 3; i++)
+                    for (int i = 0; i < 3; i++) {
+                        T sA = 0, sB = 0, sC = 0;
 #pragma unroll
-                        for (int j = 0; j < 3; j++)
+                        for (int j = 0; j < 3; j++) {
+                            T zA = 0, zD = 0;
 #pragma unroll
                             for (int k = 0; k < 3; k++) {
                                 const T pj = pt[(i * TY + j) * TZ + k];
-                                g0 += pj * (dw[0][i] * w[1][j] * w[2][k]);
-                                g1 += pj * (w[0][i] * dw[1][j] * w[2][k]);
-                                g2 += pj * (w[0][i] * w[1][j] * dw[2][k]);
+                                zA += w[2][k] * pj;
+                                zD += dw[2][k] * pj;
                             }
+                            sA += w[1][j] * zA;
+                            sB += dw[1][j] * zA;
+                            sC += w[1][j] * zD;
+                        }
+                        g0 += dw[0][i] * sA;
+                        g1 += w[0][i] * sB;
+                        g2 += w[0][i] * sC;
+                    }
                     const T sgc = ev * inv_dx * inv_dx; // both gradients carry 1/dx
                     g0 *= sgc;
                     g1 *= sgc;
