@@ -249,6 +249,57 @@ ZR_HD void svd3_jacobi(const double* A, double* U, double* s, double* V)
 // Determinant-scaled Newton iteration X <- (g X + X^{-T}/g)/2 in T; it converges quadratically to R
 // whenever det F > 0. Inverted, nearly singular or ill-conditioned F goes to the FP64 SVD.
 // Returns true when the FP64 path was taken.
+// One Newton step of the polar iteration on the 9 entries, X <- a X + b Cf, returning |step|^2, and the cofactor
+// of the new X. On Blackwell the FP32 form runs two entries per instruction (__ffma2_rn, __fmul2_rn; each lane
+// rounds as the scalar operation); FP64 and host builds keep scalar arithmetic.
+template <class T>
+ZR_HD T newton_step(T* X, T* Cf, T a, T b)
+{
+    T diff = 0;
+    for (int i = 0; i < 9; i++) {
+        const T xn = a * X[i] + b * Cf[i];
+        const T dd = xn - X[i];
+        diff += dd * dd;
+        X[i] = xn;
+    }
+    cofactor3(X, Cf);
+    return diff;
+}
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <>
+__device__ __forceinline__ float newton_step<float>(float* X, float* Cf, float a, float b)
+{
+    const float2 A = make_float2(a, a), Bv = make_float2(b, b);
+    float2 d2 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const float2 x = make_float2(X[i], X[i + 1]);
+        const float2 xn = __ffma2_rn(A, x, __fmul2_rn(Bv, make_float2(Cf[i], Cf[i + 1])));
+        const float2 dd = __fadd2_rn(xn, make_float2(-x.x, -x.y));
+        d2 = __ffma2_rn(dd, dd, d2);
+        X[i] = xn.x;
+        X[i + 1] = xn.y;
+    }
+    const float x8 = a * X[8] + b * Cf[8], d8 = x8 - X[8];
+    X[8] = x8;
+    // cofactor pairs: (A0, A1) (A2, A3) (A4, A5) (A6, A7) as p q - r s per lane, A8 scalar
+    const float2 c01 = __ffma2_rn(make_float2(X[4], X[5]), make_float2(X[8], X[6]), make_float2(-X[5] * X[7], -X[3] * X[8]));
+    const float2 c23 = __ffma2_rn(make_float2(X[3], X[2]), make_float2(X[7], X[7]), make_float2(-X[4] * X[6], -X[1] * X[8]));
+    const float2 c45 = __ffma2_rn(make_float2(X[0], X[1]), make_float2(X[8], X[6]), make_float2(-X[2] * X[6], -X[0] * X[7]));
+    const float2 c67 = __ffma2_rn(make_float2(X[1], X[2]), make_float2(X[5], X[3]), make_float2(-X[2] * X[4], -X[0] * X[5]));
+    Cf[0] = c01.x;
+    Cf[1] = c01.y;
+    Cf[2] = c23.x;
+    Cf[3] = c23.y;
+    Cf[4] = c45.x;
+    Cf[5] = c45.y;
+    Cf[6] = c67.x;
+    Cf[7] = c67.y;
+    Cf[8] = X[0] * X[4] - X[1] * X[3];
+    return d2.x + d2.y + d8 * d8;
+}
+#endif
+
 // The FP64 path of polar_rotation, kept out of line: it is rare, and inlining it into every kernel that
 // decomposes F would crowd the instruction cache of the hot loops.
 template <class T>
@@ -280,18 +331,11 @@ ZR_HD bool polar_rotation(const T* F, T* R)
             for (int it = 0; it < Eps<T>::polar_iters; it++) {
                 T g = rcbrt_(J);
                 T a = (T)0.5 * g, b = (T)0.5 / (g * J);
-                T diff = 0;
-                for (int i = 0; i < 9; i++) {
-                    T xn = a * X[i] + b * Cf[i];
-                    T dd = xn - X[i];
-                    diff += dd * dd;
-                    X[i] = xn;
-                }
+                const T diff = newton_step(X, Cf, a, b);
                 if (diff < Eps<T>::polar_tol * Eps<T>::polar_tol) {
                     ok = true;
                     break;
                 }
-                cofactor3(X, Cf);
                 J = X[0] * Cf[0] + X[1] * Cf[1] + X[2] * Cf[2];
                 if (!(J > 0)) break;
             }
