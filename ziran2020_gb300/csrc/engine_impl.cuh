@@ -1006,9 +1006,17 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
                 cfirst[tid] = 0;
                 clast[tid] = 0;
             }
-            for (int q = tid; q < cnt; q += NT) {
+            // the storage slots of all the thread's particles first (one latency for all), then one particle at a time
+            constexpr int PER = (CHUNK + NT - 1) / NT;
+            uint32_t js[PER];
+#pragma unroll
+            for (int k = 0; k < PER; k++) js[k] = tid + k * NT < cnt ? a.vals_sorted[c0 + tid + k * NT] : 0u;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                const int q = tid + k * NT;
+                if (q >= cnt) break;
                 int b[3];
-                particle_payload<T, MODELS>(a.pin, a.vals_sorted[c0 + q], sp, pay + (q + (q >> 3)), CPAD, b, fallbacks);
+                particle_payload<T, MODELS>(a.pin, js[k], sp, pay + (q + (q >> 3)), CPAD, b, fallbacks);
                 const int l0 = b[0] - s_org[0], l1 = b[1] - s_org[1], l2 = b[2] - s_org[2];
                 const bool inside = l0 >= 0 && l0 < L::sx && l1 >= 0 && l1 < L::sy && l2 >= 0 && l2 < L::sz;
                 if (!inside) raise_flag(a.st, FLAG_CAPACITY); // keys and positions disagree: abort the substep
@@ -1139,15 +1147,29 @@ __global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
 // G2P
 // ---------------------------------------------------------------------------------------------------
 // NT threads per CTA; RESIDENT: threads per SM the register budget is cut for
+// G2P's staged particle state: x, F, m, V0, d, sigma_c (fields G2P_SF) and the pid, per thread and buffer
+enum { GS_X = 0, GS_F = 3, GS_M = 12, GS_V0 = 13, GS_D = 14, GS_SC = 15, G2P_SF = 16 };
+template <class T, int NT>
+struct G2pStage {
+    // double-buffered per-thread slots, field-major so a warp's accesses are consecutive words; off where the
+    // buffers would not fit the 48 KB of static shared memory (FP64 at 256 threads)
+    static constexpr bool ON = 2 * NT * (G2P_SF * sizeof(T) + 4) <= 40 * 1024;
+    static constexpr int NS = ON ? 2 * G2P_SF * NT : 1, NP = ON ? 2 * NT : 1;
+};
+
 template <class T, int NT, int RESIDENT>
 __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
+    using GS = G2pStage<T, NT>;
     // the grid velocities around the group's block as one dense node tile (the block plus 2 nodes on the
     // + side of every axis, the reach of the quadratic stencil): every stencil read is a fixed offset
     constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
     static_assert(NVEL == 4, "one Quad per tile node");
     __shared__ Quad<T> tq[TN]; // node-major: the 4 fields of a node in one access
+    __shared__ Material<T> s_mat[MAX_MATERIALS]; // the group's scene's materials
+    __shared__ T s_st[GS::NS]; // staged state of the thread's current and next particle
+    __shared__ uint32_t s_pid[GS::NP];
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
     __shared__ uint16_t s_map[TN]; // tile node -> (neighbour block 0-7) << 8 | element in that block
     if (aborted_cta(a.st)) return;
@@ -1177,6 +1199,29 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             }
         }
         __syncthreads();
+        const SceneParams<T>& sp = a.scenes[s_scene];
+        const bool damage = sp.damage != 0;
+        const Pool<T>& P = a.pin;
+        const Pool<T>& Q = a.pout;
+        const uint32_t i0 = start + threadIdx.x;
+        uint32_t j_cur = i0 < end ? a.vals_sorted[i0] : 0u; // storage slot of the thread's current particle
+        // asynchronous copy of one particle's state into buffer bf of the thread's slots
+        auto stage = [&](int bf, uint32_t j) {
+            T* d = s_st + bf * G2P_SF * NT + threadIdx.x;
+            const T* src = P.f + j;
+            const int64_t ps = P.stride;
+#pragma unroll
+            for (int c = 0; c < 3; c++) cp_async<sizeof(T)>(d + (GS_X + c) * NT, src + (P_X + c) * ps);
+#pragma unroll
+            for (int c = 0; c < 9; c++) cp_async<sizeof(T)>(d + (GS_F + c) * NT, src + (P_F + c) * ps);
+            cp_async<sizeof(T)>(d + GS_M * NT, src + P_M * ps);
+            cp_async<sizeof(T)>(d + GS_V0 * NT, src + P_V0 * ps);
+            if (damage) {
+                cp_async<sizeof(T)>(d + GS_D * NT, src + P_D * ps);
+                cp_async<sizeof(T)>(d + GS_SC * NT, src + P_SC * ps);
+            }
+            cp_async<4>(s_pid + bf * NT + threadIdx.x, P.pid + j);
+        };
         // stage the tile from the 8 neighbouring blocks (s_map was built before the first barrier)
         for (int node = threadIdx.x; node < TN; node += NT) {
             const int m = s_map[node], slot = s_nbr[m >> 8];
@@ -1189,27 +1234,63 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             qv.w = ok ? src[3 * L::nodes] : (T)0;
             tq[node] = qv;
         }
+        {
+            constexpr int MW = (int)(sizeof(Material<T>) / 4);
+            const uint32_t* ms = reinterpret_cast<const uint32_t*>(sp.materials);
+            uint32_t* md = reinterpret_cast<uint32_t*>(s_mat);
+            for (int k = threadIdx.x; k < MAX_MATERIALS * MW; k += NT) md[k] = ms[k];
+        }
+        if (GS::ON && i0 < end) stage(0, j_cur);
         __syncthreads();
-        const SceneParams<T>& sp = a.scenes[s_scene];
         const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt, D_inv = sp.D_inv;
         const T ca = sp.apic_a, cb = sp.apic_b;
-        const bool damage = sp.damage != 0;
         const T dx2 = dx * dx, half_cfl2 = dx2 * (T)0.25 * (sp.cfl * sp.cfl);
-        const Pool<T>& P = a.pin;
-        const Pool<T>& Q = a.pout;
+        // scene constants in registers: read through sp inside the loop they would be re-read after every store
+        const int key_cells = sp.domain_cells - 3, n_mat = sp.n_materials;
+        const bool implicit = sp.implicit != 0;
         uint32_t flags = 0;
-        for (uint32_t i = start + threadIdx.x; i < end; i += NT) {
-            const uint32_t j = a.vals_sorted[i];
-            // every particle load is issued here, so one memory latency covers them all
-            T x[3], F[9];
+        // storage slots run one particle ahead of the state: with staging the next particle's state is copied
+        // while this one computes; without, its slot is known when its loads issue (one latency, not two)
+        uint32_t j_nxt = i0 + (GS::ON ? NT : 0) < end ? a.vals_sorted[i0 + (GS::ON ? NT : 0)] : 0u;
+        int bf = 0;
+        for (uint32_t i = i0; i < end; i += NT, bf ^= 1) {
+            T x[3], F[9], pm, pV0, dd = 0, sc = 0;
+            uint32_t pid, j;
+            if constexpr (GS::ON) {
+                j = j_cur;
+                cp_async_wait_all(); // this particle's state (the thread's own copies)
+                const T* d = s_st + bf * G2P_SF * NT + threadIdx.x;
 #pragma unroll
-            for (int c = 0; c < 3; c++) x[c] = P.f[(P_X + c) * P.stride + j];
+                for (int c = 0; c < 3; c++) x[c] = d[(GS_X + c) * NT];
 #pragma unroll
-            for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
-            const uint32_t pid = P.pid[j];
-            const T pm = P.f[P_M * P.stride + j], pV0 = P.f[P_V0 * P.stride + j];
-            T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
-            const T sc = damage ? P.f[P_SC * P.stride + j] : (T)0;
+                for (int c = 0; c < 9; c++) F[c] = d[(GS_F + c) * NT];
+                pm = d[GS_M * NT];
+                pV0 = d[GS_V0 * NT];
+                if (damage) {
+                    dd = d[GS_D * NT];
+                    sc = d[GS_SC * NT];
+                }
+                pid = s_pid[bf * NT + threadIdx.x];
+                if (i + NT < end) stage(bf ^ 1, j_nxt); // the other buffer was read in the previous iteration
+                j_cur = j_nxt;
+                if (i + 2 * NT < end) j_nxt = a.vals_sorted[i + 2 * NT];
+            }
+            else {
+                j = j_nxt;
+                if (i + NT < end) j_nxt = a.vals_sorted[i + NT];
+                // every particle load is issued here, so one memory latency covers them all
+#pragma unroll
+                for (int c = 0; c < 3; c++) x[c] = P.f[(P_X + c) * P.stride + j];
+#pragma unroll
+                for (int c = 0; c < 9; c++) F[c] = P.f[(P_F + c) * P.stride + j];
+                pid = P.pid[j];
+                pm = P.f[P_M * P.stride + j];
+                pV0 = P.f[P_V0 * P.stride + j];
+                if (damage) {
+                    dd = P.f[P_D * P.stride + j];
+                    sc = P.f[P_SC * P.stride + j];
+                }
+            }
             int b[3], l[3];
             T w[3][3], dw[3][3], fr[3];
 #pragma unroll
@@ -1341,28 +1422,27 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     nb[c] = base_node(xn[c], inv_dx);
-                    in_dom = in_dom && nb[c] >= 0 && nb[c] < sp.domain_cells - 3;
+                    in_dom = in_dom && nb[c] >= 0 && nb[c] < key_cells;
                 }
                 if (!in_dom) {
                     flags |= FLAG_OUT_OF_DOMAIN;
                     nb[0] = nb[1] = nb[2] = 0;
                 }
-                // a particle that stays in its cell keeps the key it was sorted by
-                if (nb[0] == b[0] && nb[1] == b[1] && nb[2] == b[2])
-                    kl.put(a.keys_next, i, kl.at(a.keys_sorted, i));
-                else
-                    kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
+                // the engine's keys carry no particle index (ib = 0), so a particle that stays in its cell gets
+                // exactly the key it was sorted by (k_keys and this kernel share base_node): the incremental
+                // sort's stayer test compares the two
+                kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
             }
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
             Q.pid[i] = pid;
-            if (sp.implicit) Q.f[P_MDT * Q.stride + i] = P.f[P_MDT * P.stride + j]; // the implicit damage solve's history travels with the particle
+            if (implicit) Q.f[P_MDT * Q.stride + i] = P.f[P_MDT * P.stride + j]; // the implicit damage solve's history travels with the particle
             if (damage) {
                 // AnisoMPM damage with the F of the start of the substep (AnisoFractureSimulation.h:210-283)
                 const uint32_t mat = pid >> L::index_bits;
-                const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
+                const Material<T>& mt = s_mat[mat < (uint32_t)n_mat ? mat : 0];
                 if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
-                    if (sp.implicit) {
+                    if (implicit) {
                         // damageG2P (AnisoFractureSimulation.h:578-610): the grid holds the solve's change of the
                         // nodal phase field; damage never decreases and stays <= 1
                         const T nd = dd + pw;

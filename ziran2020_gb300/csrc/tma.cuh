@@ -66,6 +66,19 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint3
                  : "memory");
 }
 
+// one element global -> shared without a register round trip (sm_80+ asynchronous copy; BYTES 4, 8 or 16,
+// both addresses aligned to BYTES); complete once cp_async_wait_all returns in the issuing thread. G2P stages
+// the next particle's state this way while it computes the current one.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst_smem, const void* src)
+{
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async.ca copies 4, 8 or 16 bytes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst_smem)), "l"(src), "n"(BYTES) : "memory");
+}
+
+// wait for all of this thread's asynchronous element copies (other threads' copies need a barrier after their waits)
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // order this thread's earlier generic-proxy shared-memory accesses before later async-proxy ones
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
