@@ -719,6 +719,82 @@ __device__ __forceinline__ void flush_tile(const StepArgs<T>& a, T* tile, const 
     }
 }
 
+// The fused P2G's node tiles, one per stencil x-offset ii: tile ii holds nodes x = cx + ii for cx in [0, sx), all
+// y and z of the block plus its +2 halo. The warps of one offset cover disjoint cx, and within a warp the lanes'
+// cells are distinct, so each of the 9 node steps below touches distinct nodes: a plain read-modify-write
+// replaces the shared-memory float atomics (several times their throughput). Lanes of one warp reach the same
+// node in different steps, so the steps are separated by __syncwarp (it orders the lanes' shared accesses).
+// Every lane of the warp must call it.
+template <class L>
+struct OffsetTiles {
+    static constexpr int TY = L::sy + 2, TZ = L::sz + 2;
+    static constexpr int TS = L::sx * TY * TZ; // nodes of one offset's tile (per field)
+    static constexpr int ELEMS = 3 * NACC * TS;
+};
+
+template <class T, class L>
+__device__ __forceinline__ void add_to_offset_tile(const NodeAcc<T>& acc, T* tiles, int cx, int cy, int cz, int ii, int nf)
+{
+    using OT = OffsetTiles<L>;
+    T* base = tiles + ii * NACC * OT::TS + (cx * OT::TY + cy) * OT::TZ + cz;
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            T* t = base + jj * OT::TZ + kk;
+#pragma unroll
+            for (int f = 0; f < NACC; f++)
+                if (f < nf) t[f * OT::TS] += acc.field(jj * 3 + kk, f);
+            __syncwarp();
+        }
+}
+
+// node (X, Y, z-column) of the block's 6x6x6 tile = the sum over the offsets ii with X - ii in [0, sx); written to
+// the 8 neighbouring grid blocks as flush_tile does, the offset tiles cleared behind the flush
+template <class T, int N>
+__device__ __forceinline__ void flush_offset_column(T* dst, T* tiles, int f, int X, int Y, int z0)
+{
+    using L = typename LayoutOf<T>::type;
+    using OT = OffsetTiles<L>;
+    T v[N];
+#pragma unroll
+    for (int z = 0; z < N; z++) v[z] = (T)0;
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++) {
+        const int xl = X - ii;
+        if (xl < 0 || xl >= L::sx) continue;
+        T* src = tiles + (ii * NACC + f) * OT::TS + (xl * OT::TY + Y) * OT::TZ + z0;
+#pragma unroll
+        for (int z = 0; z < N; z++) {
+            v[z] += src[z];
+            src[z] = (T)0;
+        }
+    }
+    flush_column(dst, v, N);
+}
+
+template <class T, class L>
+__device__ __forceinline__ void flush_offset_tiles(const StepArgs<T>& a, T* tiles, const int32_t* nbr, int nf, int tid, int nthreads)
+{
+    constexpr int TX = L::sx + 2, TY = L::sy + 2;
+    static_assert(L::sz + 2 - L::sz == 2, "z columns split 4 + 2");
+    for (int q = tid; q < nf * TX * TY * 2; q += nthreads) {
+        const int half = q & 1, col = q >> 1;
+        const int f = col / (TX * TY), ab = col % (TX * TY), ta = ab / TY, tb = ab % TY;
+        const int ax = ta >= L::sx, ay = tb >= L::sy;
+        const int slot = nbr[ax * 4 + ay * 2 + half];
+        if ((uint32_t)slot >= a.b_cap) {
+            check_failed(a.st, 5);
+            continue;
+        }
+        T* dst = a.acc + ((size_t)slot * NACC + f) * L::nodes + L::element(ta - ax * L::sx, tb - ay * L::sy, 0);
+        if (half)
+            flush_offset_column<T, 2>(dst, tiles, f, ta, tb, L::sz);
+        else
+            flush_offset_column<T, L::sz>(dst, tiles, f, ta, tb, 0);
+    }
+}
+
 // CHUNK: particles staged per copy (the tile of particles); the scatter CTA is the consumer threads
 // (cell x stencil x-offset) plus one producer warp
 // NBUF: staging buffers (1: the next chunk's copy overlaps the tile accumulation and flush of the current
@@ -956,10 +1032,9 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
     using L = typename LayoutOf<T>::type;
     using S = FusedShape<T>;
     constexpr int NT = S::NT, CHUNK = S::CHUNK, CPAD = S::CPAD, NC = L::nodes;
-    constexpr int TN = (L::sx + 2) * (L::sy + 2) * (L::sz + 2);
     extern __shared__ __align__(16) unsigned char fused_dyn[];
     T* pay = reinterpret_cast<T*>(fused_dyn);
-    __shared__ T tile[NACC * TN];
+    __shared__ T tile[OffsetTiles<L>::ELEMS]; // one node tile per stencil x-offset
     __shared__ uint8_t cellof[CHUNK];
     __shared__ int16_t cfirst[NC], clast[NC];
     __shared__ int s_g, s_scene, s_bad;
@@ -970,7 +1045,7 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
     const int tid = threadIdx.x;
     const int ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
-    for (int q = tid; q < NACC * TN; q += NT) tile[q] = (T)0;
+    for (int q = tid; q < OffsetTiles<L>::ELEMS; q += NT) tile[q] = (T)0;
     uint32_t fallbacks = 0;
     for (;;) {
         if (tid == 0) {
@@ -1039,10 +1114,10 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
                 for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, true>(acc, pay + (q + (q >> 3)), ii);
             else
                 for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, false>(acc, pay + (q + (q >> 3)), ii);
-            if (qb > qa) add_to_tile<T, L>(acc, tile, cx, cy, cz, ii, nf);
+            add_to_offset_tile<T, L>(acc, tile, cx, cy, cz, ii, nf); // all lanes (an empty cell adds zeros)
             __syncthreads();
         }
-        if (!bad) flush_tile<T, L>(a, tile, s_nbr, nf, tid, NT);
+        if (!bad) flush_offset_tiles<T, L>(a, tile, s_nbr, nf, tid, NT);
         __syncthreads();
     }
     if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
