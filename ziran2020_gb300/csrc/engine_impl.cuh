@@ -1643,17 +1643,44 @@ __global__ void k_dmg_prep(StepArgs<T> a)
 template <class L>
 __device__ __forceinline__ int tile_index(int lx, int ly, int lz) { return (lx * (L::sy + 2) + ly) * (L::sz + 2) + lz; }
 
-// tile -> the node vectors of the 8 neighbouring blocks (atomics), then cleared; nf fields, vector f_of[f]
-template <class T, class L>
-__device__ void flush_tile_cg(const StepArgs<T>& a, T* tile, const int32_t* nbr, int nf, const int* f_of, int tid, int nthreads)
+// The per-offset tiles of the fused P2G (OffsetTiles) for NF node vectors of the implicit solve: get(n, f) is
+// field f of the thread's node n = 3 jj + kk. Every lane of the warp must call it.
+template <class L, int NF, class T, class Get>
+__device__ __forceinline__ void add_to_offset_tile_cg(T* tiles, int cx, int cy, int cz, int ii, Get get)
 {
-    constexpr int TX = L::sx + 2, TY = L::sy + 2, TZ = L::sz + 2, TN = TX * TY * TZ;
-    for (int q = tid; q < nf * TN; q += nthreads) {
+    using OT = OffsetTiles<L>;
+    T* base = tiles + ii * NF * OT::TS + (cx * OT::TY + cy) * OT::TZ + cz;
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            T* t = base + jj * OT::TZ + kk;
+#pragma unroll
+            for (int f = 0; f < NF; f++) t[f * OT::TS] += get(jj * 3 + kk, f);
+            __syncwarp();
+        }
+}
+
+// sum the offsets' tiles per node of the block + halo into node vectors f_of[f] of the 8 neighbouring blocks
+// (scalar atomics, zeros skipped), clearing the tiles
+template <class T, class L, int NF>
+__device__ void flush_offset_tiles_cg(const StepArgs<T>& a, T* tiles, const int32_t* nbr, const int* f_of, int tid, int nthreads)
+{
+    using OT = OffsetTiles<L>;
+    constexpr int TX = L::sx + 2, TY = OT::TY, TZ = OT::TZ, TN = TX * TY * TZ;
+    for (int q = tid; q < NF * TN; q += nthreads) {
         const int f = q / TN, node = q % TN;
         const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
-        const T v = tile[q];
+        T v = (T)0;
+#pragma unroll
+        for (int ii = 0; ii < 3; ii++) {
+            const int xl = tx - ii;
+            if (xl < 0 || xl >= L::sx) continue;
+            T* src = tiles + (ii * NF + f) * OT::TS + (xl * TY + ty) * TZ + tz;
+            v += *src;
+            *src = (T)0;
+        }
         if (v == (T)0) continue;
-        tile[q] = (T)0;
         const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
         const int slot = nbr[ax * 4 + ay * 2 + az];
         if (slot < 0 || (uint32_t)slot >= a.b_cap) {
@@ -1720,7 +1747,8 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
     using L = typename LayoutOf<T>::type;
     using D = DmgShape<T>;
     constexpr int NC = L::nodes, NT = D::NT, CHUNK = D::CHUNK, TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
-    __shared__ T tile[3 * TN];
+    constexpr int TE = 3 * 3 * OffsetTiles<L>::TS; // per-offset tiles of the 3 node vectors
+    __shared__ T tile[TE];
     __shared__ T st[D::NS][CHUNK]; // fr x3, vol D~ dt/eta, vol, c
     __shared__ uint8_t cellof[CHUNK];
     __shared__ int16_t cfirst[NC], clast[NC];
@@ -1731,7 +1759,7 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
     const int64_t S = a.pstride;
     const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
-    for (int q = tid; q < 3 * TN; q += NT) tile[q] = (T)0;
+    for (int q = tid; q < TE; q += NT) tile[q] = (T)0;
     const int f_of[3] = { CG_SA, CG_SV, CG_DIAG };
     for (;;) {
         uint32_t start, end;
@@ -1775,21 +1803,11 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_rhs(
                         acc[j * 3 + k][2] += wijk * cc;
                     }
             }
-            if (qb > qa) {
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        T* t = tile + tile_index<L>(cx + ii, cy + j, cz + k);
-                        atomicAdd(t, acc[j * 3 + k][0]);
-                        atomicAdd(t + TN, acc[j * 3 + k][1]);
-                        atomicAdd(t + 2 * TN, acc[j * 3 + k][2]);
-                    }
-            }
+            add_to_offset_tile_cg<L, 3>(tile, cx, cy, cz, ii, [&](int n, int f) { return acc[n][f]; }); // all lanes
             any = true;
             __syncthreads();
         }
-        if (any) flush_tile_cg<T, L>(a, tile, s_nbr, 3, f_of, tid, NT);
+        if (any) flush_offset_tiles_cg<T, L, 3>(a, tile, s_nbr, f_of, tid, NT);
         __syncthreads();
     }
 }
@@ -1804,7 +1822,8 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_appl
     using L = typename LayoutOf<T>::type;
     using D = DmgShape<T>;
     constexpr int NC = L::nodes, NT = D::NT, CHUNK = D::CHUNK, TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
-    __shared__ T tile[TN];
+    constexpr int TE = 3 * OffsetTiles<L>::TS; // per-offset tiles of A p
+    __shared__ T tile[TE];
     __shared__ T ptile[TN];
     __shared__ T st[D::NS][CHUNK]; // fr x3, gc x3
     __shared__ uint8_t cellof[CHUNK];
@@ -1817,8 +1836,8 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_appl
     const int64_t S = a.pstride;
     const int tid = threadIdx.x, ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    for (int q = tid; q < TE; q += NT) tile[q] = (T)0;
     for (int q = tid; q < TN; q += NT) {
-        tile[q] = (T)0;
         const int tx = q / (TY * TZ), ty = (q / TZ) % TY, tz = q % TZ;
         const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
         s_map[q] = (uint16_t)(((ax * 4 + ay * 2 + az) << 8) | L::element(tx - ax * L::sx, ty - ay * L::sy, tz - az * L::sz));
@@ -1905,15 +1924,10 @@ __global__ void __launch_bounds__(DmgShape<T>::NT, DmgShape<T>::MINB) k_dmg_appl
 #pragma unroll
                     for (int k = 0; k < 3; k++) acc[j * 3 + k] += (a0 * w[1][j] + a1 * dw[1][j]) * w[2][k] + a2 * (w[1][j] * dw[2][k]);
             }
-            if (qb > qa) {
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-#pragma unroll
-                    for (int k = 0; k < 3; k++) atomicAdd(tile + tile_index<L>(cx + ii, cy + j, cz + k), acc[j * 3 + k]);
-            }
+            add_to_offset_tile_cg<L, 1>(tile, cx, cy, cz, ii, [&](int n, int) { return acc[n]; }); // all lanes
             __syncthreads();
         }
-        flush_tile_cg<T, L>(a, tile, s_nbr, 1, f_of, tid, NT);
+        flush_offset_tiles_cg<T, L, 1>(a, tile, s_nbr, f_of, tid, NT);
         __syncthreads();
     }
 }
