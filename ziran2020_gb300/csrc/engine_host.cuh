@@ -41,7 +41,8 @@ class Engine final : public EngineBase {
     static constexpr int VAR_CHUNK[3] = { CH_BIG, CH_BIG, CH_BIG / 2 };
     static constexpr int VAR_NBUF[3] = { 1, 2, 2 };
     static constexpr int G2P_NT[3] = { 64, 128, 256 };
-    // G2P register budgets: threads per SM (FP32: ~144 registers, no spills, or 128; FP64: ~255 or ~200)
+    // G2P register budgets: threads per SM (FP32 448: a ~146-register cap, under which ptxas settles at 128 with
+    // little spilling; 512: a 128 cap, more spills; FP64: ~255 or ~200)
     static constexpr int G2P_RES[2] = { sizeof(T) == 4 ? 448 : 256, sizeof(T) == 4 ? 512 : 320 };
     // fused P2G register budgets: cut for 2 or 3 CTAs per SM (FP32), 1 or 2 (FP64)
     static constexpr int FUSED_MINB[2] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2 };
