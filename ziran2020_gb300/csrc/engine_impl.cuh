@@ -1331,21 +1331,14 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
         for (uint32_t i = i0; i < end; i += NT, bf ^= 1) {
             T x[3], F[9], pm, pV0, dd = 0, sc = 0;
             uint32_t pid, j;
+            // staged: x now, the rest of the state from shared memory where it is used (it stays valid for the
+            // whole iteration), so it holds no registers through the gather
+            const T* dsl = s_st + bf * G2P_SF * NT + threadIdx.x;
             if constexpr (GS::ON) {
                 j = j_cur;
                 cp_async_wait_all(); // this particle's state (the thread's own copies)
-                const T* d = s_st + bf * G2P_SF * NT + threadIdx.x;
 #pragma unroll
-                for (int c = 0; c < 3; c++) x[c] = d[(GS_X + c) * NT];
-#pragma unroll
-                for (int c = 0; c < 9; c++) F[c] = d[(GS_F + c) * NT];
-                pm = d[GS_M * NT];
-                pV0 = d[GS_V0 * NT];
-                if (damage) {
-                    dd = d[GS_D * NT];
-                    sc = d[GS_SC * NT];
-                }
-                pid = s_pid[bf * NT + threadIdx.x];
+                for (int c = 0; c < 3; c++) x[c] = dsl[(GS_X + c) * NT];
                 if (i + NT < end) stage(bf ^ 1, j_nxt); // the other buffer was read in the previous iteration
                 j_cur = j_nxt;
                 if (i + 2 * NT < end) j_nxt = a.vals_sorted[i + 2 * NT];
@@ -1472,6 +1465,10 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                         if (!isfinite(cn)) flags |= FLAG_NONFINITE;
                         A[3 * r + c] = (r == c ? (T)1 : (T)0) + dt * Gv[3 * r + c];
                     }
+                if constexpr (GS::ON) {
+#pragma unroll
+                    for (int c = 0; c < 9; c++) F[c] = dsl[(GS_F + c) * NT];
+                }
                 mul3(A, F, Fn);
                 bool finite = true;
 #pragma unroll
@@ -1507,6 +1504,15 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
                 // exactly the key it was sorted by (k_keys and this kernel share base_node): the incremental
                 // sort's stayer test compares the two
                 kl.put(a.keys_next, i, ((uint64_t)s_scene << (kl.cp + kl.ib)) | ((L::offset(nb[0], nb[1], nb[2]) >> L::data_bits) << kl.ib));
+            }
+            if constexpr (GS::ON) {
+                pm = dsl[GS_M * NT];
+                pV0 = dsl[GS_V0 * NT];
+                pid = s_pid[bf * NT + threadIdx.x];
+                if (damage) {
+                    dd = dsl[GS_D * NT];
+                    sc = dsl[GS_SC * NT];
+                }
             }
             Q.f[P_M * Q.stride + i] = pm;
             Q.f[P_V0 * Q.stride + i] = pV0;
