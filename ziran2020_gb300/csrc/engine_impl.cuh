@@ -1613,24 +1613,28 @@ __global__ void k_dmg_prep(StepArgs<T> a)
     const Pool<T>& P = a.pin;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < a.n_total; q += gridDim.x * blockDim.x) {
         const SceneParams<T>& sp = a.scenes[kl.scene(kl.at(a.keys_sorted, q))];
-        if (!sp.implicit) continue;
         const uint32_t j = a.vals_sorted[q];
+        // every state load of the particle at once (one latency), ahead of the scene and material tests
+        T x[3], F[9];
+#pragma unroll
+        for (int e = 0; e < 3; e++) x[e] = P.f[(P_X + e) * P.stride + j];
+#pragma unroll
+        for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
+        const T V0 = P.f[P_V0 * P.stride + j], drive = P.f[P_DRV * P.stride + j];
+        T hist = P.f[P_MDT * P.stride + j];
+        const uint32_t pid = P.pid[j];
+        if (!sp.implicit) continue;
         T* y = a.pay + pay_pos(q);
 #pragma unroll
         for (int e = 0; e < 3; e++) {
-            const T xs = mul_rn(P.f[(P_X + e) * P.stride + j], sp.inv_dx);
+            const T xs = mul_rn(x[e], sp.inv_dx);
             y[(DS_F + e) * S] = xs - (T)int_floor(sub_rn(xs, (T)0.5));
         }
-        const uint32_t mat = P.pid[j] >> L::index_bits;
+        const uint32_t mat = pid >> L::index_bits;
         const Material<T>& mt = sp.materials[mat < (uint32_t)sp.n_materials ? mat : 0];
         T av = 0, vol = 0, c = 0, ev = 0;
         if (mt.damage && (mt.model == MODEL_NEOHOOKEAN_BORDEN || mt.model == MODEL_QR_STABLE_NEOHOOKEAN)) {
-            T F[9];
-#pragma unroll
-            for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
-            vol = P.f[P_V0 * P.stride + j] * det3(F);
-                const T drive = P.f[P_DRV * P.stride + j];
-            T hist = P.f[P_MDT * P.stride + j];
+            vol = V0 * det3(F);
             hist = drive > hist ? drive : hist;
             P.f[P_MDT * P.stride + j] = hist;
             const T dt = sp.dt;
