@@ -1036,7 +1036,6 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
     T* pay = reinterpret_cast<T*>(fused_dyn);
     __shared__ T tile[OffsetTiles<L>::ELEMS]; // one node tile per stencil x-offset
     __shared__ uint8_t cellof[CHUNK];
-    __shared__ int16_t cfirst[NC], clast[NC];
     __shared__ int s_g, s_scene, s_bad;
     __shared__ int32_t s_nbr[8];
     __shared__ int s_org[3];
@@ -1077,10 +1076,6 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
         for (uint32_t c0 = start; c0 < end && !bad; c0 += CHUNK) {
             const int cnt = (int)min((uint32_t)CHUNK, end - c0);
             // ---- phase 1: per particle
-            if (tid < NC) {
-                cfirst[tid] = 0;
-                clast[tid] = 0;
-            }
             // the storage slots of all the thread's particles first (one latency for all), then one particle at a time
             constexpr int PER = (CHUNK + NT - 1) / NT;
             uint32_t js[PER];
@@ -1098,18 +1093,21 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
                 cellof[q] = inside ? (uint8_t)L::element(l0, l1, l2) : (uint8_t)0xff;
             }
             __syncthreads();
-            // particles of one cell are contiguous (sorted by cell inside the block)
-            for (int q = tid; q < cnt; q += NT) {
-                const int e = cellof[q];
-                if (e >= NC) continue;
-                if (q == 0 || cellof[q - 1] != e) cfirst[e] = (int16_t)q;
-                if (q == cnt - 1 || cellof[q + 1] != e) clast[e] = (int16_t)(q + 1);
-            }
-            __syncthreads();
-            // ---- phases 2 and 3
+            // ---- phases 2 and 3. Particles of one cell are contiguous and the cells ascend (sorted by cell inside
+            // the block): the cell's range by two binary searches over the chunk's cells, no pass or barrier of its
+            // own (a position that disagreed with its key has raised FLAG_CAPACITY; the searches stay in [0, cnt])
+            auto cell_lower = [&](int v) {
+                int lo = 0, hi = cnt;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (cellof[mid] < v) lo = mid + 1;
+                    else hi = mid;
+                }
+                return lo;
+            };
+            const int qa = cell_lower(c), qb = cell_lower(c + 1);
             NodeAcc<T> acc;
             acc.zero();
-            const int qa = cfirst[c], qb = clast[c];
             if (nf == NACC)
                 for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, true>(acc, pay + (q + (q >> 3)), ii);
             else
