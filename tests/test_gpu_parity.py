@@ -2,7 +2,7 @@
 
 Tolerances (stated per test): the FP64 GPU path differs from the FP64 oracle only by the order of
 floating-point sums (atomic scatter vs the reference's colour-ordered scatter), so it agrees to ~1e-12
-relative; the FP32 path is held to the benchmark spec's bound of 1e-4 domain-relative position error."""
+relative; the FP32 path is held to 1e-4 domain-relative position error (the path's stated FP32 bound)."""
 import numpy as np
 import pytest
 
