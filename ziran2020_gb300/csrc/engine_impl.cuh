@@ -459,17 +459,21 @@ __device__ __forceinline__ void particle_payload(const Pool<T>& P, uint32_t j, c
     uint32_t& fallbacks)
 {
     using L = typename LayoutOf<T>::type;
+    // The corotated stress's polar decomposition needs many registers: with it, v and C are loaded after the
+    // stress (a second memory latency) instead of being held through it (spills)
+    constexpr bool LATE_VC = (MODELS & 1) != 0;
     T x[3], v[3], Cm[9], F[9];
+    auto load_vc = [&]() {
 #pragma unroll
-    for (int e = 0; e < 3; e++) {
-        x[e] = P.f[(P_X + e) * P.stride + j];
-        v[e] = P.f[(P_V + e) * P.stride + j];
-    }
+        for (int e = 0; e < 3; e++) v[e] = P.f[(P_V + e) * P.stride + j];
 #pragma unroll
-    for (int e = 0; e < 9; e++) {
-        Cm[e] = P.f[(P_C + e) * P.stride + j];
-        F[e] = P.f[(P_F + e) * P.stride + j];
-    }
+        for (int e = 0; e < 9; e++) Cm[e] = P.f[(P_C + e) * P.stride + j];
+    };
+#pragma unroll
+    for (int e = 0; e < 3; e++) x[e] = P.f[(P_X + e) * P.stride + j];
+#pragma unroll
+    for (int e = 0; e < 9; e++) F[e] = P.f[(P_F + e) * P.stride + j];
+    if constexpr (!LATE_VC) load_vc();
     const T mass = P.f[P_M * P.stride + j], V0 = P.f[P_V0 * P.stride + j];
     const bool damage = sp.damage != 0;
     const T dd = damage ? P.f[P_D * P.stride + j] : (T)0;
@@ -484,6 +488,7 @@ __device__ __forceinline__ void particle_payload(const Pool<T>& P, uint32_t j, c
         tau_qrnh(mt, F, g, tau);
     else
         tau_nhb(mt, F, g, tau);
+    if constexpr (LATE_VC) load_vc();
     const T dx = sp.dx, inv_dx = sp.inv_dx, dt = sp.dt;
     T fr[3];
 #pragma unroll
