@@ -727,7 +727,7 @@ __device__ __forceinline__ void flush_tile(const StepArgs<T>& a, T* tile, const 
 // The fused P2G's node tiles, one per stencil x-offset ii: tile ii holds nodes x = cx + ii for cx in [0, sx), all
 // y and z of the block plus its +2 halo. The warps of one offset cover disjoint cx, and within a warp the lanes'
 // cells are distinct, so each of the 9 node steps below touches distinct nodes: a plain read-modify-write
-// replaces the shared-memory float atomics (several times their throughput). Lanes of one warp reach the same
+// replaces the shared-memory float atomics (about twice their throughput). Lanes of one warp reach the same
 // node in different steps, so the steps are separated by __syncwarp (it orders the lanes' shared accesses).
 // Every lane of the warp must call it.
 template <class L>
