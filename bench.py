@@ -34,14 +34,6 @@ WORKLOADS = {
     # the same slab with the implicit damage solve (AnisoFractureSimulation.h:437-626) instead of the explicit update
     "aniso_slab_implicit_dx256": (1, dict(dx=1 / 256, l0=0.5 / 256, implicit_damage=1)),
 }
-# CPU sample: the same slab at the same resolution, cropped to a 0.125 x 0.1 x 0.125 m piece
-CPU_SAMPLE = {"aniso_slab_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125)),
-              "aniso_slab_dx128": dict(size=(0.25, 0.1, 0.25)),
-              "elastic_box_dx64": dict(),
-              "aniso_slab_qr_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), model=2, fiber_stiffness=10.0),
-              "aniso_slab_implicit_dx256": dict(dx=1 / 256, l0=0.5 / 256, size=(0.125, 0.1, 0.125), implicit_damage=1)}
-
-
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -56,7 +48,13 @@ def parse():
     ap.add_argument("--accuracy-steps", default="100,500", help="substeps at which FP32 is compared with the FP64 path")
     ap.add_argument("--oracle-steps", type=int, default=200, help="substeps of the elastic-cube check against the FP64 oracle")
     ap.add_argument("--fp64-steps", type=int, default=10)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--oracle-slab-steps", type=int, default=100,
+                    help="substeps of the whole workload on the FP64 oracle: the GPU paths' error against it, and the CPU baseline")
+    ap.add_argument("--no-batch", action="store_true", help="default workload: skip the 256-scene batch summary")
+    ap.add_argument("--no-serve", action="store_true", help="default workload: skip the serving summary")
+    ap.add_argument("--batch-steps", type=int, default=20, help="default workload: timed substeps of the batch summary")
+    ap.add_argument("--serve-rates", default="8,32", help="default workload: arrival rates (requests/s) of the serving summary")
+    ap.add_argument("--serve-requests", type=int, default=24, help="default workload: requests per rate in the serving summary")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="with --profile-only: launch kernels one at a time, not as graphs")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
@@ -195,32 +193,56 @@ def algorithmic_bytes(s_bytes, n, blocks, nodes_per_block, damage):
 
 
 # ------------------------------------------------------------------------------------------- arms
+# recipe fields of WORKLOADS -> the oracle's scene-family parameters (oracle/pyoracle.py RECIPE_DEFAULTS)
+_ORACLE_KEYS = {"dx": "dx", "l0": "l0", "model": "model", "fiber_stiffness": "fiber", "implicit_damage": "implicit", "size": "size"}
+
+
+def oracle_workload(kind, over, seed, inputs=None):
+    """The workload as an FP64 oracle scene (test infrastructure, the CPU baseline). With inputs=None the
+    particles come from the oracle's own seeded generator (the reference arm loads no product library);
+    otherwise from the given arrays (the same inputs as the GPU run)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+
+    kw = {_ORACLE_KEYS[k]: v for k, v in over.items() if k in _ORACLE_KEYS}
+    if "implicit" in kw:
+        kw["implicit"] = bool(kw["implicit"])
+    return po.recipe_scene(kind, 8, seed=seed, inputs=inputs, **kw)
+
+
 def run_reference(args, world, rank):
-    """The reference's CPU algorithm (the oracle restatement: the reference itself cannot be built here)
-    on all host threads, FP64 as the reference's AnisoMPM driver is compiled (anisofracture.cpp:13-14)."""
+    """The reference's CPU algorithm on all host threads: the oracle restatement (the reference itself cannot be
+    built here or on Arm), FP64 as the reference's AnisoMPM driver is compiled (anisofracture.cpp:13-14), on the
+    same workload, seed and particle count as the GPU arm, with inputs from the oracle's own generator."""
     if rank != 0:
         return None
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     import pyoracle as po
-    import scenes
 
     kind, over = WORKLOADS[args.workload]
-    smp = CPU_SAMPLE[args.workload]
-    desc = _desc_for(kind, smp, scenes)
-    o = scenes.oracle_scene(desc, 8)
-    n = len(desc["m"])
-    o.step(max(1, args.warmup))
+    o, n = oracle_workload(kind, over, seed=12345)
     t0 = time.perf_counter()
-    o.step(args.steps)
+    o.step(max(1, args.warmup))
+    per_step = (time.perf_counter() - t0) / max(1, args.warmup)
+    # every requested substep is timed unless that would take more than REF_TIMED_S (a run with the default
+    # 1000 substeps); the line then states how many were timed
+    steps = args.steps if per_step * args.steps <= REF_TIMED_S else max(1, int(REF_TIMED_S / per_step))
+    t0 = time.perf_counter()
+    o.step(steps)
     el = time.perf_counter() - t0
-    val = n * args.steps / el
+    val = n * steps / el
+    cfg = _config(args, "fp64")
+    cfg["particles"] = int(n)
+    cfg["substeps_timed"] = steps
     return {"impl": "reference", "metric": "particle-substeps/sec", "value": val, "unit": "particle-substeps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": _config(args),
-            "cpu_baseline": {"value": val, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port",
-                             "sample": f"{n} particles of the same slab at the same dx (cropped {smp.get('size')}), {args.steps} substeps"},
+            "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; inputs from the oracle's own generator)", "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
+                             "sample": f"the whole workload ({n} particles), {steps} substeps after {max(1, args.warmup)} warm-up substeps"},
             "e2e": {"value": val, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+REF_TIMED_S = 240.0
 
 
 def error_vs_oracle(steps):
@@ -255,12 +277,15 @@ def error_vs_oracle(steps):
     return out
 
 
-def _desc_for(kind, over, scenes):
-    if kind == 1:
-        dx = over.get("dx", 1 / 128)
-        return scenes.aniso_slab(size=over.get("size", (0.5, 0.1, 0.5)), dx=dx, seed=12345, model=over.get("model") or None,
-                                 fiber=over.get("fiber_stiffness", 0.0), implicit=bool(over.get("implicit_damage")))
-    return scenes.elastic_box(size=over.get("size", 0.25), dx=over.get("dx", 1 / 64), seed=12345)
+def field_errors(a, b):
+    """max and RMS of |a - b| for x, v, F and d (float64)."""
+    import numpy as np
+
+    out = {}
+    for f in ("x", "v", "F", "d"):
+        e = np.abs(np.asarray(a[f], dtype=np.float64) - np.asarray(b[f], dtype=np.float64))
+        out[f] = {"max": float(e.max()) if e.size else 0.0, "rms": float(np.sqrt(np.mean(e * e))) if e.size else 0.0}
+    return out
 
 
 def apply_schedule(obj, spec):
@@ -274,18 +299,17 @@ def apply_schedule(obj, spec):
         obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]), g2p_tight=int(f[5]) if len(f) > 5 else 0)
 
 
-def _config(args):
-    return {"workload": args.workload, "particles": None, "substeps_timed": args.steps, "precision_path": "fp32",
+def _config(args, precision="fp32"):
+    return {"workload": args.workload, "particles": None, "substeps_timed": args.steps, "precision_path": precision,
             "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{args.gpus}"}
 
 
-def run_batch(args, world, rank):
-    """256 independent elastic boxes (N log-uniform in 5k-400k, E ~ U(5e3, 5e4), centre ~ U[0.3,0.7]^3,
-    v0 ~ U[-1,1]^3; dx = 1/64, dt = 1e-4) advanced together: one launch per kernel for the whole batch."""
+def measure_batch(recs, steps, warmup, world=1, fp64_steps=10):
+    """Advance the batch of recipes (one launch per kernel for all scenes): timed substeps, per-phase kernel times,
+    the roofline of the dominant transfer kernel, and the plain FP64 GPU path on the same batch."""
     import ziran2020_gb300 as zr
     from ziran2020_gb300 import workloads
 
-    recs = workloads.batch_recipes(seed=20200713 + rank)
     n = workloads.total_particles(recs)
     b = zr.Batch(zr.F32)
     for r in recs:
@@ -293,39 +317,69 @@ def run_batch(args, world, rank):
     b.commit()
     clocks = ClockSampler()
     clocks.start()
-    b.step(args.warmup)
+    b.step(warmup)
     barrier(world)
-    b.step(args.steps)
+    b.step(steps)
     ms = b.last_step_ms
     barrier(world)
     clock_info = clocks.stop()
-    ms_max = allreduce_max(world, ms)
-    value = allreduce_sum(world, n) * args.steps / (ms_max / 1e3)
     stats = b.stats()
     b.set_timing(True)
-    b.step(min(args.steps, 20))
+    b.step(min(steps, 20))
     phases, ksteps = b.timing()
     b.set_timing(False)
     per = {k: v / ksteps for k, v in phases.items()}
+    schedule = b.schedule()
+    del b
     peak, peak_kind = measured_peaks()
-    blocks = None
     alg = algorithmic_bytes(4, n, 0, 64, False)  # particle bytes only: the batch reports no block count
     dom = max(("p2g", "g2p"), key=lambda k: per[k])
     achieved = alg[dom] / (per[dom] / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "traffic": profiled_traffic(dom, "batch256"),
             "algorithmic_bytes": alg[dom], "kernel_ms": round(per[dom], 4), "phase_ms_per_substep": {k: round(v, 4) for k, v in per.items()},
+            "frac_by_phase": {k: round(alg[k] / (per[k] / 1e3) / 1e9 / peak, 4) for k in ("p2g", "g2p") if per.get(k)},
             "note": "algorithmic bytes count particle traffic only (grid nodes excluded)"}
+    b64 = zr.Batch(zr.F64)
+    for r in recs:
+        b64.add_recipe(r)
+    b64.step(2)
+    b64.step(fp64_steps)
+    fp64_value = n * fp64_steps / (b64.last_step_ms / 1e3)
+    del b64
+    return {"particles": int(n), "ms": ms, "stats": stats, "clocks": clock_info, "roofline": roof, "schedule": schedule, "fp64_value": fp64_value}
+
+
+def batch_summary(args):
+    """The 256-scene batch of elastic boxes (N log-uniform in 5k-400k) beside the single-scene line: throughput,
+    roofline fraction and the plain FP64 GPU path on the same batch."""
+    from ziran2020_gb300 import workloads
+
+    recs = workloads.batch_recipes(seed=20200713)
+    m = measure_batch(recs, args.batch_steps, max(3, args.warmup), fp64_steps=args.fp64_steps)
+    value = m["particles"] * args.batch_steps / (m["ms"] / 1e3)
+    return {"workload": "batch256", "scenes": len(recs), "particles": m["particles"], "metric": "particle-substeps/sec", "value": value,
+            "unit": "particle-substeps/s", "steps": args.batch_steps, "ms_per_step": m["ms"] / args.batch_steps, "roofline": m["roofline"],
+            "clocks": m["clocks"], "schedule": m["schedule"], "gpu_launches": int(m["stats"]["launches_per_step"]) * args.batch_steps,
+            "fp64_path": {"value": m["fp64_value"], "unit": "particle-substeps/s", "fp32_over_fp64": value / m["fp64_value"]}}
+
+
+def run_batch(args, world, rank):
+    """256 independent elastic boxes (N log-uniform in 5k-400k, E ~ U(5e3, 5e4), centre ~ U[0.3,0.7]^3,
+    v0 ~ U[-1,1]^3; dx = 1/64, dt = 1e-4) advanced together: one launch per kernel for the whole batch."""
+    from ziran2020_gb300 import workloads
+
+    recs = workloads.batch_recipes(seed=20200713 + rank)
+    m = measure_batch(recs, args.steps, args.warmup, world, fp64_steps=args.fp64_steps)
+    n = m["particles"]
+    ms_max = allreduce_max(world, m["ms"])
+    value = allreduce_sum(world, n) * args.steps / (ms_max / 1e3)
     cpu = None
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
         import pyoracle as po
-        import scenes
 
-        desc = scenes.elastic_box(size=0.25, dx=1 / 64)
-        o = scenes.oracle_scene(desc, 8)
-        ns = len(desc["m"])
+        o, ns = po.recipe_scene(0, 8, seed=12345)
         o.step(1)
         t0 = time.perf_counter()
         o.step(20)
@@ -333,46 +387,37 @@ def run_batch(args, world, rank):
         cpu = {"value": ns * 20 / el, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
                "sample": f"one {ns}-particle elastic box of the family (dx=1/64), 20 substeps; the batch would run its scenes one by one"}
     cfg = {"workload": "batch256", "scenes": len(recs), "particles": int(n), "substeps_timed": args.steps, "precision_path": "fp32",
-           "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{world}", "schedule": b.schedule()}
-    del b
-    # the plain FP64 GPU path on the same batch
-    b64 = zr.Batch(zr.F64)
-    for r in recs:
-        b64.add_recipe(r)
-    b64.step(2)
-    b64.step(args.fp64_steps)
-    fp64_value = n * args.fp64_steps / (b64.last_step_ms / 1e3)
-    del b64
+           "l2": "particle state larger than L2 (no flush needed)", "parallelism": f"replicas x{world}", "schedule": m["schedule"]}
     line = {"metric": "particle-substeps/sec", "value": value, "unit": "particle-substeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded recipe family)", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
+            "dtype": "f32", "data": "synthetic (seeded recipe family)", "config": cfg, "roofline": m["roofline"], "cpu_baseline": cpu,
             "e2e": {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "measured on the single-scene workload"},
-            "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
-            "clocks": clock_info, "fp64_fallbacks": stats["fallbacks"],
-            "fp64_path": {"value": fp64_value, "unit": "particle-substeps/s", "fp32_over_fp64": value / world / fp64_value}}
+            "gpu_launches": int(m["stats"]["launches_per_step"]) * args.steps, "kernels_per_substep": int(m["stats"]["launches_per_step"]),
+            "clocks": m["clocks"], "fp64_fallbacks": m["stats"]["fallbacks"],
+            "fp64_path": {"value": m["fp64_value"], "unit": "particle-substeps/s", "fp32_over_fp64": value / world / m["fp64_value"]}}
     return line if rank == 0 else None
 
 
-def run_serve(args, world, rank):
+def serve_sweep(rates, count, tick, seed_base=4242):
     """Poisson stream of scene-advance requests (elastic or AnisoMPM family, 10k-2M particles log-uniform,
-    50-500 substeps uniform), FP32, state resident on the device, admission by a 60 GB budget; p50/p99
-    request latency (submit -> result on the host) and aggregate particle-substeps/s per arrival rate."""
+    50-500 substeps uniform), FP32, state resident on the device, admission by a 60 GB budget; per arrival rate
+    the p50/p99 request latency (submit -> result on the host) and the aggregate particle-substeps/s."""
     import numpy as np
 
     import ziran2020_gb300 as zr
     from ziran2020_gb300 import workloads
 
     sweep = []
-    for ri, lam in enumerate(float(r) for r in args.rates.split(",")):
-        reqs = workloads.request_stream(seed=4242 + 17 * ri + 1000 * rank, count=args.requests)
+    for ri, lam in enumerate(rates):
+        reqs = workloads.request_stream(seed=seed_base + 17 * ri, count=count)
         built = []
         for r, steps in reqs:
             sc = zr.Scene(zr.F32)
             sc.from_recipe(r)  # host-side scene construction happens before the clock starts
             built.append((sc, steps, zr.recipe_count(r)))
         arrivals = np.cumsum(np.random.default_rng(99 + ri).exponential(1.0 / lam, len(reqs)))
-        sv = zr.Server(zr.F32, budget_bytes=60e9, tick_substeps=args.tick, max_scenes=256)
+        sv = zr.Server(zr.F32, budget_bytes=60e9, tick_substeps=tick, max_scenes=256)
         ids, k = [], 0
         t0 = time.perf_counter()
         while True:
@@ -394,6 +439,21 @@ def run_serve(args, world, rank):
                       "throughput": ps / wall, "device_throughput": st["particle_substeps"] / (st["device_ms"] / 1e3),
                       "peak_device_bytes": st["device_bytes"]})
         del sv, built
+    return sweep
+
+
+def serve_summary(args):
+    """Continuous batching under a Poisson request stream, beside the single-scene line (bounded: a few rates and
+    requests)."""
+    rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
+    sweep = serve_sweep(rates, args.serve_requests, args.tick)
+    return {"workload": "serve", "metric": "p50/p99 request latency (s) and aggregate particle-substeps/s", "requests_per_rate": args.serve_requests,
+            "budget_bytes": 60e9, "tick_substeps": args.tick, "precision_path": "fp32", "rates": sweep}
+
+
+def run_serve(args, world, rank):
+    """The serving workload on its own line: the sweep over --rates with --requests per rate."""
+    sweep = serve_sweep([float(r) for r in args.rates.split(",")], args.requests, args.tick, seed_base=4242 + 1000 * rank)
     best = max(sweep, key=lambda e: e["throughput"])
     cfg = {"workload": "serve", "requests_per_rate": args.requests, "rates_per_s": [e["rate_per_s"] for e in sweep], "budget_bytes": 60e9,
            "tick_substeps": args.tick, "precision_path": "fp32", "parallelism": f"replicas x{world}"}
@@ -496,25 +556,52 @@ def run_ours(args, world, rank):
     fp64_value = n * args.fp64_steps / (s64.last_step_ms / 1e3)
     del s64
 
-    # FP32 vs FP64 after the same numbers of substeps from the same seeded inputs (the FP64 GPU path is
-    # pinned to the FP64 oracle by tests/test_gpu_parity.py; a full-size oracle run would take hours)
-    acc = None
+    # FP32 against the FP64 GPU path at the --accuracy-steps marks, and both GPU paths against the FP64 oracle
+    # on the whole workload (the same inputs) after --oracle-slab-steps substeps; that oracle run, timed over
+    # its substeps after the first, is also the CPU baseline (the oracle on all host threads, kind "port")
+    acc, slab_vs_oracle, cpu, late = None, None, None, None
     marks = sorted({int(v) for v in str(args.accuracy_steps).split(",") if v.strip() and int(v) > 0})
-    if marks and rank == 0:
+    K = 0 if args.no_cpu else max(0, args.oracle_slab_steps)
+    if rank == 0 and (marks or K):
+        ref = None
+        if K:
+            o, no = oracle_workload(kind, over, seed=12345 + rank, inputs=zr.recipe_generate(r))
+            import pyoracle as po
+
+            t0 = time.perf_counter()
+            o.step(1)
+            first = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            if K > 1:
+                o.step(K - 1)
+            el = time.perf_counter() - t0
+            ref = o.state()
+            del o
+            timed, secs = (K - 1, el) if K > 1 else (1, first)
+            cpu = {"value": no * timed / secs, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
+                   "sample": f"the whole workload ({no} particles, same inputs), substeps {2 if K > 1 else 1}-{K}: {secs:.1f} s"}
         a32, a64 = zr.Scene(zr.F32), zr.Scene(zr.F64)
         a32.from_recipe(r)
         a64.from_recipe(r)
-        acc = {"reference": "FP64 GPU path", "x_unit": "metres in a unit domain (domain-relative)", "at": []}
+        acc = {"reference": "FP64 GPU path", "x_unit": "metres in a unit domain (domain-relative)", "at": []} if marks else None
         done = 0
-        for mk in marks:
+        for mk in sorted(set(marks) | ({K} if K else set())):
             a32.step(mk - done)
+            seg_ms = a32.last_step_ms
             a64.step(mk - done)
+            if mk == max(marks or [0]) and mk - done >= 50:
+                # the timed value covers the first substeps of the pull; the damage grows later (more particles take
+                # the tensile split): device throughput over the last segment of this run, graph-launched as well
+                late = {"substeps": f"{done + 1}-{mk}", "value": n * (mk - done) / (seg_ms / 1e3), "unit": "particle-substeps/s"}
             done = mk
-            row = {"substeps": mk}
-            for f in ("x", "v", "F", "d"):
-                e = np.abs(a32.get(f) - a64.get(f))
-                row[f] = {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
-            acc["at"].append(row)
+            s32 = {f: a32.get(f) for f in ("x", "v", "F", "d")}
+            s64 = {f: a64.get(f) for f in ("x", "v", "F", "d")}
+            if mk in marks:
+                acc["at"].append({"substeps": mk, **field_errors(s32, s64)})
+            if mk == K:
+                slab_vs_oracle = {"scene": f"{args.workload}, {n} particles, {K} substeps, inputs shared with the oracle",
+                                  "reference": "FP64 oracle (CPU)", "x_unit": "metres in a unit domain (domain-relative)",
+                                  "fp32": field_errors(s32, ref), "fp64": field_errors(s64, ref)}
         del a32, a64
 
     # FP32 and FP64 GPU paths against the FP64 oracle on the elastic cube (32,768 particles, dx = 1/64,
@@ -522,27 +609,6 @@ def run_ours(args, world, rank):
     vs_oracle = None
     if rank == 0 and not args.no_cpu and args.oracle_steps > 0:
         vs_oracle = error_vs_oracle(args.oracle_steps)
-
-    # CPU baseline: the oracle restatement on a bounded sample of the same workload, all host threads
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        import pyoracle as po
-        import scenes
-
-        desc = _desc_for(kind, CPU_SAMPLE[args.workload], scenes)
-        o = scenes.oracle_scene(desc, 8)
-        ns = len(desc["m"])
-        t0 = time.perf_counter()
-        o.step(1)
-        one = time.perf_counter() - t0
-        k = max(1, min(50, int(args.cpu_seconds / max(one, 1e-3))))
-        t0 = time.perf_counter()
-        o.step(k)
-        el = time.perf_counter() - t0
-        cpu = {"value": ns * k / el, "unit": "particle-substeps/s", "cores": po.num_threads(), "kind": "port", "precision": "f64",
-               "sample": f"{ns} particles ({desc['dx']:.6g} m cells, cropped slab piece), {k} substeps, {el:.1f} s"}
 
     cfg = _config(args)
     cfg["particles"] = int(n)
@@ -558,7 +624,12 @@ def run_ours(args, world, rank):
             "dtype": "f32", "data": "synthetic (seeded recipe)", "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(stats["launches_per_step"]) * args.steps, "kernels_per_substep": int(stats["launches_per_step"]),
             "clocks": clock_info, "fp64_path": {"value": fp64_value, "unit": "particle-substeps/s", "fp32_over_fp64": value / world / fp64_value},
-            "fp32_vs_fp64_error": acc, "error_vs_fp64_oracle": vs_oracle, "fp64_fallbacks": stats["fallbacks"]}
+            "late_state": late, "fp32_vs_fp64_error": acc, "error_vs_fp64_oracle": vs_oracle, "error_vs_fp64_oracle_slab": slab_vs_oracle,
+            "fp64_fallbacks": stats["fallbacks"]}
+    if rank == 0 and not args.no_batch:
+        line["batch"] = batch_summary(args)
+    if rank == 0 and not args.no_serve:
+        line["serving"] = serve_summary(args)
     return line if rank == 0 else None
 
 

@@ -281,9 +281,12 @@ const char* zr_server_last_error(zr_server* sv);
  * (capacity n); *n_groups (host) the number of blocks. All scratch lives in one static device array of
  * ZR_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; n above ZR_NOALLOC_MAX_PARTICLES is
  * rejected with ZR_ERR_ARG. The first call on a device resolves that array's address and sizes the
- * sort (no allocation): make it before any stream capture. Calls share the array, so calls that overlap
- * on the GPU (different streams or threads) race; serialise them. Returns ZR_ERR_OUT_OF_DOMAIN when a
- * base node lies outside [0, domain_cells) (0 = the full SPGrid range). The call synchronises `stream`. */
+ * sort (no allocation): make it before any stream capture. The first call of each precision also loads
+ * that precision's kernels (lazy module loading), so a caller that must see no device memory change during
+ * its run makes one warm-up call per precision at start-up. Calls must use the device's primary context
+ * (the runtime API's context). Calls share the array, so calls that overlap on the GPU (different streams
+ * or threads) race; serialise them. Returns ZR_ERR_OUT_OF_DOMAIN when a base node lies outside
+ * [0, domain_cells) (0 = the full SPGrid range). The call synchronises `stream` before it returns. */
 #define ZR_NOALLOC_MAX_PARTICLES (1 << 20)
 #define ZR_NOALLOC_SCRATCH_BYTES (16u << 20)
 int zr_bin_device_noalloc(int precision, int64_t n, const void* x, double dx, int32_t domain_cells, uint64_t* sorted_keys, int32_t* order,

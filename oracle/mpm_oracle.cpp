@@ -42,6 +42,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <random>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -1485,6 +1486,54 @@ using namespace orc;
         }                                      \
     } while (0)
 
+// ----------------------------------------------------------------------------------------------
+// Seeded scene inputs, restated here so that the CPU baseline builds its inputs without the product
+// library. The sampling is the reference's (MpmInitializationHelper.h:1344-1414 samples a jittered
+// lattice; MpmParticleHandleBase.cpp:175-268 draws fibres and turns one director into F with
+// initializeRotatedFHelper); the random stream is the library's recipe format: raw std::mt19937_64
+// outputs (defined bit for bit by the C++ standard), uniforms from the top 53 bits, normals by
+// Box-Muller, fibres from a von Mises-Fisher law about +x by Wood's method for the 2-sphere. Per
+// particle, in lattice order (cell i, j, k; sub-cell a, b, c): three jitter uniforms; for the slab also
+// a fibre (two uniforms) and sigma_c (two uniforms).
+// ----------------------------------------------------------------------------------------------
+struct SeedStream {
+    std::mt19937_64 g;
+    explicit SeedStream(uint64_t seed) : g(seed) {}
+    double u01() { return (double)(g() >> 11) * 0x1.0p-53; }
+    double gauss()
+    {
+        const double a = std::max(u01(), 1e-300), b = u01();
+        return std::sqrt(-2.0 * std::log(a)) * std::cos(2.0 * M_PI * b);
+    }
+    void fibre(double kappa, double d[3])
+    {
+        const double u = u01();
+        const double w = std::min(1.0, std::max(-1.0, 1.0 + std::log(u + (1.0 - u) * std::exp(-2.0 * kappa)) / kappa));
+        const double ph = 2.0 * M_PI * u01(), r = std::sqrt(std::max(0.0, 1.0 - w * w));
+        d[0] = w;
+        d[1] = r * std::cos(ph);
+        d[2] = r * std::sin(ph);
+    }
+};
+
+// initializeRotatedFHelper for one director a (MpmParticleHandleBase.cpp:224-268): F's columns are a,
+// a_perp = normalize(-a_y, a_x, 0) (e_x when a lies along z) and a x a_perp
+inline void rotated_F(const double a[3], double F[9])
+{
+    double p[3] = { 1, 0, 0 };
+    if (!(std::fabs(a[0]) < 1e-6 && std::fabs(a[1]) < 1e-6)) {
+        const double len = std::sqrt(a[1] * a[1] + a[0] * a[0]);
+        p[0] = -a[1] / len;
+        p[1] = a[0] / len;
+    }
+    const double q[3] = { a[1] * p[2] - a[2] * p[1], a[2] * p[0] - a[0] * p[2], a[0] * p[1] - a[1] * p[0] };
+    for (int r = 0; r < 3; r++) {
+        F[3 * r] = a[r];
+        F[3 * r + 1] = p[r];
+        F[3 * r + 2] = q[r];
+    }
+}
+
 extern "C" {
 
 void* orc_create(int precision, double dx, double dt, const double* gravity, double apic_ratio, double cfl)
@@ -1785,6 +1834,52 @@ void orc_reductions(void* hp, double* out)
         out[4] = KE;
         out[5] = vmax;
     });
+}
+
+// Seeded inputs of a box or slab of size[3] metres centred at center[3], snapped to whole cells of dx, ppc_side^3
+// particles per cell. kind 0: elastic box (F = I, sigma_c = 1); kind 1: fibre slab (F from a vMF(kappa) fibre
+// about +x, sigma_c ~ N(sc_mean, sc_std)). Any output may be NULL. Returns the particle count; with x == NULL only
+// the count is computed. lo_cell (3 ints, may be NULL) receives the first cell of the lattice.
+int64_t orc_seeded_inputs(int kind, int ppc_side, uint64_t seed, double dx, const double* size, const double* center, const double* vel, double rho,
+    double kappa, double sc_mean, double sc_std, double* x, double* v, double* m, double* V0, double* F, double* sigma_c, int64_t* lo_cell)
+{
+    if (!(dx > 0) || ppc_side <= 0) return -1;
+    int64_t nc[3], lo[3];
+    for (int a = 0; a < 3; a++) {
+        nc[a] = std::max<int64_t>(1, std::llround(size[a] / dx));
+        lo[a] = std::llround((center[a] - 0.5 * (double)nc[a] * dx) / dx);
+        if (lo_cell) lo_cell[a] = lo[a];
+    }
+    const int64_t per = (int64_t)ppc_side * ppc_side * ppc_side, count = nc[0] * nc[1] * nc[2] * per;
+    if (!x) return count;
+    const double h = dx / ppc_side, vol = dx * dx * dx / (double)per;
+    SeedStream rs(seed);
+    int64_t p = 0;
+    for (int64_t i = 0; i < nc[0]; i++)
+        for (int64_t j = 0; j < nc[1]; j++)
+            for (int64_t k = 0; k < nc[2]; k++)
+                for (int64_t sub = 0; sub < per; sub++, p++) {
+                    const int64_t cell[3] = { lo[0] + i, lo[1] + j, lo[2] + k };
+                    const int64_t sl[3] = { sub / (ppc_side * ppc_side), (sub / ppc_side) % ppc_side, sub % ppc_side };
+                    for (int a = 0; a < 3; a++) {
+                        const double u = rs.u01();
+                        const double base = (double)cell[a] * dx, off = ((double)sl[a] + u) * h;
+                        x[3 * p + a] = base + off;
+                        if (v) v[3 * p + a] = vel[a];
+                    }
+                    if (m) m[p] = rho * vol;
+                    if (V0) V0[p] = vol;
+                    double Fp[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 }, sc = 1.0;
+                    if (kind == 1) {
+                        double dir[3];
+                        rs.fibre(kappa, dir);
+                        rotated_F(dir, Fp);
+                        sc = sc_mean + sc_std * rs.gauss();
+                    }
+                    if (F) std::memcpy(F + 9 * p, Fp, sizeof Fp);
+                    if (sigma_c) sigma_c[p] = sc;
+                }
+    return count;
 }
 
 int orc_num_threads()

@@ -57,6 +57,8 @@ def lib():
         L.orc_svd3.argtypes = [i32, P(d), P(d), P(d), P(d)]
         L.orc_reductions.argtypes = [vp, P(d)]
         L.orc_num_threads.restype = i32
+        L.orc_seeded_inputs.restype = i64
+        L.orc_seeded_inputs.argtypes = [i32, i32, u64, d, P(d), P(d), P(d), d, d, d, d] + [P(d)] * 6 + [P(i64)]
         _lib = L
     return _lib
 
@@ -173,3 +175,63 @@ def tau(precision, model, E, nu, F, g=1.0, effective=False, kx_scale=0.0, ky_sca
 
 def num_threads():
     return int(lib().orc_num_threads())
+
+
+# Scene families of the benchmarks (the library's recipe defaults, restated): kind 0 = elastic box, kind 1 =
+# AnisoMPM fibre slab. Values: MpmSimulationBase.cpp:39-48 (cfl 0.6), examples/vonMisesTear.h:28 (RPIC for the
+# AnisoMPM demos), anisofractureBatch3D.py:144-147 (eta 0.1, zeta 1, residual 0.01).
+RECIPE_DEFAULTS = {
+    0: dict(dx=1 / 64, dt=1e-4, size=(0.25, 0.25, 0.25), center=(0.5, 0.6, 0.5), velocity=(0.0, -1.0, 0.0), gravity=(0.0, -9.8, 0.0),
+            E=1e4, nu=0.3, rho=1000.0, apic=1.0, ground_y=0.05),
+    1: dict(dx=1 / 128, dt=5e-5, size=(0.5, 0.1, 0.5), center=(0.5, 0.5, 0.5), velocity=(0.0, 0.0, 0.0), gravity=(0.0, 0.0, 0.0),
+            E=5e4, nu=0.25, rho=800.0, apic=0.0, kappa=20.0, alpha=-1.0, l0=None, eta=0.1, zeta=1.0, residual=0.01,
+            sigma_c=(400.0, 40.0), pull=0.5, grip=2, model=1, fiber=0.0),
+}
+
+
+def seeded_inputs(kind, seed=12345, ppc_side=2, **over):
+    """Particles of a recipe scene from the oracle's own generator: dict of x, v, m, V0, F, sigma_c (float64)
+    plus the scene parameters used."""
+    p = dict(RECIPE_DEFAULTS[kind])
+    p.update(over)
+    size, center, vel = (np.asarray(p[k], dtype=np.float64) for k in ("size", "center", "velocity"))
+    sc = p.get("sigma_c", (1.0, 0.0))
+    L = lib()
+    args = [kind, ppc_side, seed, p["dx"], _p(size), _p(center), _p(vel), p["rho"], p.get("kappa", 0.0), sc[0], sc[1]]
+    n = L.orc_seeded_inputs(*args, None, None, None, None, None, None, None)
+    if n <= 0:
+        raise ValueError("empty recipe")
+    out = {"x": np.zeros((n, 3)), "v": np.zeros((n, 3)), "m": np.zeros(n), "V0": np.zeros(n), "F": np.zeros((n, 9)), "sigma_c": np.zeros(n)}
+    lo = np.zeros(3, np.int64)
+    L.orc_seeded_inputs(*args, *(_p(out[k]) for k in ("x", "v", "m", "V0", "F", "sigma_c")), _p(lo, C.c_int64))
+    nc = [max(1, int(round(s_ / p["dx"]))) for s_ in size]
+    p["lo_cell"], p["cells"] = lo.tolist(), nc
+    return out, p
+
+
+def recipe_scene(kind, precision=8, seed=12345, inputs=None, **over):
+    """An OracleScene of a recipe family with inputs from seeded_inputs: the elastic box (corotated, sticky ground)
+    or the fibre slab (Neo-Hookean Borden or QR-stable with anisotropic damage, ends pulled apart by sticky
+    plates grip cells wide). inputs: particle arrays (x, v, m, V0, F, sigma_c) to use instead of the generated
+    ones (the same scene fed with another generator's particles). Returns (scene, particle count)."""
+    inp, p = seeded_inputs(kind, seed=seed, **over)
+    if inputs is not None:
+        if len(inputs["m"]) != len(inp["m"]):
+            raise ValueError("inputs of another particle count")
+        inp = {k: np.asarray(inputs[k], dtype=np.float64).reshape(inp[k].shape) for k in inp}
+    dx = p["dx"]
+    o = OracleScene(precision, dx, p["dt"], p["gravity"], p["apic"], 0.6)
+    if kind == 0:
+        o.add_material(0, p["E"], p["nu"])
+        o.add_halfspace((0.0, p["ground_y"], 0.0), (0.0, 1.0, 0.0), 1, 0.0)
+        o.set_particles(inp["x"], inp["v"], inp["m"], inp["V0"], F=inp["F"])
+    else:
+        l0 = p["l0"] if p.get("l0") is not None else 0.5 * dx
+        o.add_material(p["model"], p["E"], p["nu"], True, p["alpha"], l0, p["eta"], p["zeta"], p["residual"], kx_scale=p["fiber"])
+        x_lo, x_hi = p["lo_cell"][0] * dx, (p["lo_cell"][0] + p["cells"][0]) * dx
+        o.add_halfspace((x_lo + p["grip"] * dx, 0.0, 0.0), (1.0, 0.0, 0.0), 1, 0.0, (-p["pull"], 0.0, 0.0))
+        o.add_halfspace((x_hi - p["grip"] * dx, 0.0, 0.0), (-1.0, 0.0, 0.0), 1, 0.0, (p["pull"], 0.0, 0.0))
+        o.set_particles(inp["x"], inp["v"], inp["m"], inp["V0"], F=inp["F"], sigma_c=inp["sigma_c"])
+        if p.get("implicit"):
+            o.set_implicit_damage(True)
+    return o, len(inp["m"])

@@ -31,3 +31,35 @@ def test_batch_matches_single_scenes(prec):
         for f in ("x", "v", "F", "d"):
             a, c = b.get(k, f), sc.get(f)
             assert np.abs(a - c).max() <= tol[f] * max(1.0, np.abs(c).max()), (k, f, np.abs(a - c).max())
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_batch_reductions_match_single_scenes(prec):
+    """Per-scene FP64 reductions of a batch of four scenes of different sizes (MpmSimulationDataAnalysis.h:67-80,
+    130-151): particle mass, momentum, kinetic energy and the grid mass of the last P2G equal each scene's own
+    values. Grid blocks of different scenes share warps and CTAs of the grid update, so a per-warp or per-CTA
+    attribution would move mass between scenes. The grid mass is a sum of FP64 (FP32) node masses that the
+    batch and the lone scene add in different orders: relative 1e-12 (1e-5)."""
+    descs = [scenes.elastic_box(size=0.0625, seed=1, center=(0.4, 0.5, 0.5)),
+             scenes.elastic_box(size=0.125, seed=2, E=3e4, v0=(0.5, -0.5, 0.2)),
+             scenes.elastic_box(size=0.03125, seed=3, center=(0.6, 0.4, 0.55), v0=(0.0, 0.3, -0.7)),
+             scenes.aniso_slab(size=(0.08, 0.04, 0.08), sigma_c=(20.0, 2.0), pull=1.0)]
+    b = zr.Batch(prec)
+    singles = []
+    for d in descs:
+        sc = scenes.gpu_scene(d, prec)
+        b.add_scene(sc)
+        singles.append(sc)
+    b.commit()
+    b.step(5)
+    rtol = 1e-12 if prec == 8 else 1e-5
+    for k, sc in enumerate(singles):
+        sc.step(5)
+        rb, rs = b.reductions(k), sc.reductions()
+        m = rs[0]
+        assert m > 0
+        assert abs(rb[0] - m) <= 1e-14 * m, (k, rb[0], m)  # particle mass: the same particles
+        assert abs(rs[6] - m) <= 10 * rtol * m, (k, rs[6], m)  # the lone scene's grid holds its mass
+        assert abs(rb[6] - rs[6]) <= rtol * m, (k, rb[6], rs[6])  # and the batch attributes the same to it
+        p_scale = m * max(1.0, float(np.abs(rs[1:4]).max()) / m)
+        np.testing.assert_allclose(rb[1:4], rs[1:4], rtol=0, atol=(1e-11 if prec == 8 else 1e-5) * p_scale)

@@ -1,0 +1,62 @@
+"""GPU: the AnisoMPM slab exactly as the plain-FP64 benchmark scene states it, against the FP64 oracle.
+
+dx = 1/128, a 0.5 x 0.1 x 0.5 m slab with 8 particles per cell (425,984 particles), Neo-Hookean (Borden)
+E = 5e4 Pa, nu = 0.25, rho = 800, fibres vMF(kappa = 20) about +x, anisotropic damage alpha = -1,
+l0 = 0.5 dx, sigma_c ~ N(400, 40) Pa, d = 0, the two x-ends pulled apart at +-0.5 m/s, dt = 5e-5, all 500
+substeps (Projects/anisofracture/AnisoFractureSimulation.h:129-283, Lib/MPM/MpmSimulationBase.cpp:262-357).
+
+Bounds: the FP64 GPU path differs from the oracle only in the order of the grid sums: positions within
+1e-11 m (domain-relative in the unit box), damage within 1e-8. The FP32 path: positions within 1e-4 of the
+domain (the path's stated bound); its damage against the FP64 oracle within the bounds measured on this
+scene with about 3x margin (the damage threshold phi > 1 turns FP32 rounding of the stress into damage
+differences at the particles that sit on it). Max and RMS errors are printed."""
+import numpy as np
+import pytest
+
+import ziran2020_gb300 as zr
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 500
+
+
+@pytest.fixture(scope="module")
+def slab_and_oracle():
+    d = scenes.aniso_slab(size=(0.5, 0.1, 0.5), dx=1 / 128, seed=12345, sigma_c=(400.0, 40.0), pull=0.5)
+    assert len(d["m"]) == 425984
+    o = scenes.oracle_scene(d, 8)
+    o.step(200)
+    r200 = o.state()
+    o.step(STEPS - 200)
+    return d, r200, o.state()
+
+
+def _run(d, prec, steps):
+    s = scenes.gpu_scene(d, prec)
+    s.step(steps[0])
+    a = scenes.gpu_state(s)
+    s.step(steps[1] - steps[0])
+    return a, scenes.gpu_state(s)
+
+
+def test_config1_fp64_matches_oracle(slab_and_oracle):
+    d, r200, r500 = slab_and_oracle
+    g200, g500 = _run(d, zr.F64, (200, STEPS))
+    for tag, g, r in (("200", g200, r200), ("500", g500, r500)):
+        e = scenes.errors(g, r)
+        print(f"FP64 GPU vs FP64 oracle after {tag} substeps: {e}")
+        assert e["x"][0] <= 1e-11, (tag, e)
+        assert e["d"][0] <= 1e-8, (tag, e)
+    assert r500["d"].max() > 0.5  # the slab tore: the comparison covers grown damage
+
+
+def test_config1_fp32_within_bounds_of_fp64_oracle(slab_and_oracle):
+    d, r200, r500 = slab_and_oracle
+    g200, g500 = _run(d, zr.F32, (200, STEPS))
+    for tag, g, r, dmax, drms in (("200", g200, r200, 2e-2, 1e-3), ("500", g500, r500, 2e-2, 1e-3)):
+        e = scenes.errors(g, r)
+        print(f"FP32 GPU vs FP64 oracle after {tag} substeps: {e}")
+        assert e["x"][0] <= 1e-4, (tag, e)
+        assert e["d"][0] <= dmax, (tag, e)
+        assert e["d"][1] <= drms, (tag, e)

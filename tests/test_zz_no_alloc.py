@@ -5,7 +5,8 @@ start-up, a loop with a fixed budget, a callback inside another runtime); all it
 device array shared by every call. This file is collected last so that a failure here comes after every
 other test has run. Its output must equal, bit for bit, the binning of the allocating scene API
 (zr_scene_binning) on the same positions, on two consecutive calls (the second smaller than the first,
-so stale scratch from the first call would show up)."""
+so stale scratch from the first call would show up); a call after the warm-up calls must leave the device's
+free memory unchanged; a particle outside the stated domain is reported."""
 import ctypes as C
 
 import numpy as np
@@ -74,3 +75,57 @@ def test_noalloc_rejects_sizes_beyond_its_static_scratch():
     p = C.c_void_p(dummy.data_ptr())
     ng = C.c_int64()
     assert L.zr_bin_device_noalloc(zr.F32, big, p, 1 / 64, 0, p, p, p, C.byref(ng), None) == zr.ZR_ERR_ARG
+
+
+def _noalloc_call(L, prec, xd, n, dx, domain_cells, keys, order, first, ng, stream):
+    return L.zr_bin_device_noalloc(prec, n, C.c_void_p(xd.data_ptr()), dx, domain_cells, C.c_void_p(keys.data_ptr()),
+                                   C.c_void_p(order.data_ptr()), C.c_void_p(first.data_ptr()), C.byref(ng), C.c_void_p(stream))
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """The property the entry point exists for: once each precision has been called (set-up and kernel
+    loading), a call changes the device's free memory by nothing (cudaMemGetInfo before and after)."""
+    import torch
+
+    L = zr.load_library()
+    dx = 1 / 128
+    x = positions(5, 32, dx, (0.3, 0.3, 0.3))
+    n = len(x)
+    bufs = {}
+    for prec, dtype in ((zr.F32, torch.float32), (zr.F64, torch.float64)):
+        bufs[prec] = (torch.tensor(x.reshape(-1), dtype=dtype, device="cuda"), torch.empty(n, dtype=torch.int64, device="cuda"),
+                      torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"))
+    stream = torch.cuda.current_stream().cuda_stream
+    ng = C.c_int64(-1)
+    for prec in (zr.F32, zr.F64):  # warm-up: per-device set-up and each precision's kernels
+        xd, keys, order, first = bufs[prec]
+        assert _noalloc_call(L, prec, xd, n, dx, 0, keys, order, first, ng, stream) == zr.ZR_OK
+    torch.cuda.synchronize()
+    for prec in (zr.F32, zr.F64):
+        xd, keys, order, first = bufs[prec]
+        free0 = torch.cuda.mem_get_info()[0]
+        assert _noalloc_call(L, prec, xd, n, dx, 0, keys, order, first, ng, stream) == zr.ZR_OK
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0, prec
+
+
+def test_noalloc_reports_particles_outside_the_domain():
+    """A base node at or beyond domain_cells gives ZR_ERR_OUT_OF_DOMAIN (the reference's SPGrid range
+    assertion); the next call with in-domain positions succeeds again (the flag is cleared per call)."""
+    import torch
+
+    L = zr.load_library()
+    dx = 1 / 64
+    x = positions(9, 12, dx, (0.2, 0.2, 0.2))
+    x[7] = (1.5, 0.3, 0.3)  # base node 95 in x, beyond a 68-cell domain
+    n = len(x)
+    xd = torch.tensor(x.reshape(-1), dtype=torch.float64, device="cuda")
+    keys = torch.empty(n, dtype=torch.int64, device="cuda")
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    first = torch.empty(n, dtype=torch.int32, device="cuda")
+    ng = C.c_int64(-1)
+    stream = torch.cuda.current_stream().cuda_stream
+    assert _noalloc_call(L, zr.F64, xd, n, dx, 68, keys, order, first, ng, stream) == zr.ZR_ERR_OUT_OF_DOMAIN
+    x[7] = (0.25, 0.3, 0.3)
+    xd.copy_(torch.tensor(x.reshape(-1), dtype=torch.float64))
+    assert _noalloc_call(L, zr.F64, xd, n, dx, 68, keys, order, first, ng, stream) == zr.ZR_OK

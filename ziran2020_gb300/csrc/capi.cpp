@@ -607,25 +607,31 @@ int zr_scene_load_state(zr_scene* s, const void* buf, int64_t bytes)
     if (bytes < state_bytes(s->precision, h.n, nf) || !(h.dt > 0) || !(h.time >= 0)) return set_err(s->err, ZR_ERR_ARG, "state image truncated or corrupt");
     const char* p = (const char*)buf + sizeof h;
     const size_t es = s->precision == ZR_F64 ? 8 : 4;
+    // the fields are written one at a time: a device checkpoint taken first is restored if any write fails, so
+    // the scene keeps either its old state or the whole image, never a mix
+    int rc = s->eng->checkpoint_save();
+    if (rc) {
+        s->err = s->eng->last_error();
+        return rc;
+    }
+    auto fail = [&](int code) {
+        s->err = s->eng->last_error();
+        if (s->eng->checkpoint_restore() != ZR_OK) s->err += " (and restoring the previous state failed)";
+        return code;
+    };
     for (int f = 0; f < nf; f++) {
-        int rc = s->eng->set_field(0, kStateFields[f], p, s->precision == ZR_F32);
-        if (rc) {
-            s->err = s->eng->last_error();
-            return rc;
-        }
+        rc = s->eng->set_field(0, kStateFields[f], p, s->precision == ZR_F32);
+        if (rc) return fail(rc);
         p += (size_t)h.n * kStateComps[f] * es;
     }
     if (nf < 9) { // an image without the history: it restarts from zero
         std::vector<char> zeros((size_t)h.n * es, 0);
-        int rc = s->eng->set_field(0, ZR_FIELD_DTILDE_MAX, zeros.data(), s->precision == ZR_F32);
-        if (rc) {
-            s->err = s->eng->last_error();
-            return rc;
-        }
+        rc = s->eng->set_field(0, ZR_FIELD_DTILDE_MAX, zeros.data(), s->precision == ZR_F32);
+        if (rc) return fail(rc);
     }
-    int rc = s->eng->set_time(0, h.time);
+    rc = s->eng->set_time(0, h.time);
     if (!rc) rc = s->eng->set_dt(0, h.dt);
-    if (rc) s->err = s->eng->last_error();
+    if (rc) return fail(rc);
     s->desc.dt = h.dt;
     return rc;
 }

@@ -1135,19 +1135,22 @@ template <class T>
 __global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    __shared__ double s_mass[GRID_NT / 32];
-    __shared__ int s_msc[GRID_NT / 32];
+    // GV consecutive nodes of one block per thread: every field moves as one 16-byte access; TPB threads cover
+    // one block (16 in both precisions), so a warp spans 32 / TPB blocks, which may belong to different scenes
+    constexpr int GV = (int)(16 / sizeof(T));
+    constexpr int TPB = L::nodes / GV;
+    static_assert(L::nodes % GV == 0, "a block holds whole vectors");
+    static_assert(32 % TPB == 0 && GRID_NT % TPB == 0, "a warp holds whole blocks");
+    __shared__ double s_mass[GRID_NT / TPB];
+    __shared__ int s_msc[GRID_NT / TPB];
     if (aborted_cta(a.st)) return;
     const uint32_t B = min(a.st->n_blocks, a.b_cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_blocks_seen = max(a.st->max_blocks_seen, B);
-    // GV consecutive nodes of one block per thread: every field moves as one 16-byte access
-    constexpr int GV = (int)(16 / sizeof(T));
-    static_assert(L::nodes % GV == 0, "a block holds whole vectors");
     const uint32_t total = B * (L::nodes / GV);
     // every thread of the CTA runs the same iterations (the loop holds barriers)
     for (uint32_t base = blockIdx.x * GRID_NT; base < total; base += gridDim.x * GRID_NT) {
         const uint32_t t = base + threadIdx.x;
-        T gm = 0;
+        double gm = 0; // grid mass of the thread's nodes, accumulated in FP64 from the first add
         int scene = -1;
         if (t < total) {
             const uint32_t b = t / (L::nodes / GV), e0 = (t % (L::nodes / GV)) * GV;
@@ -1169,7 +1172,7 @@ __global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
 #pragma unroll
             for (int k = 0; k < GV; k++) {
                 const T mk = m.v[k];
-                gm += mk;
+                gm += (double)mk;
                 if (mk != (T)0) {
                     const int e = (int)e0 + k;
                     const int lx = e >> (L::zbits + L::ybits), ly = (e >> L::zbits) & (L::sy - 1), lz = e & (L::sz - 1);
@@ -1191,21 +1194,21 @@ __global__ void __launch_bounds__(GRID_NT) k_grid(StepArgs<T> a)
             V[2 * FS] = o2;
             V[3 * FS] = o3;
         }
-        // grid mass per scene: nodes of one warp share a block (and so a scene) whenever L::nodes >= 32; the
-        // CTA's warps then combine their sums, one atomic per run of warps of one scene (a single scene would
-        // otherwise send every warp's atomic to the same address)
-        double s = (double)gm;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        const int sc0 = __shfl_sync(0xffffffffu, scene, 0);
-        if ((threadIdx.x & 31) == 0) {
-            s_mass[threadIdx.x >> 5] = s;
-            s_msc[threadIdx.x >> 5] = sc0;
+        // grid mass per scene (MpmSimulationDataAnalysis.h:130-151, FP64): the TPB threads of one block (one scene)
+        // sum in a segmented shuffle, then thread 0 combines the CTA's block sums, one atomic per run of blocks of
+        // one scene (a single scene would otherwise send every block's atomic to the same address). Threads past
+        // the last block form whole segments with scene -1 (total and base are multiples of TPB).
+        double s = gm;
+        for (int o = TPB / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPB);
+        if (threadIdx.x % TPB == 0) {
+            s_mass[threadIdx.x / TPB] = s;
+            s_msc[threadIdx.x / TPB] = scene;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             double run = 0;
             int rsc = -1;
-            for (int w = 0; w < GRID_NT / 32; w++) {
+            for (int w = 0; w < GRID_NT / TPB; w++) {
                 if (s_msc[w] != rsc) {
                     if (rsc >= 0 && run != 0.0) atomicAdd(&a.grid_mass[rsc], run);
                     rsc = s_msc[w];

@@ -32,8 +32,7 @@ constexpr int64_t kMaxN = ZR_NOALLOC_MAX_PARTICLES;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 struct DeviceScratch {
-    bool ready = false;
-    int status = ZR_OK;
+    bool ready = false; // set only by a set-up that succeeded
     unsigned char* base = nullptr; // device address of g_noalloc_scratch on this device
     size_t sort_bytes[2] = { 0, 0 }, sel_bytes[2] = { 0, 0 }; // CUB temporary storage at kMaxN (float, double keys)
 };
@@ -68,35 +67,34 @@ Layout layout(const DeviceScratch& d)
 }
 
 // Set-up, once per device, with that device current: resolve the array's device address and check that
-// the radix sort and the selection fit next to the key buffer.
+// the radix sort and the selection fit next to the key buffer. Only a set-up that succeeded is kept: after a
+// failure (for example a sticky error left by an unrelated earlier launch) the next call tries again. The
+// address belongs to the device's primary context (the runtime API's context), which every call must use.
 int setup(int dev)
 {
     std::lock_guard<std::mutex> lk(g_setup_mutex);
     DeviceScratch& d = g_dev[dev];
-    if (d.ready) return d.status;
-    d.ready = true;
+    if (d.ready) return ZR_OK;
+    DeviceScratch fresh;
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-        d.status = ZR_ERR_CUDA;
-        return d.status;
-    }
-    d.base = (unsigned char*)p;
+    if (e != cudaSuccess || !p) return ZR_ERR_CUDA;
+    fresh.base = (unsigned char*)p;
     uint64_t* k = nullptr;
     uint32_t* v = nullptr;
     uint32_t* cnt = nullptr;
     for (int t = 0; t < 2; t++) {
         cub::DoubleBuffer<uint64_t> kb(k, k);
         cub::DoubleBuffer<uint32_t> vb(v, v);
-        if (cub::DeviceRadixSort::SortPairs(nullptr, d.sort_bytes[t], kb, vb, (int64_t)kMaxN, 0, 64) != cudaSuccess
-            || cub::DeviceSelect::If(nullptr, d.sel_bytes[t], thrust::counting_iterator<uint32_t>(0), v, cnt, (int64_t)kMaxN, HeadOp{ k })
-                != cudaSuccess) {
-            d.status = ZR_ERR_CUDA;
-            return d.status;
-        }
+        if (cub::DeviceRadixSort::SortPairs(nullptr, fresh.sort_bytes[t], kb, vb, (int64_t)kMaxN, 0, 64) != cudaSuccess
+            || cub::DeviceSelect::If(nullptr, fresh.sel_bytes[t], thrust::counting_iterator<uint32_t>(0), v, cnt, (int64_t)kMaxN, HeadOp{ k })
+                != cudaSuccess)
+            return ZR_ERR_CUDA;
     }
-    d.status = layout(d).end <= kScratchBytes ? ZR_OK : ZR_ERR_CAPACITY;
-    return d.status;
+    if (layout(fresh).end > kScratchBytes) return ZR_ERR_CAPACITY;
+    fresh.ready = true;
+    d = fresh;
+    return ZR_OK;
 }
 
 template <class T>
