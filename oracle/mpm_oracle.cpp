@@ -757,13 +757,28 @@ inline bool resolve_halfspace(const HalfSpace<T>& h, T time, const T x[3], T v[3
     return true;
 }
 
-// CollisionObject.cpp:67-105: objects are applied in order; a STICKY hit ends the loop
+// CollisionObject.cpp:67-105: objects are applied in order; a STICKY hit ends the loop; the normal of every
+// SLIP/SEPARATE hit is Gram-Schmidt orthogonalised against the earlier ones (:84-92) and, when it is not
+// zero, normalised into the basis; the dim-th basis vector ends the loop (:93-98)
 template <class T>
 inline void multi_object_collision(const std::vector<HalfSpace<T>>& objs, T time, const T x[3], T v[3])
 {
+    T basis[3][3];
+    int count = 0;
     for (auto& h : objs) {
         bool hit = resolve_halfspace(h, time, x, v);
-        if (hit && h.type == OBJ_STICKY) break;
+        if (!hit) continue;
+        if (h.type == OBJ_STICKY) break;
+        T n[3] = { h.n[0], h.n[1], h.n[2] };
+        for (int c = 0; c < count; c++) {
+            T dot = basis[c][0] * n[0] + basis[c][1] * n[1] + basis[c][2] * n[2];
+            for (int d = 0; d < 3; d++) n[d] -= dot * basis[c][d];
+        }
+        T length = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (length != 0) {
+            for (int d = 0; d < 3; d++) basis[count][d] = n[d] / length;
+            if (++count == 3) break;
+        }
     }
 }
 
@@ -1880,6 +1895,34 @@ int64_t orc_seeded_inputs(int kind, int ppc_side, uint64_t seed, double dx, cons
                     if (sigma_c) sigma_c[p] = sc;
                 }
     return count;
+}
+
+// One grid node through the collision objects (multiObjectCollision): objs holds per object origin[3],
+// normal[3] (normalised here, as HalfSpace does), velocity[3], friction and type (11 doubles).
+void orc_collide(int precision, int n_obj, const double* objs, double time, const double* x, double* v)
+{
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        std::vector<HalfSpace<T>> hs(n_obj);
+        for (int k = 0; k < n_obj; k++) {
+            const double* o = objs + 11 * k;
+            double nn = std::sqrt(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]);
+            for (int a = 0; a < 3; a++) {
+                hs[k].o[a] = (T)o[a];
+                hs[k].n[a] = (T)(o[3 + a] / nn);
+                hs[k].vel[a] = (T)o[6 + a];
+            }
+            hs[k].friction = (T)o[9];
+            hs[k].type = (int)o[10];
+        }
+        T xt[3] = { (T)x[0], (T)x[1], (T)x[2] }, vt[3] = { (T)v[0], (T)v[1], (T)v[2] };
+        multi_object_collision(hs, (T)time, xt, vt);
+        for (int a = 0; a < 3; a++) v[a] = (double)vt[a];
+    };
+    if (precision == 4)
+        run(0.0f);
+    else
+        run(0.0);
 }
 
 int orc_num_threads()

@@ -107,4 +107,33 @@ int shim_key(int prec, int i, int j, int k, unsigned id, unsigned long long* key
     *key = prec == 4 ? SpLayout<6>::key(i, j, k, id) : SpLayout<7>::key(i, j, k, id);
     return 0;
 }
+
+// one grid node through the scene's collision objects (collide): objs as in the oracle's orc_collide,
+// origin[3] normal[3] velocity[3] friction type per object (normal normalised as the engine does)
+void shim_collide(int prec, int n_obj, const double* objs, double time, const double* x, double* v)
+{
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        SceneParams<T> sp{};
+        sp.n_objects = n_obj;
+        for (int k = 0; k < n_obj; k++) {
+            const double* o = objs + 11 * k;
+            double nn = std::sqrt(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]);
+            for (int a = 0; a < 3; a++) {
+                sp.objects[k].origin[a] = (T)o[a];
+                sp.objects[k].normal[a] = (T)(o[3 + a] / nn);
+                sp.objects[k].vel[a] = (T)o[6 + a];
+            }
+            sp.objects[k].friction = (T)o[9];
+            sp.objects[k].type = (int)o[10];
+        }
+        T xt[3] = { (T)x[0], (T)x[1], (T)x[2] }, vt[3] = { (T)v[0], (T)v[1], (T)v[2] };
+        collide(sp, (T)time, xt, vt);
+        for (int a = 0; a < 3; a++) v[a] = (double)vt[a];
+    };
+    if (prec == 4)
+        run(0.0f);
+    else
+        run(0.0);
+}
 }

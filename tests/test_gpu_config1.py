@@ -6,10 +6,12 @@ l0 = 0.5 dx, sigma_c ~ N(400, 40) Pa, d = 0, the two x-ends pulled apart at +-0.
 substeps (Projects/anisofracture/AnisoFractureSimulation.h:129-283, Lib/MPM/MpmSimulationBase.cpp:262-357).
 
 Bounds: the FP64 GPU path differs from the oracle only in the order of the grid sums: positions within
-1e-11 m (domain-relative in the unit box), damage within 1e-8. The FP32 path: positions within 1e-4 of the
-domain (the path's stated bound); its damage against the FP64 oracle within the bounds measured on this
-scene with about 3x margin (the damage threshold phi > 1 turns FP32 rounding of the stress into damage
-differences at the particles that sit on it). Max and RMS errors are printed."""
+1e-12 m (domain-relative in the unit box; measured 3.3e-16), damage within 1e-10 (measured 3.9e-13 after 500
+substeps). The FP32 path: positions within 1e-4 of the domain (the path's stated bound; measured 5.2e-6 after
+200 and 1.3e-5 after 500 substeps); its damage against the FP64 oracle within about 3x of what this scene
+measured (max 5.5e-4 / RMS 1.6e-5 after 200 substeps, 1.8e-3 / 5.7e-5 after 500: the damage threshold
+phi > 1 turns FP32 rounding of the stress into damage differences at the particles that sit on it). Max and
+RMS errors are printed."""
 import numpy as np
 import pytest
 
@@ -46,15 +48,15 @@ def test_config1_fp64_matches_oracle(slab_and_oracle):
     for tag, g, r in (("200", g200, r200), ("500", g500, r500)):
         e = scenes.errors(g, r)
         print(f"FP64 GPU vs FP64 oracle after {tag} substeps: {e}")
-        assert e["x"][0] <= 1e-11, (tag, e)
-        assert e["d"][0] <= 1e-8, (tag, e)
+        assert e["x"][0] <= 1e-12, (tag, e)
+        assert e["d"][0] <= 1e-10, (tag, e)
     assert r500["d"].max() > 0.5  # the slab tore: the comparison covers grown damage
 
 
 def test_config1_fp32_within_bounds_of_fp64_oracle(slab_and_oracle):
     d, r200, r500 = slab_and_oracle
     g200, g500 = _run(d, zr.F32, (200, STEPS))
-    for tag, g, r, dmax, drms in (("200", g200, r200, 2e-2, 1e-3), ("500", g500, r500, 2e-2, 1e-3)):
+    for tag, g, r, dmax, drms in (("200", g200, r200, 2e-3, 5e-5), ("500", g500, r500, 6e-3, 2e-4)):
         e = scenes.errors(g, r)
         print(f"FP32 GPU vs FP64 oracle after {tag} substeps: {e}")
         assert e["x"][0] <= 1e-4, (tag, e)

@@ -32,6 +32,7 @@ def shim(tmp_path_factory):
     L.shim_qr.argtypes = [pd, pd, pd]
     L.shim_damage2.restype = C.c_double
     L.shim_damage2.argtypes = [C.c_int] + [C.c_double] * 7 + [pd] + [C.c_double] * 4
+    L.shim_collide.argtypes = [C.c_int, C.c_int, pd, C.c_double, pd, pd]
     return L
 
 
@@ -293,3 +294,74 @@ def test_damage_drive_zero_bound_changes_nothing(shim, alpha):
         else:
             computed += 1
     assert skipped > 50 and computed > 50
+
+
+def _objects(rows):
+    """collision objects as the 11-double rows of shim_collide / orc_collide"""
+    return np.ascontiguousarray([list(o) + list(n) + list(v) + [fr, ty] for o, n, v, fr, ty in rows], dtype=np.float64)
+
+
+def _collide(fn, prec, objs, t, x, v):
+    out = np.array(v, dtype=np.float64)
+    fn(prec, len(objs), p(objs), t, p(np.asarray(x, dtype=np.float64)), p(out))
+    return out
+
+
+def _oracle_collide(prec, n, objs, t, x, v):
+    lib = po.lib()
+    lib.orc_collide.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    out = np.array(v, dtype=np.float64)
+    lib.orc_collide(prec, n, p(objs), t, p(np.asarray(x, dtype=np.float64)), p(out))
+    return out
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_collide_matches_oracle_multi_object(shim, prec):
+    """collide (CollisionObject.cpp:67-105, :342-406) against the oracle on random nodes and velocities through
+    a corner of three SLIP/SEPARATE walls with friction, moving objects, and a STICKY plane listed last: where
+    a node lies inside the three walls the basis is complete after them and the STICKY plane is never applied
+    (the loop ends after dim slip normals); elsewhere it applies when the node is inside it."""
+    rng = np.random.default_rng(7)
+    rows = [((0.0, 0.2, 0.0), (0.1, 1.0, 0.05), (0.0, 0.0, 0.0), 0.4, 2),  # tilted floor, SLIP with friction
+            ((0.3, 0.0, 0.0), (1.0, 0.0, 0.2), (0.05, 0.0, 0.0), 0.0, 3),  # moving wall, SEPARATE
+            ((0.0, 0.0, 0.3), (0.0, 0.3, 1.0), (0.0, 0.0, 0.0), 0.2, 3),  # SEPARATE with friction
+            ((0.0, 0.25, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 0.0), 0.0, 1)]  # STICKY plane after the walls
+    objs = _objects(rows)
+    stopped = applied_sticky = 0
+    for _ in range(4000):
+        x = rng.uniform(0.1, 0.4, 3)
+        v = rng.normal(0, 1, 3)
+        t = float(rng.uniform(0, 0.5))
+        g = _collide(shim.shim_collide, prec, objs, t, x, v)
+        o = _oracle_collide(prec, len(rows), objs, t, x, v)
+        tol = 1e-5 if prec == 4 else 1e-12
+        assert np.abs(g - o).max() <= tol * max(1.0, np.abs(o).max()), (x, v, g, o)
+        inside = [np.dot(np.array(n) / np.linalg.norm(n), x - np.array(vel) * t - np.array(org)) <= 0 for org, n, vel, _, _ in rows]
+        if all(inside[:3]) and inside[3]:
+            stopped += 1
+            assert not np.allclose(g, 0.0)  # the STICKY plane did not apply
+        elif inside[3] and not any(inside[:3]):
+            applied_sticky += 1
+            assert np.allclose(g, 0.0)
+    assert stopped > 20 and applied_sticky > 20  # both cases were exercised
+
+
+def test_collide_parallel_normals_add_nothing_to_the_basis(shim):
+    """Two SLIP planes with the same normal count once: after them two more SLIP planes with independent
+    normals still apply, and a STICKY plane after those does not (three basis vectors)."""
+    rows = [((0.0, 0.5, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 0.0), 0.0, 2),
+            ((0.0, 0.6, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 0.0), 0.0, 2),
+            ((0.5, 0.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.0, 2),
+            ((0.0, 0.0, 0.5), (0.0, 0.0, 1.0), (0.0, 0.0, 0.0), 0.0, 2),
+            ((1.0, 1.0, 1.0), (1.0, 1.0, 1.0), (0.3, 0.0, 0.0), 0.0, 1)]
+    objs = _objects(rows)
+    x, v = (0.2, 0.2, 0.2), (-1.0, -2.0, -3.0)
+    for prec in (4, 8):
+        g = _collide(shim.shim_collide, prec, objs, 0.0, x, v)
+        o = _oracle_collide(prec, len(rows), objs, 0.0, x, v)
+        assert np.array_equal(g, o)
+        assert np.array_equal(g, np.zeros(3))  # three orthogonal SLIP walls remove every component; STICKY skipped
+    rows[3] = ((0.0, 0.0, -5.0), (0.0, 0.0, 1.0), (0.0, 0.0, 0.0), 0.0, 2)  # the z wall no longer contains x
+    objs = _objects(rows)
+    g = _collide(shim.shim_collide, 8, objs, 0.0, x, v)
+    assert np.allclose(g, (0.3, 0.0, 0.0))  # two basis vectors only: the moving STICKY plane applies

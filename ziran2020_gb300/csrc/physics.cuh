@@ -632,11 +632,17 @@ ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, 
     return nd < (T)1 ? nd : (T)1;
 }
 
-// Analytic translating half-spaces at a grid node (CollisionObject.cpp:67-105, :342-406,
-// AnalyticLevelSet.cpp:318-334). Objects apply in order; a STICKY hit ends the loop.
+// Analytic translating half-spaces at a grid node (AnalyticCollisionObject::multiObjectCollision and
+// detectAndResolveCollision, CollisionObject.cpp:67-105, :342-406; HalfSpace, AnalyticLevelSet.cpp:318-334).
+// Objects apply in order: a STICKY hit sets the object's velocity and ends the loop; a SLIP hit removes the
+// normal part of the relative velocity, a SEPARATE hit only an approaching one, both with kinetic friction.
+// Every SLIP or SEPARATE hit adds its normal to a basis, orthogonalised against the earlier ones (Gram-Schmidt,
+// a parallel normal adds nothing); once the basis holds three normals the loop ends.
 template <class T>
 ZR_HD void collide(const SceneParams<T>& sp, T time, const T* x, T* v)
 {
+    T basis[3][3];
+    int nslip = 0;
     for (int k = 0; k < sp.n_objects; k++) {
         const HalfSpaceObj<T>& h = sp.objects[k];
         T phi = h.normal[0] * (x[0] - h.vel[0] * time - h.origin[0]) + h.normal[1] * (x[1] - h.vel[1] * time - h.origin[1])
@@ -663,6 +669,16 @@ ZR_HD void collide(const SceneParams<T>& sp, T time, const T* x, T* v)
             }
         }
         for (int a = 0; a < 3; a++) v[a] = r[a] + h.vel[a];
+        T nv[3] = { h.normal[0], h.normal[1], h.normal[2] };
+        for (int c = 0; c < nslip; c++) {
+            const T d = basis[c][0] * nv[0] + basis[c][1] * nv[1] + basis[c][2] * nv[2];
+            for (int a = 0; a < 3; a++) nv[a] -= d * basis[c][a];
+        }
+        const T len = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        if (len != (T)0) {
+            for (int a = 0; a < 3; a++) basis[nslip][a] = nv[a] / len;
+            if (++nslip == 3) break;
+        }
     }
 }
 
