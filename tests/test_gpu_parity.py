@@ -85,6 +85,7 @@ def test_qr_stable_slab_matches_oracle(fiber):
         s = scenes.gpu_scene(d, prec)
         s.step(30)
         e = scenes.errors(scenes.gpu_state(s), r)
+        print(f"QR-stable slab, fibre {fiber}, precision {prec}: {e}")
         assert e["x"][0] < xtol, (prec, e)
         assert e["d"][0] < (1e-9 if prec == zr.F64 else 2e-2), (prec, e)
 
@@ -93,6 +94,7 @@ def test_aniso_slab_fp32_close_to_fp64_oracle():
     d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0)
     s, o, g, r = run_pair(d, zr.F32, 60)
     e = scenes.errors(g, r)
+    print(f"slab FP32 after 60 substeps: {e}")
     assert e["x"][0] < 1e-5, e
     assert e["d"][0] < 2e-2, e
     assert e["d"][1] < 1e-3, e

@@ -647,13 +647,13 @@ public:
     Schedule schedule() const override { return sched_; }
     int set_schedule(const Schedule& sc) override
     {
-        if (sc.fused < 0 || sc.fused > 2 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
+        if (sc.fused < 0 || sc.fused > 3 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
             || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8 || sc.g2p_tight < 0 || sc.g2p_tight > 1)
             return arg("schedule: unknown P2G form, (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
         sched_ = sc;
         if (sc.fused) {
-            sched_.chunk = FusedShape<T>::CHUNK;
-            sched_.buffers = 0;
+            sched_.chunk = sc.fused == 3 ? WsShape<T>::CHUNK : FusedShape<T>::CHUNK;
+            sched_.buffers = sc.fused == 3 ? WsShape<T>::NSTAGE : 0;
         }
         sched_.tuned = 0;
         fixed_schedule_ = true; // explicit schedules are not overridden by the autotuner
@@ -690,6 +690,7 @@ private:
     size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
     int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
     int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [register budget variant][model set]
+    int occ_ws_[4] = { 1, 1, 1, 1 }; // warp-specialised P2G, per model set
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
     bool implicit_ = false; // some scene solves its damage implicitly
@@ -911,6 +912,10 @@ private:
         fused_setup<2, FUSED_MINB[1]>(1, 1);
         fused_setup<4, FUSED_MINB[1]>(1, 2);
         fused_setup<7, FUSED_MINB[1]>(1, 3);
+        ws_setup<1>(0);
+        ws_setup<2>(1);
+        ws_setup<4>(2);
+        ws_setup<7>(3);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[0], k_stress<T, 1>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 4>, 256, 0);
@@ -1070,7 +1075,9 @@ private:
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
-        if (sched_.fused) {
+        if (sched_.fused == 3)
+            launch_ws(a, nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_ws_[models_slot()]));
+        else if (sched_.fused) {
             const int fv = sched_.fused == 2 ? 1 : 0;
             const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[fv][models_slot()]);
             if (fv == 0)
@@ -1323,6 +1330,27 @@ private:
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[var][slot], k, FusedShape<T>::NT, FusedShape<T>::dyn_bytes);
         occ_fused_[var][slot] = std::max(1, occ_fused_[var][slot]);
     }
+    template <int M>
+    void ws_setup(int slot)
+    {
+        auto k = k_p2g_ws<T, M>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WsShape<T>::dyn_bytes);
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ws_[slot], k, WsShape<T>::NT, WsShape<T>::dyn_bytes);
+        occ_ws_[slot] = std::max(1, occ_ws_[slot]);
+    }
+    void launch_ws(const StepArgs<T>& a, int ctas)
+    {
+        const int ms = models_slot();
+        if (ms == 0)
+            k_p2g_ws<T, 1><<<ctas, WsShape<T>::NT, WsShape<T>::dyn_bytes, stream_>>>(a);
+        else if (ms == 1)
+            k_p2g_ws<T, 2><<<ctas, WsShape<T>::NT, WsShape<T>::dyn_bytes, stream_>>>(a);
+        else if (ms == 2)
+            k_p2g_ws<T, 4><<<ctas, WsShape<T>::NT, WsShape<T>::dyn_bytes, stream_>>>(a);
+        else
+            k_p2g_ws<T, 7><<<ctas, WsShape<T>::NT, WsShape<T>::dyn_bytes, stream_>>>(a);
+    }
     template <int MINB>
     void launch_fused(const StepArgs<T>& a, int ctas)
     {
@@ -1437,6 +1465,10 @@ private:
         for (int fv = 0; fv < 2; fv++) {
             const int of = occ_fused_[fv][models_slot()];
             for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1 + fv, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 0, 1 });
+        }
+        {
+            const int ow = occ_ws_[models_slot()];
+            for (int c = ow; c >= std::max(1, ow - 1); c--) p2g_c.push_back(Schedule{ 3, WsShape<T>::CHUNK, WsShape<T>::NSTAGE, c, G2P_NT[1], 0, 1 });
         }
         constexpr int REPS = 2; // the first run of a candidate warms caches and instruction memory
         Schedule best = p2g_c[0];

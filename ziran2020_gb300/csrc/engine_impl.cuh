@@ -1127,6 +1127,196 @@ __global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Warp-specialised fused P2G (the same arithmetic as k_p2g_fused). Producer warps load each chunk's particle
+// state, evaluate V0 tau and stage the payload in one of NSTAGE shared-memory buffers; consumer warps (thread per
+// (cell, stencil x-offset)) accumulate the previous buffer meanwhile, so the state loads' latency and the
+// accumulation overlap inside the CTA instead of alternating behind CTA-wide barriers. Hand-offs are mbarriers:
+// full[s] completes when every producer thread has written buffer s, empty[s] when every consumer warp has read
+// it. A group's node tiles are double-buffered: the consumer warps meet on one mbarrier before the flush of a
+// group, while the next group's additions go to the other tile buffer. Every wait is bounded (2 s) and raises
+// FLAG_TIMEOUT. Groups are dealt to CTAs round-robin (blockIdx, + gridDim, ...), so every producer thread knows
+// the sequence of chunks without exchanging it.
+// ---------------------------------------------------------------------------------------------------
+template <class T>
+struct WsShape {
+    using L = typename LayoutOf<T>::type;
+    static constexpr int NCONS = 3 * L::nodes; // consumers: cells x stencil x-offsets
+    static constexpr int NPROD = sizeof(T) == 4 ? 128 : 64;
+    static constexpr int NT = NCONS + NPROD;
+    static constexpr int CHUNK = sizeof(T) == 4 ? 256 : 128;
+    static constexpr int CPAD = CHUNK + CHUNK / 8;
+    static constexpr int NSTAGE = 2;
+    static constexpr size_t pay_bytes = sizeof(T) * Y_CELL * CPAD;
+    static constexpr size_t stage_bytes = pay_bytes + CHUNK; // payload fields Y_F..Y_D, then the cells
+    static constexpr size_t dyn_bytes = NSTAGE * stage_bytes;
+    static_assert(pay_bytes % 16 == 0 && NCONS % 32 == 0 && NPROD % 32 == 0, "whole warps, aligned buffers");
+};
+
+struct WsItem {
+    uint32_t c0; // first sorted particle of the chunk
+    int32_t cnt, flags, scene, nf;
+    int32_t nbr[8];
+};
+
+template <class T, int MODELS>
+__global__ void __launch_bounds__(WsShape<T>::NT, 2) k_p2g_ws(StepArgs<T> a)
+{
+    using L = typename LayoutOf<T>::type;
+    using S = WsShape<T>;
+    using OT = OffsetTiles<L>;
+    constexpr int NCONS = S::NCONS, NPROD = S::NPROD, CHUNK = S::CHUNK, CPAD = S::CPAD, NST = S::NSTAGE, NC = L::nodes;
+    extern __shared__ __align__(16) unsigned char ws_dyn[];
+    __shared__ T tiles[2][OT::ELEMS]; // one set of per-offset node tiles per group parity
+    __shared__ __align__(8) uint64_t full[NST], empty[NST], flushed;
+    __shared__ WsItem item[NST];
+    __shared__ int32_t s_nbr[2][8];
+    if (aborted_cta(a.st)) return;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < NST; s++) {
+            mbar_init(&full[s], NPROD);
+            mbar_init(&empty[s], NCONS / 32);
+        }
+        mbar_init(&flushed, NCONS / 32);
+        mbar_init_fence();
+    }
+    for (int q = tid; q < 2 * OT::ELEMS; q += S::NT) (&tiles[0][0])[q] = (T)0;
+    __syncthreads(); // the last CTA-wide barrier: the roles never meet again
+    const uint32_t G = a.st->n_groups;
+    if (tid >= NCONS) {
+        // ---------------- producers
+        const int pt = tid - NCONS;
+        uint32_t fallbacks = 0, k = 0;
+        bool stop = false;
+        for (uint32_t g = blockIdx.x; g < G && !stop; g += gridDim.x) {
+            const uint32_t start = a.g_start[g], end = (g + 1 < G) ? a.g_start[g + 1] : a.n_total;
+            const uint64_t key0 = a.kl.at(a.keys_sorted, start);
+            uint32_t bi, bj, bk;
+            L::block_of_page(a.kl.page(key0), bi, bj, bk);
+            const int scene = (int)a.kl.scene(key0);
+            const int org0 = (int)(bi * L::sx), org1 = (int)(bj * L::sy), org2 = (int)(bk * L::sz);
+            const SceneParams<T>& sp = a.scenes[scene];
+            int bad = (end <= start || end > a.n_total) ? 1 : 0;
+            if (bad) check_failed(a.st, 1);
+            for (uint32_t c0 = start; c0 < end || (bad && c0 == start); c0 += CHUNK) {
+                const int s = k % NST;
+                if (!mbar_wait(&empty[s], ((k / NST) & 1u) ^ 1u, WAIT_LIMIT_NS)) {
+                    raise_flag(a.st, FLAG_TIMEOUT);
+                    stop = true;
+                    break;
+                }
+                const int cnt = bad ? 0 : (int)min((uint32_t)CHUNK, end - c0);
+                const bool last = bad || c0 + CHUNK >= end;
+                WsItem& it = item[s];
+                if (pt < 32) { // the first producer warp fills the item; a failed slot lookup raised FLAG_CAPACITY
+                    int slot = 0;
+                    if (pt < 8) {
+                        slot = a.g_nbr[g * 8 + pt];
+                        it.nbr[pt] = slot;
+                    }
+                    const bool nbad = __ballot_sync(0xffffffffu, pt < 8 && (slot < 0 || (uint32_t)slot >= a.b_cap)) != 0;
+                    if (pt == 0) {
+                        it.c0 = c0;
+                        it.cnt = cnt;
+                        it.scene = scene;
+                        it.nf = sp.damage ? NACC : 4;
+                        it.flags = (last ? ITEM_LAST : 0) | ((bad || nbad) ? ITEM_BAD : 0);
+                    }
+                }
+                T* pay = reinterpret_cast<T*>(ws_dyn + s * S::stage_bytes);
+                uint8_t* cellof = ws_dyn + s * S::stage_bytes + S::pay_bytes;
+                constexpr int PER = (CHUNK + NPROD - 1) / NPROD;
+                uint32_t js[PER];
+#pragma unroll
+                for (int r = 0; r < PER; r++) js[r] = pt + r * NPROD < cnt ? a.vals_sorted[c0 + pt + r * NPROD] : 0u;
+#pragma unroll
+                for (int r = 0; r < PER; r++) {
+                    const int q = pt + r * NPROD;
+                    if (q >= cnt) break;
+                    int b[3];
+                    particle_payload<T, MODELS>(a.pin, js[r], sp, pay + (q + (q >> 3)), CPAD, b, fallbacks);
+                    const int l0 = b[0] - org0, l1 = b[1] - org1, l2 = b[2] - org2;
+                    const bool inside = l0 >= 0 && l0 < L::sx && l1 >= 0 && l1 < L::sy && l2 >= 0 && l2 < L::sz;
+                    if (!inside) raise_flag(a.st, FLAG_CAPACITY); // keys and positions disagree: abort the substep
+                    cellof[q] = inside ? (uint8_t)L::element(l0, l1, l2) : (uint8_t)0xff;
+                }
+                mbar_arrive(&full[s]);
+                k++;
+                if (bad) break;
+            }
+        }
+        if (!stop) { // the end marker
+            const int s = k % NST;
+            if (mbar_wait(&empty[s], ((k / NST) & 1u) ^ 1u, WAIT_LIMIT_NS)) {
+                if (pt == 0) item[s].flags = ITEM_DONE;
+                mbar_arrive(&full[s]);
+            }
+            else
+                raise_flag(a.st, FLAG_TIMEOUT);
+        }
+        if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
+        return;
+    }
+    // ---------------- consumers: cell c, stencil x-offset ii
+    const int ii = tid / NC, c = tid % NC, lane = tid & 31;
+    const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
+    int tb = 0; // tile buffer of the current group
+    uint32_t gseq = 0; // groups flushed (parity of the flush barrier)
+    for (uint32_t k = 0;; k++) {
+        const int s = k % NST;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[s], (k / NST) & 1u, WAIT_LIMIT_NS));
+        if (!ok) {
+            if (lane == 0) raise_flag(a.st, FLAG_TIMEOUT);
+            break;
+        }
+        const WsItem& it = item[s];
+        const int fl = it.flags;
+        if (fl & ITEM_DONE) break;
+        const int cnt = it.cnt, nf = it.nf;
+        const T* pay = reinterpret_cast<const T*>(ws_dyn + s * S::stage_bytes);
+        const uint8_t* cellof = ws_dyn + s * S::stage_bytes + S::pay_bytes;
+        if ((fl & ITEM_LAST) && tid < 8) s_nbr[tb][tid] = it.nbr[tid]; // read before this warp releases the buffer
+        NodeAcc<T> acc;
+        acc.zero();
+        const bool use = !(fl & ITEM_BAD);
+        if (use) {
+            auto cell_lower = [&](int v) {
+                int lo = 0, hi = cnt;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (cellof[mid] < v) lo = mid + 1;
+                    else hi = mid;
+                }
+                return lo;
+            };
+            const int qa = cell_lower(c), qb = cell_lower(c + 1);
+            if (nf == NACC)
+                for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, true>(acc, pay + (q + (q >> 3)), ii);
+            else
+                for (int q = qa; q < qb; q++) accumulate_particle<T, CPAD, false>(acc, pay + (q + (q >> 3)), ii);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]); // the buffer is free for the producers
+        if (use) add_to_offset_tile<T, L>(acc, tiles[tb], cx, cy, cz, ii, nf); // all lanes (an empty cell adds zeros)
+        if (fl & ITEM_LAST) {
+            // every consumer warp has added the group: flush its tiles (the next group fills the other tile buffer)
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&flushed);
+            const bool fok = __all_sync(0xffffffffu, mbar_wait(&flushed, gseq & 1u, WAIT_LIMIT_NS));
+            gseq++;
+            if (!fok) {
+                if (lane == 0) raise_flag(a.st, FLAG_TIMEOUT);
+                break;
+            }
+            if (use) flush_offset_tiles<T, L>(a, tiles[tb], s_nbr[tb], nf, tid, NCONS);
+            else
+                for (int q = tid; q < OT::ELEMS; q += NCONS) tiles[tb][q] = (T)0; // a bad group's partial sums are dropped
+            tb ^= 1;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
 // grid update
 // ---------------------------------------------------------------------------------------------------
 constexpr int GRID_NT = 256; // threads per CTA of the grid update
