@@ -66,7 +66,8 @@ struct StepReport {
 struct Schedule {
     int fused = 0; // P2G: 1 = one kernel evaluating the stress itself, 2 = the same with registers cut for one more
                    // CTA per SM, 3 = the same split into producer warps (state loads, stress, payload) and consumer
-                   // warps (accumulation) working on alternating shared-memory buffers; 0 = a stress kernel writing a
+                   // warps (accumulation) working on alternating shared-memory buffers, 4 = form 1 cut for two more
+                   // CTAs per SM with half-block chunks; 0 = a stress kernel writing a
                    // payload that a scatter kernel streams into shared memory with bulk asynchronous copies
     int chunk = 0; // P2G: particles per chunk staged in shared memory by one bulk copy per payload field
     int buffers = 1; // P2G: staging buffers (2: the next chunk's copy overlaps the whole current chunk)

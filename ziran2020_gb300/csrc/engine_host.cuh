@@ -44,8 +44,12 @@ class Engine final : public EngineBase {
     // G2P register budgets: threads per SM (FP32 448: a ~146-register cap, under which ptxas settles at 128 with
     // little spilling; 512: a 128 cap, more spills; FP64: ~255 or ~200)
     static constexpr int G2P_RES[2] = { sizeof(T) == 4 ? 448 : 256, sizeof(T) == 4 ? 512 : 320 };
-    // fused P2G register budgets: cut for 2 or 3 CTAs per SM (FP32), 1 or 2 (FP64)
-    static constexpr int FUSED_MINB[2] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2 };
+    // fused P2G variants (schedule fused = 1, 2, 4): register budgets cut for 2, 3 or 4 CTAs per SM (FP32; 1, 2 or 3
+    // for FP64), the last with half-block chunks so that four CTAs' staging buffers fit in shared memory
+    static constexpr int FUSED_MINB[3] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2, sizeof(T) == 4 ? 4 : 3 };
+    static constexpr int FUSED_CH[3] = { FusedShape<T>::CHUNK, FusedShape<T>::CHUNK, FusedShape<T>::CHUNK / 2 };
+    static int fused_variant(int fused) { return fused == 4 ? 2 : fused - 1; }
+    static int fused_code(int fv) { return fv == 2 ? 4 : fv + 1; }
 
 public:
     Engine() { init_device(); }
@@ -134,8 +138,8 @@ public:
                 ZR_CUDA(cudaMemcpyAsync(grown_pid[0] + np[q].first, old_pid + src_first[q], 4 * np[q].count, cudaMemcpyDeviceToDevice, stream_));
             }
             ZR_CUDA(cudaStreamSynchronize(stream_));
-            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, sel_tmp_, pay_,
-                inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
+            void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, pay_,
+                sort_aux_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
             for (void* p : olds)
                 if (p) cudaFree(p);
             pool_[0] = grown_pool[0];
@@ -144,30 +148,26 @@ public:
             pid_[1] = grown_pid[1];
             cap_ = (uint64_t)cap;
             pay_ = nullptr;
-            inc_stay_ = inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
+            sort_aux_ = nullptr;
+            inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
             inc_cnt_ = nullptr;
             // P2G payload: NPAY fields of sorted particles at q + q/8, plus the copy granularity at the end
             pstride_ = (int64_t)((pay_pos((uint64_t)cap) + 64 + 63) & ~(uint64_t)63);
             if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
                 || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_)
-                || alloc((void**)&inc_stay_, 4 * cap) || alloc((void**)&inc_move_, 4 * cap) || alloc((void**)&inc_mkeys_, 4 * cap)
+                || alloc((void**)&sort_aux_, sort_aux_bytes(cap)) || alloc((void**)&inc_move_, 4 * cap) || alloc((void**)&inc_mkeys_, 4 * cap)
                 || alloc((void**)&inc_mvals_, 4 * cap) || alloc((void**)&inc_mkeys2_, 4 * cap) || alloc((void**)&inc_mvals2_, 4 * cap)
                 || alloc((void**)&inc_cnt_, 16))
                 return ZR_ERR_CUDA_;
             mcap_ = std::min<int64_t>(cap, std::max<int64_t>(MCAP_MIN, cap / 32));
             ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
             k_iota<T><<<nsm_ * 4, 256, 0, stream_>>>(iota_, (uint32_t)cap);
-            size_t sb = 0, sb32 = 0, se = 0;
+            size_t sb = 0, sb32 = 0;
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, keys_in_, keys_sorted_, iota_, vals_sorted_, cap, 0, 64, stream_));
             ZR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb32, (uint32_t*)keys_in_, (uint32_t*)keys_sorted_, iota_, vals_sorted_, cap, 0, 32,
                 stream_));
-            sb = std::max(sb, sb32); // the key width follows the batch: room for either
-            sb = std::max(sb, inc_sort_bytes(cap)); // and for the incremental sort's passes
-            ZR_CUDA(cub::DeviceSelect::If(nullptr, se, thrust::counting_iterator<uint32_t>(0), g_start_, (uint32_t*)nullptr, cap,
-                GroupHead{ keys_sorted_, kl }, stream_));
-            sort_bytes_ = sb;
-            sel_bytes_ = se;
-            if (alloc(&sort_tmp_, sort_bytes_) || alloc(&sel_tmp_, sel_bytes_)) return ZR_ERR_CUDA_;
+            sort_bytes_ = std::max(sb, sb32); // the key width follows the batch: room for either
+            if (alloc(&sort_tmp_, sort_bytes_)) return ZR_ERR_CUDA_;
             dst = 0;
         }
         else {
@@ -235,8 +235,7 @@ public:
         // keys, and a first binning pass that sizes the grid (every group activates at most 8 blocks)
         k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
         ZR_CUDA(sort_keys((int64_t)N_));
-        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, (int64_t)N_,
-            GroupHead{ keys_sorted_, kl_ }, stream_));
+        ZR_CUDA(group_heads((int64_t)N_));
         DevStatus hs;
         ZR_CUDA(cudaMemcpyAsync(&hs, st_, sizeof hs, cudaMemcpyDeviceToHost, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
@@ -332,11 +331,15 @@ public:
             k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_);
             ZR_CUDA(cudaStreamSynchronize(stream_));
             const uint32_t f = hst_->flags;
-            if ((f & FLAG_SORT) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK | FLAG_CAPACITY)) && mcap_ < (int64_t)cap_) {
+            if ((f & FLAG_SORT) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK | FLAG_CAPACITY))) {
+                // more movers than the list holds (grow it), or a bucket beyond the merge's shared memory: the
+                // substep is repeated with a full sort (it cannot raise FLAG_SORT, so every retry makes progress)
                 const int64_t mm = (int64_t)hst_->max_movers;
-                mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(2 * mcap_, mm + mm / 2));
-                drop_graphs();
-                continue; // repeat the substep (a full sort) with room for more movers next time
+                if (mm > mcap_ && mcap_ < (int64_t)cap_) {
+                    mcap_ = std::min<int64_t>((int64_t)cap_, std::max<int64_t>(2 * mcap_, mm + mm / 2));
+                    drop_graphs();
+                }
+                continue;
             }
             if ((f & FLAG_CAPACITY) && !(f & (FLAG_CFL | FLAG_NONFINITE | FLAG_OUT_OF_DOMAIN | FLAG_TIMEOUT | FLAG_CHECK)) && grow_rounds < 6) {
                 grow_rounds++;
@@ -567,7 +570,7 @@ public:
             StepArgs<T> a = args(cur_);
             ZR_CUDA(sort_keys(n));
             k_cellfix<T><<<nsm_ * 8, 256, 0, stream_>>>(keys_sorted_, vals_sorted_, pid_[cur_], N_, kl_);
-            ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
+            ZR_CUDA(group_heads(n));
             k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
             ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
             ZR_CUDA(cudaStreamSynchronize(stream_));
@@ -647,12 +650,12 @@ public:
     Schedule schedule() const override { return sched_; }
     int set_schedule(const Schedule& sc) override
     {
-        if (sc.fused < 0 || sc.fused > 3 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
+        if (sc.fused < 0 || sc.fused > 4 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
             || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8 || sc.g2p_tight < 0 || sc.g2p_tight > 1)
             return arg("schedule: unknown P2G form, (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
         sched_ = sc;
         if (sc.fused) {
-            sched_.chunk = sc.fused == 3 ? WsShape<T>::CHUNK : FusedShape<T>::CHUNK;
+            sched_.chunk = sc.fused == 3 ? WsShape<T>::CHUNK : FUSED_CH[fused_variant(sc.fused)];
             sched_.buffers = sc.fused == 3 ? WsShape<T>::NSTAGE : 0;
         }
         sched_.tuned = 0;
@@ -686,10 +689,10 @@ private:
     double* grid_mass_ = nullptr;
     DevStatus* st_ = nullptr;
     DevStatus* hst_ = nullptr;
-    void *sort_tmp_ = nullptr, *sel_tmp_ = nullptr, *stage_ = nullptr;
-    size_t sort_bytes_ = 0, sel_bytes_ = 0, stage_bytes_ = 0;
+    void *sort_tmp_ = nullptr, *stage_ = nullptr;
+    size_t sort_bytes_ = 0, stage_bytes_ = 0;
     int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
-    int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [register budget variant][model set]
+    int occ_fused_[3][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [fused variant][model set]
     int occ_ws_[4] = { 1, 1, 1, 1 }; // warp-specialised P2G, per model set
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
@@ -714,9 +717,11 @@ private:
     bool sort_base_stale_ = true;
     bool inc_sort_on_ = true; // ZR_SORT=full turns the incremental sort off
     static constexpr int64_t MCAP_MIN = 4096;
-    // stayer indices; mover indices, keys and storage indices before and after their sort
-    uint32_t *inc_stay_ = nullptr, *inc_move_ = nullptr, *inc_mkeys_ = nullptr, *inc_mvals_ = nullptr, *inc_mkeys2_ = nullptr, *inc_mvals2_ = nullptr;
-    int64_t* inc_cnt_ = nullptr; // stayers, movers
+    // the sort's tile arrays (stayer bits, per-tile counts and keys, bucket counts, group-head look-back words);
+    // the movers' list, buckets and tickets, and their keys and storage indices grouped by bucket
+    unsigned char* sort_aux_ = nullptr;
+    uint32_t *inc_move_ = nullptr, *inc_mkeys_ = nullptr, *inc_mvals_ = nullptr, *inc_mkeys2_ = nullptr, *inc_mvals2_ = nullptr;
+    int64_t* inc_cnt_ = nullptr; // [0] movers found
     int64_t mcap_ = 0; // movers the incremental sort takes per substep
     void *ck_pool_ = nullptr, *ck_pid_ = nullptr, *ck_scenes_ = nullptr; // device checkpoint
     uint64_t ck_cap_ = 0;
@@ -745,34 +750,61 @@ private:
             kl_.total(), stream_);
     }
 
-    // temporary storage of the incremental sort's CUB passes for up to cap particles
-    size_t inc_sort_bytes(int64_t cap)
+    // tiles of the sort and of the group-head pass (SORT_TILE keys each) for up to cap particles
+    static int64_t sort_tiles(int64_t n) { return std::max<int64_t>(1, (n + SORT_TILE - 1) / SORT_TILE); }
+    // sort_aux_: [stay bits: ceil(cap/32) u32][t_stay, t_first, b_cnt: tiles u32 each][look-back: tiles + 1 u64]
+    static size_t sort_aux_words(int64_t cap) { return (size_t)((cap + 31) / 32) + 3 * (size_t)sort_tiles(cap) + 1; }
+    static size_t sort_aux_bytes(int64_t cap) { return 4 * sort_aux_words(cap) + 8 * ((size_t)sort_tiles(cap) + 2); }
+    uint64_t* lookback_words() const
     {
-        size_t a = 0, b = 0;
-        cub::DevicePartition::If(nullptr, a, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, cap,
-            KeptCell{ nullptr, nullptr }, AnyItem{}, stream_);
-        cub::DeviceRadixSort::SortPairs(nullptr, b, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, cap, 0, 32, stream_);
-        return std::max(a, b);
+        const size_t off = (4 * sort_aux_words((int64_t)cap_) + 7) & ~(size_t)7;
+        return reinterpret_cast<uint64_t*>(sort_aux_ + off);
     }
-    bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_stay_; }
+    bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_move_; }
 
-    // The sorted keys and storage indices of keys_in_ from the previous substep's sorted keys (keys_sorted_):
-    // split stayers / movers (one pass, both in storage order), gather the movers' keys (padded), sort the movers
-    // (stable), merge the two key-sorted sequences into keys_sorted_ / vals_sorted_ (k_inc_merge).
+    // The sorted keys and storage indices of keys_in_ from the previous substep's sorted keys (keys_sorted_), by
+    // the hand-written kernels of the incremental sort (stayers in place, movers bucketed by stayer tile and merged).
     cudaError_t sort_keys_incremental(int64_t n)
     {
         const uint32_t* nk = (const uint32_t*)keys_in_;
         const uint32_t* ok = (const uint32_t*)keys_sorted_;
-        size_t tb = sort_bytes_;
-        cudaError_t e = cub::DevicePartition::If(sort_tmp_, tb, thrust::counting_iterator<uint32_t>(0), inc_stay_, inc_move_, inc_mvals2_, inc_cnt_, n,
-            KeptCell{ nk, ok }, AnyItem{}, stream_);
+        SortBufs sb;
+        const int64_t tiles = sort_tiles(n);
+        uint32_t* w = reinterpret_cast<uint32_t*>(sort_aux_);
+        sb.stay_bits = w;
+        sb.t_stay = w + (cap_ + 31) / 32;
+        sb.t_first = sb.t_stay + sort_tiles((int64_t)cap_);
+        sb.b_cnt = sb.t_first + sort_tiles((int64_t)cap_);
+        sb.m_idx = inc_move_;
+        sb.m_bkt = inc_mkeys_;
+        sb.m_tkt = inc_mvals_;
+        sb.b_key = inc_mkeys2_;
+        sb.b_idx = inc_mvals2_;
+        sb.cnt = inc_cnt_;
+        sb.mcap = mcap_;
+        sb.n = n;
+        sb.tiles = (int)tiles;
+        cudaError_t e = cudaMemsetAsync(inc_cnt_, 0, 16, stream_);
         if (e != cudaSuccess) return e;
-        k_inc_prep<<<nsm_ * 4, 256, 0, stream_>>>(inc_move_, nk, inc_mkeys_, inc_mvals_, inc_cnt_, n, mcap_, st_);
-        tb = sort_bytes_;
-        e = cub::DeviceRadixSort::SortPairs(sort_tmp_, tb, inc_mkeys_, inc_mkeys2_, inc_mvals_, inc_mvals2_, mcap_, 0, 32, stream_);
+        const int mgrid = (int)std::min<int64_t>(nsm_ * 4, (mcap_ + 255) / 256);
+        k_sort_tiles<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, ok, sb, st_);
+        k_sort_scan1<<<1, 1024, 0, stream_>>>(sb, st_);
+        k_sort_bucket<<<mgrid, 256, 0, stream_>>>(nk, sb);
+        k_sort_scan2<<<1, 1024, 0, stream_>>>(sb);
+        k_sort_place<<<mgrid, 256, 0, stream_>>>(nk, sb, st_);
+        k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, st_);
+        return cudaGetLastError();
+    }
+
+    // first sorted index of every (scene, page) into g_start_, their number into st_->n_groups
+    cudaError_t group_heads(int64_t n)
+    {
+        const int64_t tiles = sort_tiles(n);
+        uint64_t* lb = lookback_words();
+        cudaError_t e = cudaMemsetAsync(lb, 0, 8 * ((size_t)tiles + 1), stream_);
         if (e != cudaSuccess) return e;
-        const int tiles = (int)std::max<int64_t>(1, (n + MERGE_TILE - 1) / MERGE_TILE);
-        k_inc_merge<<<tiles, MERGE_NT, 0, stream_>>>(inc_stay_, nk, inc_mkeys2_, inc_mvals2_, inc_cnt_, n, mcap_, (uint32_t*)keys_sorted_, vals_sorted_, st_);
+        k_group_heads<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(keys_sorted_, n, kl_, lb, reinterpret_cast<uint32_t*>(lb + tiles), g_start_,
+            (uint32_t)cap_, st_);
         return cudaGetLastError();
     }
 
@@ -904,14 +936,9 @@ private:
         scatter_setup<0>();
         scatter_setup<1>();
         scatter_setup<2>();
-        fused_setup<1, FUSED_MINB[0]>(0, 0);
-        fused_setup<2, FUSED_MINB[0]>(0, 1);
-        fused_setup<4, FUSED_MINB[0]>(0, 2);
-        fused_setup<7, FUSED_MINB[0]>(0, 3);
-        fused_setup<1, FUSED_MINB[1]>(1, 0);
-        fused_setup<2, FUSED_MINB[1]>(1, 1);
-        fused_setup<4, FUSED_MINB[1]>(1, 2);
-        fused_setup<7, FUSED_MINB[1]>(1, 3);
+        fused_setup_all<0>();
+        fused_setup_all<1>();
+        fused_setup_all<2>();
         ws_setup<1>(0);
         ws_setup<2>(1);
         ws_setup<4>(2);
@@ -1069,7 +1096,7 @@ private:
             ZR_CUDA(sort_keys(n));
         else
             ZR_CUDA(sort_keys_incremental(n));
-        ZR_CUDA(cub::DeviceSelect::If(sel_tmp_, sel_bytes_, thrust::counting_iterator<uint32_t>(0), g_start_, &st_->n_groups, n, GroupHead{ keys_sorted_, kl_ }, stream_));
+        ZR_CUDA(group_heads(n));
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
@@ -1078,12 +1105,14 @@ private:
         if (sched_.fused == 3)
             launch_ws(a, nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_ws_[models_slot()]));
         else if (sched_.fused) {
-            const int fv = sched_.fused == 2 ? 1 : 0;
+            const int fv = fused_variant(sched_.fused);
             const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[fv][models_slot()]);
             if (fv == 0)
-                launch_fused<FUSED_MINB[0]>(a, fctas);
+                launch_fused<0>(a, fctas);
+            else if (fv == 1)
+                launch_fused<1>(a, fctas);
             else
-                launch_fused<FUSED_MINB[1]>(a, fctas);
+                launch_fused<2>(a, fctas);
         }
         else {
             const int ms = models_slot();
@@ -1321,14 +1350,23 @@ private:
         else
             k_g2p<T, G2P_NT[2], G2P_RES[R]><<<nsm_ * occ_g2p_[R][2], G2P_NT[2], 0, stream_>>>(a);
     }
-    template <int M, int MINB>
-    void fused_setup(int var, int slot)
+    template <int M, int V>
+    void fused_setup(int slot)
     {
-        auto k = k_p2g_fused<T, M, MINB>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedShape<T>::dyn_bytes);
+        using FS = FusedShape<T, FUSED_CH[V]>;
+        auto k = k_p2g_fused<T, M, FUSED_MINB[V], FUSED_CH[V]>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FS::dyn_bytes);
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[var][slot], k, FusedShape<T>::NT, FusedShape<T>::dyn_bytes);
-        occ_fused_[var][slot] = std::max(1, occ_fused_[var][slot]);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_fused_[V][slot], k, FS::NT, FS::dyn_bytes);
+        occ_fused_[V][slot] = std::max(1, occ_fused_[V][slot]);
+    }
+    template <int V>
+    void fused_setup_all()
+    {
+        fused_setup<1, V>(0);
+        fused_setup<2, V>(1);
+        fused_setup<4, V>(2);
+        fused_setup<7, V>(3);
     }
     template <int M>
     void ws_setup(int slot)
@@ -1351,18 +1389,20 @@ private:
         else
             k_p2g_ws<T, 7><<<ctas, WsShape<T>::NT, WsShape<T>::dyn_bytes, stream_>>>(a);
     }
-    template <int MINB>
+    template <int V>
     void launch_fused(const StepArgs<T>& a, int ctas)
     {
+        using FS = FusedShape<T, FUSED_CH[V]>;
+        constexpr int MB = FUSED_MINB[V], CH = FUSED_CH[V];
         const int ms = models_slot();
         if (ms == 0)
-            k_p2g_fused<T, 1, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            k_p2g_fused<T, 1, MB, CH><<<ctas, FS::NT, FS::dyn_bytes, stream_>>>(a);
         else if (ms == 1)
-            k_p2g_fused<T, 2, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            k_p2g_fused<T, 2, MB, CH><<<ctas, FS::NT, FS::dyn_bytes, stream_>>>(a);
         else if (ms == 2)
-            k_p2g_fused<T, 4, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            k_p2g_fused<T, 4, MB, CH><<<ctas, FS::NT, FS::dyn_bytes, stream_>>>(a);
         else
-            k_p2g_fused<T, 7, MINB><<<ctas, FusedShape<T>::NT, FusedShape<T>::dyn_bytes, stream_>>>(a);
+            k_p2g_fused<T, 7, MB, CH><<<ctas, FS::NT, FS::dyn_bytes, stream_>>>(a);
     }
     int models_slot() const { return models_ == 1 ? 0 : (models_ == 2 ? 1 : (models_ == 4 ? 2 : 3)); }
     template <int V>
@@ -1462,9 +1502,9 @@ private:
         for (int vi = 0; vi < 3; vi++)
             for (int c = occ_scatter_[vi]; c >= std::max(1, occ_scatter_[vi] - 1); c--)
                 p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 0, 1 });
-        for (int fv = 0; fv < 2; fv++) {
+        for (int fv = 0; fv < 3; fv++) {
             const int of = occ_fused_[fv][models_slot()];
-            for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ 1 + fv, FusedShape<T>::CHUNK, 0, c, G2P_NT[1], 0, 1 });
+            for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ fused_code(fv), FUSED_CH[fv], 0, c, G2P_NT[1], 0, 1 });
         }
         {
             const int ow = occ_ws_[models_slot()];
@@ -1542,8 +1582,8 @@ private:
     {
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
-            d_scenes_, grid_mass_, st_, sort_tmp_, sel_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
-            inc_stay_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_, inv_ };
+            d_scenes_, grid_mass_, st_, sort_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
+            sort_aux_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_, inv_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1558,14 +1598,15 @@ private:
         d_scenes_ = nullptr;
         grid_mass_ = nullptr;
         st_ = nullptr;
-        sort_tmp_ = sel_tmp_ = stage_ = nullptr;
+        sort_tmp_ = stage_ = nullptr;
         stage_bytes_ = 0;
         pay_ = nullptr;
         pstride_ = 0;
         cg_ = nullptr;
         cgs_ = nullptr;
         implicit_ = false;
-        inc_stay_ = inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
+        sort_aux_ = nullptr;
+        inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
         inc_cnt_ = nullptr;
         mcap_ = 0;
         inv_ = nullptr;

@@ -231,129 +231,379 @@ struct GroupHead {
 };
 
 // ---------------------------------------------------------------------------------------------------
-// Incremental sort (32-bit keys). The storage order is the previous substep's sorted order, so the particles
-// whose cell did not change ("stayers") are already sorted; only the particles that changed cell ("movers",
-// ~2% per substep at the slab's speeds) need sorting: partition the storage indices (both parts keep storage
-// order), sort the movers by key (stable), merge the two key-sorted sequences straight into the sorted keys and
-// indices. Particles of one cell may come out in another order than a full stable sort gives (a mover after the
-// cell's stayers); any order of a cell's particles is a valid binning.
+// Incremental sort (32-bit keys), hand-written. The storage order is the previous substep's sorted order, so the
+// particles whose cell did not change ("stayers") are already sorted; only the particles that changed cell
+// ("movers", ~2% per substep at the slab's speeds) need placing.
+//
+// Storage is cut into tiles of SORT_TILE indices. B[j] = the smallest stayer key in tiles >= j (non-decreasing;
+// "no key" past the last stayer). Mover key k belongs to bucket b(k) = the largest j with B[j] <= k (0 when there is
+// none): every element of bucket j (its movers) and tile j (its stayers) lies in [B[j], B[j+1]] and comes after
+// every element of lower tiles and buckets, so tile j's merged output starts at
+// (stayers in tiles < j) + (movers in buckets < j). Inside it, in the order (key, stayers first, storage index), a
+// stayer goes to its rank among the tile's stayers plus the bucket's movers with a smaller key, a mover to its rank
+// in the bucket plus the tile's stayers with a key not above its own. The order is fully determined by the keys
+// and storage indices (no dependence on the order in which movers were found).
+//
+//   k_sort_tiles    per tile: stayer count and first stayer key; movers appended to a list (overflow: FLAG_SORT)
+//   k_sort_scan1    one CTA: stayer offsets per tile, B, bucket counters cleared
+//   k_sort_bucket   per mover: bucket (binary search over B) and a ticket within it
+//   k_sort_scan2    one CTA: mover offsets per bucket
+//   k_sort_place    per mover: (key, storage index) into its bucket
+//   k_sort_merge    per tile: the tile's stayers and its bucket's movers (sorted in shared memory) to their places
+//
+// More movers than the list holds, or a bucket larger than SORT_MAXM, raises FLAG_SORT: the host repeats the
+// substep with a full radix sort (and grows the list).
 // ---------------------------------------------------------------------------------------------------
-struct KeptCell { // the new key equals the one the particle was sorted by in the previous substep
-    const uint32_t* knew;
-    const uint32_t* kold;
-    __host__ __device__ bool operator()(uint32_t i) const { return knew[i] == kold[i]; }
+constexpr int SORT_NT = 256, SORT_PER = 8, SORT_TILE = SORT_NT * SORT_PER, SORT_MAXM = 1024;
+constexpr uint32_t SORT_NOKEY = 0xffffffffu; // keys of the incremental sort hold at most 31 bits
+
+struct SortBufs {
+    uint32_t* t_stay; // [tiles] stayers per tile, then (scan1) their exclusive offsets
+    uint32_t* t_first; // [tiles] first stayer key per tile, then (scan1) B (non-decreasing)
+    uint32_t* b_cnt; // [tiles] movers per bucket, then (scan2) their exclusive offsets
+    uint32_t* m_idx; // [mcap] movers' storage indices (list order)
+    uint32_t* m_bkt; // [mcap] bucket of each listed mover
+    uint32_t* m_tkt; // [mcap] ticket of each listed mover inside its bucket
+    uint32_t* b_key; // [mcap] movers' keys grouped by bucket
+    uint32_t* b_idx; // [mcap] movers' storage indices grouped by bucket
+    uint32_t* stay_bits; // [ceil(n / 32)] bit i % 32 of word i / 32: storage index i keeps its key
+    int64_t* cnt; // [0] movers found, [1] unused
+    int64_t mcap;
+    int64_t n;
+    int tiles;
 };
-struct AnyItem {
-    __host__ __device__ bool operator()(uint32_t) const { return true; }
-};
-// Gather the movers' keys, padded to mcap items with the largest key (padding sorts last; real keys have at most
-// 31 bits). More than mcap movers abort the substep with FLAG_SORT (the host grows the buffer and repeats it with
-// a full sort); the movers' list is then padding only, so the sort that still runs reads no index.
-static __global__ void k_inc_prep(const uint32_t* move_idx, const uint32_t* keys, uint32_t* move_keys, uint32_t* move_vals, const int64_t* cnt,
-    int64_t n, int64_t mcap, DevStatus* st)
-{
-    const int64_t S = cnt[0];
-    int64_t M = cnt[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&st->max_movers, (uint32_t)(M >= 0 && M < 0xffffffffLL ? M : 0xffffffffLL));
-    if (S < 0 || M < 0 || S + M != n || M > mcap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) raise_flag(st, FLAG_SORT);
-        M = 0;
-    }
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < mcap; t += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t i = t < M ? move_idx[t] : ~0u;
-        move_keys[t] = i < (uint64_t)n ? keys[i] : ~0u;
-        move_vals[t] = i;
-    }
-}
 
-// Merge of the stayers (storage order, key-sorted) with the sorted movers straight into the sorted keys and
-// storage indices. In the order (key, stayers before movers, rank) the output position of a stayer is its rank
-// among the stayers plus the movers with a smaller key; of a mover, its rank among the movers plus the stayers
-// with a key not above it. CTA j takes MERGE_TILE consecutive stayers and owns the movers [lb_j, lb_j+1), lb_j =
-// the movers below its first stayer key (lb_0 = 0; the last tile owns the movers up to M): every owned mover
-// lies between this tile's first stayer and the next tile's, so both counts come from this tile and its window
-// of movers. Positions outside [0, n) (inconsistent inputs) raise a check instead of writing.
-constexpr int MERGE_NT = 256, MERGE_TILE = 1024;
-
-__device__ __forceinline__ int64_t lower_bound_u32(const uint32_t* v, int64_t lo, int64_t hi, uint32_t key)
+static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* knew, const uint32_t* kold, SortBufs sb, DevStatus* st)
 {
-    while (lo < hi) {
-        const int64_t mid = lo + ((hi - lo) >> 1);
-        if (v[mid] < key)
-            lo = mid + 1;
-        else
-            hi = mid;
+    __shared__ uint32_t s_cnt[SORT_NT / 32], s_first[SORT_NT / 32];
+    const int j = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)j * SORT_TILE;
+    uint32_t nst = 0, first = SORT_NOKEY;
+    // items in storage order; a warp takes 256 consecutive ones, 32 at a time
+    for (int r = 0; r < SORT_PER; r++) {
+        const int64_t i = t0 + (int64_t)w * (32 * SORT_PER) + r * 32 + lane;
+        bool stay = false, move = false;
+        uint32_t k = 0;
+        if (i < sb.n) {
+            k = knew[i];
+            stay = k == kold[i];
+            move = !stay;
+        }
+        const unsigned bs = __ballot_sync(0xffffffffu, stay), bm = __ballot_sync(0xffffffffu, move);
+        if (lane == 0 && i < sb.n) sb.stay_bits[i >> 5] = bs; // the merge reads these: it overwrites the old keys
+        if (bs && first == SORT_NOKEY) first = __shfl_sync(0xffffffffu, k, __ffs(bs) - 1);
+        nst += __popc(bs);
+        if (bm) {
+            uint64_t base = 0;
+            if (lane == 0) base = (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)__popc(bm));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (move) {
+                const uint64_t pos = base + __popc(bm & ((1u << lane) - 1u));
+                if (pos < (uint64_t)sb.mcap) sb.m_idx[pos] = (uint32_t)i;
+            }
+        }
     }
-    return lo;
-}
-
-// lower bound of key in the sorted v[lo, hi) by a whole warp: 32 probes per step narrow the range 32-fold, so a
-// search over 2^17 values takes four dependent loads instead of seventeen. Every lane must call it.
-__device__ __forceinline__ int64_t warp_lower_bound(const uint32_t* v, int64_t lo, int64_t hi, uint32_t key)
-{
-    const int lane = threadIdx.x & 31;
-    while (hi - lo > 32) { // the answer lies in [lo, hi]
-        const int64_t step = (hi - lo + 31) / 32, p = lo + lane * step;
-        const int c = __popc(__ballot_sync(0xffffffffu, p < hi && v[p] < key)); // probes below the answer
-        const int64_t nlo = c == 0 ? lo : lo + (int64_t)(c - 1) * step + 1;
-        const int64_t nhi = c == 32 ? hi : (lo + (int64_t)c * step < hi ? lo + (int64_t)c * step : hi);
-        lo = nlo;
-        hi = nhi;
-    }
-    const int64_t p = lo + lane;
-    return lo + __popc(__ballot_sync(0xffffffffu, p < hi && v[p] < key));
-}
-
-static __global__ void __launch_bounds__(MERGE_NT) k_inc_merge(const uint32_t* stay, const uint32_t* keys, const uint32_t* mkeys, const uint32_t* mvals,
-    const int64_t* cnt, int64_t n, int64_t mcap, uint32_t* out_keys, uint32_t* out_vals, DevStatus* st)
-{
-    __shared__ uint32_t sk[MERGE_TILE]; // this tile's stayer keys
-    __shared__ int64_t s_lb[2];
-    const int64_t S = cnt[0], M = cnt[1];
-    if (S < 0 || M < 0 || S + M != n || M > mcap) return; // k_inc_prep raised FLAG_SORT: the substep is repeated
-    const int64_t a0 = (int64_t)blockIdx.x * MERGE_TILE;
-    if (a0 >= S && blockIdx.x > 0) return; // (tile 0 also runs when every particle moved)
-    const int na = (int)(S - a0 < MERGE_TILE ? (S - a0 > 0 ? S - a0 : 0) : MERGE_TILE);
-    for (int t = threadIdx.x; t < na; t += MERGE_NT) sk[t] = keys[stay[a0 + t]];
-    const int warp = threadIdx.x >> 5;
-    if (warp < 2) { // warp 0: this tile's first mover, warp 1: the next tile's (both warp-uniform branches)
-        int64_t lb;
-        if (warp == 0)
-            lb = blockIdx.x == 0 ? 0 : warp_lower_bound(mkeys, 0, M, keys[stay[a0]]);
-        else
-            lb = a0 + MERGE_TILE >= S ? M : warp_lower_bound(mkeys, 0, M, keys[stay[a0 + MERGE_TILE]]);
-        if ((threadIdx.x & 31) == 0) s_lb[warp] = lb;
+    if (lane == 0) {
+        s_cnt[w] = nst;
+        s_first[w] = first;
     }
     __syncthreads();
-    const int64_t lo = s_lb[0], hi = s_lb[1] > s_lb[0] ? s_lb[1] : s_lb[0];
-    for (int t = threadIdx.x; t < na; t += MERGE_NT) {
-        const uint32_t k = sk[t];
-        const int64_t pos = a0 + t + lower_bound_u32(mkeys, lo, hi, k);
-        if (pos < 0 || pos >= n) {
-            check_failed(st, 8);
-            continue;
+    if (threadIdx.x == 0) {
+        uint32_t c = 0, f = SORT_NOKEY;
+        for (int q = 0; q < SORT_NT / 32; q++) {
+            c += s_cnt[q];
+            if (f == SORT_NOKEY) f = s_first[q];
         }
-        out_keys[pos] = k;
-        out_vals[pos] = stay[a0 + t];
+        sb.t_stay[j] = c;
+        sb.t_first[j] = f;
     }
-    for (int64_t m = lo + threadIdx.x; m < hi; m += MERGE_NT) {
-        const uint32_t k = mkeys[m];
-        // stayers of this tile with a key not above k
-        int l = 0, h = na;
-        while (l < h) {
-            const int mid = (l + h) >> 1;
-            if (sk[mid] <= k)
-                l = mid + 1;
-            else
-                h = mid;
+    (void)st;
+}
+
+// one CTA: exclusive offsets of the tiles' stayers, B = suffix minimum of the first stayer keys (stayers ascend in
+// storage order, so this is the first stayer key at or after each tile), bucket counters cleared; too many movers
+// raise FLAG_SORT
+static __global__ void __launch_bounds__(1024) k_sort_scan1(SortBufs sb, DevStatus* st)
+{
+    __shared__ uint32_t s_part[1024];
+    const int T = sb.tiles, tid = threadIdx.x;
+    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
+    const int64_t M = sb.cnt[0];
+    if (tid == 0) atomicMax(&st->max_movers, (uint32_t)(M < 0xffffffffLL ? M : 0xffffffffLL));
+    if (tid == 0 && M > sb.mcap) raise_flag(st, FLAG_SORT);
+    uint32_t sum = 0;
+    for (int q = lo; q < hi; q++) sum += sb.t_stay[q];
+    s_part[tid] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) { // inclusive scan of the per-thread sums
+        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
+        __syncthreads();
+        s_part[tid] += v;
+        __syncthreads();
+    }
+    uint32_t run = tid ? s_part[tid - 1] : 0u;
+    for (int q = lo; q < hi; q++) {
+        const uint32_t c = sb.t_stay[q];
+        sb.t_stay[q] = run;
+        run += c;
+        sb.b_cnt[q] = 0;
+    }
+    __syncthreads();
+    // suffix minimum of the first keys: per-thread block minima, scanned from the right
+    uint32_t mn = SORT_NOKEY;
+    for (int q = lo; q < hi; q++) mn = min(mn, sb.t_first[q]);
+    s_part[tid] = mn;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid + o < 1024 ? s_part[tid + o] : SORT_NOKEY;
+        __syncthreads();
+        s_part[tid] = min(s_part[tid], v);
+        __syncthreads();
+    }
+    uint32_t suf = tid + 1 < 1024 ? s_part[tid + 1] : SORT_NOKEY;
+    for (int q = hi - 1; q >= lo; q--) {
+        suf = min(suf, sb.t_first[q]);
+        sb.t_first[q] = suf;
+    }
+}
+
+static __global__ void k_sort_bucket(const uint32_t* knew, SortBufs sb)
+{
+    const int64_t M = min(sb.cnt[0], sb.mcap);
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = sb.m_idx[m];
+        const uint32_t k = i < (uint64_t)sb.n ? knew[i] : SORT_NOKEY;
+        int lo = 0, hi = sb.tiles; // first j with B[j] > k
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sb.t_first[mid] <= k) lo = mid + 1;
+            else hi = mid;
         }
-        const int64_t pos = m + a0 + l;
-        if (pos < 0 || pos >= n) {
+        const uint32_t b = lo > 0 ? (uint32_t)(lo - 1) : 0u;
+        sb.m_bkt[m] = b;
+        sb.m_tkt[m] = atomicAdd(&sb.b_cnt[b], 1u);
+    }
+}
+
+// one CTA: exclusive offsets of the buckets' movers
+static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
+{
+    __shared__ uint32_t s_part[1024];
+    const int T = sb.tiles, tid = threadIdx.x;
+    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
+    uint32_t sum = 0;
+    for (int q = lo; q < hi; q++) sum += sb.b_cnt[q];
+    s_part[tid] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
+        __syncthreads();
+        s_part[tid] += v;
+        __syncthreads();
+    }
+    uint32_t run = tid ? s_part[tid - 1] : 0u;
+    for (int q = lo; q < hi; q++) {
+        const uint32_t c = sb.b_cnt[q];
+        sb.b_cnt[q] = run;
+        run += c;
+    }
+}
+
+static __global__ void k_sort_place(const uint32_t* knew, SortBufs sb, DevStatus* st)
+{
+    const int64_t M = min(sb.cnt[0], sb.mcap);
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = sb.m_idx[m];
+        const uint64_t pos = (uint64_t)sb.b_cnt[sb.m_bkt[m]] + sb.m_tkt[m];
+        if (pos >= (uint64_t)M || i >= (uint64_t)sb.n) {
+            check_failed(st, 8);
+            continue;
+        }
+        sb.b_key[pos] = knew[i];
+        sb.b_idx[pos] = i;
+    }
+}
+
+static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* knew, SortBufs sb, uint32_t* out_keys, uint32_t* out_vals, DevStatus* st)
+{
+    __shared__ uint32_t s_key[SORT_TILE], s_idx[SORT_TILE]; // the tile's stayers in storage (= key) order
+    __shared__ uint32_t m_key[SORT_MAXM], m_idx[SORT_MAXM], m_key2[SORT_MAXM], m_idx2[SORT_MAXM];
+    __shared__ uint32_t s_wcnt[SORT_PER][SORT_NT / 32];
+    __shared__ int s_ns;
+    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t M = sb.cnt[0];
+    if (M > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
+    const uint32_t bo = sb.b_cnt[j], be = j + 1 < sb.tiles ? sb.b_cnt[j + 1] : (uint32_t)M;
+    if (be < bo || be - bo > (uint32_t)SORT_MAXM) {
+        if (tid == 0) raise_flag(st, FLAG_SORT);
+        return;
+    }
+    const int nm = (int)(be - bo);
+    // the tile's stayers, compacted in storage order: item (r, w, lane) = t0 + r*256 + w*32 + lane
+    const int64_t t0 = (int64_t)j * SORT_TILE;
+    unsigned mine = 0; // bit r: this thread's item of round r stays
+    uint32_t keys[SORT_PER];
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const int64_t i = t0 + r * SORT_NT + tid;
+        keys[r] = 0;
+        bool stay = false;
+        if (i < sb.n) {
+            keys[r] = knew[i];
+            stay = (sb.stay_bits[i >> 5] >> lane) & 1u; // i % 32 == lane: rounds and warps start at multiples of 32
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, stay);
+        if (stay) mine |= 1u << r;
+        if (lane == 0) s_wcnt[r][w] = __popc(b);
+    }
+    for (int q = tid; q < nm; q += SORT_NT) {
+        m_key[q] = sb.b_key[bo + q];
+        m_idx[q] = sb.b_idx[bo + q];
+    }
+    __syncthreads();
+    if (tid == 0) { // exclusive offsets of the (round, warp) groups, in storage order
+        uint32_t run = 0;
+        for (int r = 0; r < SORT_PER; r++)
+            for (int q = 0; q < SORT_NT / 32; q++) {
+                const uint32_t c = s_wcnt[r][q];
+                s_wcnt[r][q] = run;
+                run += c;
+            }
+        s_ns = (int)run;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
+        if ((mine >> r) & 1u) {
+            const uint32_t pos = s_wcnt[r][w] + __popc(b & ((1u << lane) - 1u));
+            s_key[pos] = keys[r];
+            s_idx[pos] = (uint32_t)(t0 + r * SORT_NT + tid);
+        }
+    }
+    // the bucket's movers ranked by (key, storage index): distinct pairs, so the ranks are a permutation
+    for (int q = tid; q < nm; q += SORT_NT) {
+        const uint32_t k = m_key[q], i = m_idx[q];
+        int rank = 0;
+        for (int o = 0; o < nm; o++) rank += (m_key[o] < k || (m_key[o] == k && m_idx[o] < i)) ? 1 : 0;
+        m_key2[rank] = k;
+        m_idx2[rank] = i;
+    }
+    __syncthreads();
+    const int ns = s_ns;
+    const int64_t base = (int64_t)sb.t_stay[j] + bo; // elements of lower tiles and buckets
+    for (int t = tid; t < ns; t += SORT_NT) { // stayer: its rank + the bucket's movers with a smaller key
+        const uint32_t k = s_key[t];
+        int lo = 0, hi = nm;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (m_key2[mid] < k) lo = mid + 1;
+            else hi = mid;
+        }
+        const int64_t pos = base + t + lo;
+        if (pos < 0 || pos >= sb.n) {
             check_failed(st, 8);
             continue;
         }
         out_keys[pos] = k;
-        out_vals[pos] = mvals[m];
+        out_vals[pos] = s_idx[t];
+    }
+    for (int r = tid; r < nm; r += SORT_NT) { // mover: its rank + the tile's stayers with a key not above its own
+        const uint32_t k = m_key2[r];
+        int lo = 0, hi = ns;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (s_key[mid] <= k) lo = mid + 1;
+            else hi = mid;
+        }
+        const int64_t pos = base + r + lo;
+        if (pos < 0 || pos >= sb.n) {
+            check_failed(st, 8);
+            continue;
+        }
+        out_keys[pos] = k;
+        out_vals[pos] = m_idx2[r];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// group heads: the first sorted index of every (scene, SPGrid page), compacted in order into g_start, their number
+// into n_groups. One pass over the sorted keys with a decoupled look-back: tiles are taken in order from a counter
+// (a tile's predecessors have started, so they publish), each publishes its head count, then the running total
+// once its predecessors' is known. Waits are bounded; a wait that runs out raises FLAG_TIMEOUT.
+// ---------------------------------------------------------------------------------------------------
+constexpr uint64_t LB_AGG = 1ull << 62, LB_PREFIX = 2ull << 62, LB_VALUE = (1ull << 62) - 1;
+
+static __global__ void __launch_bounds__(SORT_NT) k_group_heads(const uint64_t* keys, int64_t n, KeyLayout kl, uint64_t* status, uint32_t* counter,
+    uint32_t* g_start, uint32_t cap, DevStatus* st)
+{
+    __shared__ uint32_t s_w[SORT_PER][SORT_NT / 32];
+    __shared__ int s_tile;
+    __shared__ uint64_t s_prefix;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int j = s_tile;
+    const int64_t t0 = (int64_t)j * SORT_TILE;
+    unsigned mine = 0;
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const int64_t i = t0 + r * SORT_NT + tid;
+        const bool head = i < n && (i == 0 || kl.group(kl.at(keys, (uint32_t)i)) != kl.group(kl.at(keys, (uint32_t)(i - 1))));
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        if (head) mine |= 1u << r;
+        if (lane == 0) s_w[r][w] = __popc(b);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (int r = 0; r < SORT_PER; r++)
+            for (int q = 0; q < SORT_NT / 32; q++) {
+                const uint32_t c = s_w[r][q];
+                s_w[r][q] = run;
+                run += c;
+            }
+        volatile uint64_t* vs = status;
+        uint64_t prefix = 0;
+        if (j == 0)
+            vs[0] = LB_PREFIX | run;
+        else {
+            vs[j] = LB_AGG | run;
+            int q = j - 1;
+            uint32_t spins = 0;
+            while (q >= 0) {
+                const uint64_t v = vs[q];
+                if (v & LB_PREFIX) {
+                    prefix += v & LB_VALUE;
+                    break;
+                }
+                if (v & LB_AGG) {
+                    prefix += v & LB_VALUE;
+                    q--;
+                    continue;
+                }
+                if (++spins > (1u << 22)) { // a predecessor never published: give up (the substep is aborted)
+                    raise_flag(st, FLAG_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+            vs[j] = LB_PREFIX | (prefix + run);
+        }
+        s_prefix = prefix;
+        if ((int64_t)(j + 1) * SORT_TILE >= n) st->n_groups = (uint32_t)(prefix + run); // the last tile
+    }
+    __syncthreads();
+    const uint64_t prefix = s_prefix;
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
+        if ((mine >> r) & 1u) {
+            const uint64_t pos = prefix + s_w[r][w] + __popc(b & ((1u << lane) - 1u));
+            if (pos < cap) g_start[pos] = (uint32_t)(t0 + r * SORT_NT + tid);
+            else check_failed(st, 9);
+        }
     }
 }
 
@@ -1021,21 +1271,22 @@ __global__ void __launch_bounds__(ScatterShape<T, CHUNK, NBUF>::NT, MIN_CTAS) k_
 // payload in shared memory (bank-staggered at q + q/8); phases 2 and 3 are those of k_scatter. No payload
 // round trip through HBM, at the price of the state loads' latency inside the kernel: the autotuner times
 // both forms on the workload.
-template <class T>
+// CH: particles staged per chunk (a whole block at 8 per cell by default; half of it lets more CTAs fit)
+template <class T, int CH = (sizeof(T) == 4 ? 512 : 256)>
 struct FusedShape {
     using L = typename LayoutOf<T>::type;
     static constexpr int NT = 3 * L::nodes; // cells x stencil x-offsets
-    static constexpr int CHUNK = sizeof(T) == 4 ? 512 : 256;
+    static constexpr int CHUNK = CH;
     static constexpr int CPAD = CHUNK + CHUNK / 8;
     static constexpr size_t dyn_bytes = sizeof(T) * Y_CELL * CPAD; // fields Y_F..Y_D
 };
 
 // MINB: CTAs per SM the register budget is cut for (more CTAs hide more load latency; fewer registers may spill)
-template <class T, int MODELS, int MINB>
-__global__ void __launch_bounds__(FusedShape<T>::NT, MINB) k_p2g_fused(StepArgs<T> a)
+template <class T, int MODELS, int MINB, int CH = FusedShape<T>::CHUNK>
+__global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
-    using S = FusedShape<T>;
+    using S = FusedShape<T, CH>;
     constexpr int NT = S::NT, CHUNK = S::CHUNK, CPAD = S::CPAD, NC = L::nodes;
     extern __shared__ __align__(16) unsigned char fused_dyn[];
     T* pay = reinterpret_cast<T*>(fused_dyn);
