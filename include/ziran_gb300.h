@@ -138,6 +138,22 @@ int zr_scene_save_state(zr_scene* s, void* buf, int64_t bytes);
 int zr_scene_load_state(zr_scene* s, const void* buf, int64_t bytes);
 int zr_scene_write_state_file(zr_scene* s, const char* path);
 int zr_scene_read_state_file(zr_scene* s, const char* path);
+/* Frame output for visualisation (writePartio, Lib/Ziran/Math/Geometry/PartioIO.h:166-210, called from
+ * MpmSimulationBase::writeState, MpmSimulationBase.cpp:1067-1080; AnisoFractureSimulation::writeState,
+ * Projects/anisofracture/AnisoFractureSimulation.h:73-100, through aniso_visualize_particles_vec,
+ * AnisoVisualizer.h:36-64): a Houdini classic binary geometry file (.bgeo, format version 5, the layout partio
+ * writes) with one point per particle in the caller's order, its position, and the attributes the flags select,
+ * all as 32-bit floats of the vector type: ZR_BGEO_V "v" (3), ZR_BGEO_D "d" (1, damage), ZR_BGEO_A1 "a_1"
+ * (3, the current fibre director R e1, R the rotation of F's polar decomposition; the fibre of F0 from
+ * initializeRotatedFHelper is its first column). flags = 0 writes positions only, as writePartio does. The
+ * reference's "laplacian" attribute is not written: the substep does not keep it. */
+#define ZR_BGEO_V 1
+#define ZR_BGEO_D 2
+#define ZR_BGEO_A1 4
+int zr_scene_write_bgeo(zr_scene* s, const char* path, int flags);
+/* The file writer alone, for host arrays: n points at x (3n doubles), nattr attributes, attribute k named
+ * names[k] with sizes[k] components per point at data[k] (sizes[k] * n doubles). Values are stored as floats. */
+int zr_write_bgeo(const char* path, int64_t n, const double* x, int nattr, const char* const* names, const int32_t* sizes, const double* const* data);
 /* Advance whole frames the way SimulationBase::simulate does (SimulationBase.h:275-354): substeps from
  * TimeStepping::nextDt (TimeStepping.h:45-59) between min_dt and the scene's dt (max_dt), hitting every frame
  * boundary exactly; with cfl_dt != 0 the wanted substep is cfl dx / max particle speed (calculateDt,

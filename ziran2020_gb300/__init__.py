@@ -23,6 +23,7 @@ COROTATED, NEOHOOKEAN_BORDEN, QR_STABLE_NEOHOOKEAN = 0, 1, 2
 STICKY, SLIP, SEPARATE = 1, 2, 3
 FIELD = {"x": (0, 3), "v": (1, 3), "C": (2, 9), "F": (3, 9), "d": (4, 1), "m": (5, 1), "V0": (6, 1), "sigma_c": (7, 1), "dtilde_max": (8, 1)}
 RECIPE_ELASTIC_BOX, RECIPE_ANISO_SLAB = 0, 1
+BGEO_V, BGEO_D, BGEO_A1 = 1, 2, 4
 
 
 class ZrError(RuntimeError):
@@ -98,6 +99,8 @@ def load_library(build_if_needed=True):
         "zr_scene_load_state": (i32, [vp, vp, i64]),
         "zr_scene_write_state_file": (i32, [vp, C.c_char_p]),
         "zr_scene_read_state_file": (i32, [vp, C.c_char_p]),
+        "zr_scene_write_bgeo": (i32, [vp, C.c_char_p, i32]),
+        "zr_write_bgeo": (i32, [C.c_char_p, i64, pd, i32, P(C.c_char_p), P(C.c_int32), P(pd)]),
         "zr_scene_advance_frames": (i32, [vp, i32, d, d, i32, P(i32)]),
         "zr_scene_set_schedule": (i32, [vp, P(i32)]),
         "zr_scene_get_schedule": (i32, [vp, P(i32)]),
@@ -370,6 +373,12 @@ class Scene:
     def read_state(self, path):
         self._check(self.L.zr_scene_read_state_file(self.h, os.fsencode(path)))
 
+    def write_bgeo(self, path, v=False, d=False, a1=False):
+        """Frame file for visualisation (.bgeo): positions and, as chosen, velocity "v", damage "d" and the current
+        fibre director "a_1" (the reference's writePartio / anisoFrax frames)."""
+        flags = (BGEO_V if v else 0) | (BGEO_D if d else 0) | (BGEO_A1 if a1 else 0)
+        self._check(self.L.zr_scene_write_bgeo(self.h, os.fsencode(path), flags))
+
     def advance_frames(self, frames, frame_dt, min_dt=1e-6, cfl_dt=False):
         """Whole frames with the reference's time stepping and CFL restarts; returns the number of restarts."""
         r = C.c_int()
@@ -556,3 +565,22 @@ class Server:
 
 def version():
     return load_library().zr_version().decode()
+
+
+def write_bgeo(path, x, attributes=None):
+    """Write n points (x: (n, 3)) and named float attributes ({name: (n,) or (n, k) array}) as a .bgeo file."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+    attributes = attributes or {}
+    names, sizes, arrays = [], [], []
+    for k, a in attributes.items():
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(len(x), -1)
+        names.append(k.encode())
+        sizes.append(a.shape[1])
+        arrays.append(a)
+    na = len(names)
+    cn = (C.c_char_p * max(1, na))(*names)
+    cs = (C.c_int32 * max(1, na))(*sizes)
+    cd = (C.POINTER(C.c_double) * max(1, na))(*[_dp(a) for a in arrays])
+    rc = load_library().zr_write_bgeo(os.fsencode(path), len(x), _dp(x), na, cn, cs, cd)
+    if rc:
+        raise ZrError(rc, f"cannot write {path}")

@@ -1,6 +1,7 @@
 // C ABI of the GB300 explicit-MPM engine (declared in include/ziran_gb300.h).
 #include "../../include/ziran_gb300.h"
 #include "engine.h"
+#include "physics.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -662,6 +663,123 @@ int zr_scene_read_state_file(zr_scene* s, const char* path)
     while ((got = std::fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
     std::fclose(f);
     return zr_scene_load_state(s, buf.data(), (int64_t)buf.size());
+}
+
+// ---------------------------------------------------------------------------------------------------
+// .bgeo frame files. Houdini's classic binary geometry layout, version 5, as partio writes it (all numbers
+// big-endian): the magic "Bgeo", the version character 'V' and int32 version 5; int32 counts of points,
+// primitives, point groups, primitive groups, point attributes (besides the position), vertex attributes,
+// primitive attributes and detail attributes; per point attribute its name (uint16 length, then the bytes), its
+// component count (uint16), its type (int32: 5 = float vector) and one default value per component (float32);
+// then per point x, y, z, w = 1 and each attribute's components (float32); then the end bytes 0x00 0xff.
+// ---------------------------------------------------------------------------------------------------
+namespace {
+
+struct BigEndianFile {
+    FILE* f = nullptr;
+    bool ok = true;
+    void bytes(const void* p, size_t n) { ok = ok && std::fwrite(p, 1, n, f) == n; }
+    void u16(uint16_t v)
+    {
+        const unsigned char b[2] = { (unsigned char)(v >> 8), (unsigned char)v };
+        bytes(b, 2);
+    }
+    void u32(uint32_t v)
+    {
+        const unsigned char b[4] = { (unsigned char)(v >> 24), (unsigned char)(v >> 16), (unsigned char)(v >> 8), (unsigned char)v };
+        bytes(b, 4);
+    }
+    void f32(float v)
+    {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        u32(u);
+    }
+};
+
+} // namespace
+
+extern "C" int zr_write_bgeo(const char* path, int64_t n, const double* x, int nattr, const char* const* names, const int32_t* sizes,
+    const double* const* data)
+{
+    if (!path || n < 0 || n > 0x7fffffff || (n > 0 && !x) || nattr < 0 || (nattr > 0 && (!names || !sizes || !data))) return ZR_ERR_ARG;
+    for (int k = 0; k < nattr; k++)
+        if (!names[k] || sizes[k] < 1 || sizes[k] > 0xffff || std::strlen(names[k]) > 0xffff || (n > 0 && !data[k])) return ZR_ERR_ARG;
+    BigEndianFile o;
+    o.f = std::fopen(path, "wb");
+    if (!o.f) return ZR_ERR_ARG;
+    o.bytes("Bgeo", 4);
+    o.bytes("V", 1);
+    o.u32(5);
+    const uint32_t counts[8] = { (uint32_t)n, 0, 0, 0, (uint32_t)nattr, 0, 0, 0 };
+    for (uint32_t c : counts) o.u32(c);
+    for (int k = 0; k < nattr; k++) {
+        const size_t len = std::strlen(names[k]);
+        o.u16((uint16_t)len);
+        o.bytes(names[k], len);
+        o.u16((uint16_t)sizes[k]);
+        o.u32(5); // vector of floats (Partio::VECTOR, as the reference adds every attribute)
+        for (int c = 0; c < sizes[k]; c++) o.f32(0.0f);
+    }
+    std::vector<unsigned char> row;
+    for (int64_t p = 0; p < n && o.ok; p++) {
+        for (int a = 0; a < 3; a++) o.f32((float)x[3 * p + a]);
+        o.f32(1.0f);
+        for (int k = 0; k < nattr; k++)
+            for (int c = 0; c < sizes[k]; c++) o.f32((float)data[k][(size_t)sizes[k] * p + c]);
+    }
+    const unsigned char end[2] = { 0x00, 0xff };
+    o.bytes(end, 2);
+    const bool closed = std::fclose(o.f) == 0;
+    return o.ok && closed ? ZR_OK : ZR_ERR_ARG;
+}
+
+extern "C" int zr_scene_write_bgeo(zr_scene* s, const char* path, int flags)
+{
+    NEED_ENGINE(s);
+    if (!path || (flags & ~(ZR_BGEO_V | ZR_BGEO_D | ZR_BGEO_A1))) return set_err(s->err, ZR_ERR_ARG, "unknown .bgeo attribute flags");
+    const int64_t n = s->desc.n;
+    std::vector<double> x((size_t)(3 * n)), v, d, a1, F;
+    std::vector<const char*> names;
+    std::vector<int32_t> sizes;
+    std::vector<const double*> data;
+    auto field = [&](int f, std::vector<double>& out, int comps) {
+        out.resize((size_t)(comps * n));
+        int rc = s->eng->get_field(0, f, out.data(), 0);
+        if (rc) s->err = s->eng->last_error();
+        return rc;
+    };
+    int rc = field(ZR_FIELD_X, x, 3);
+    if (!rc && (flags & ZR_BGEO_V)) {
+        rc = field(ZR_FIELD_V, v, 3);
+        names.push_back("v");
+        sizes.push_back(3);
+        data.push_back(v.data());
+    }
+    if (!rc && (flags & ZR_BGEO_A1)) {
+        rc = field(ZR_FIELD_F, F, 9);
+        if (!rc) { // the current director R e1 (AnisoFractureSimulation.h:90-97 takes R = U V^T of F's SVD)
+            a1.resize((size_t)(3 * n));
+            for (int64_t p = 0; p < n; p++) {
+                double R[9];
+                zr::polar_rotation(F.data() + 9 * p, R);
+                for (int a = 0; a < 3; a++) a1[3 * p + a] = R[3 * a];
+            }
+            names.push_back("a_1");
+            sizes.push_back(3);
+            data.push_back(a1.data());
+        }
+    }
+    if (!rc && (flags & ZR_BGEO_D)) {
+        rc = field(ZR_FIELD_D, d, 1);
+        names.push_back("d");
+        sizes.push_back(1);
+        data.push_back(d.data());
+    }
+    if (rc) return rc;
+    rc = zr_write_bgeo(path, n, x.data(), (int)names.size(), names.data(), sizes.data(), data.data());
+    if (rc) return set_err(s->err, rc, std::string("cannot write ") + path);
+    return ZR_OK;
 }
 
 // ---------------------------------------------------------------------------------------------------
