@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--eager", action="store_true", help="with --profile-only: launch kernels one at a time, not as graphs")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
     ap.add_argument("--schedule", default="auto",
-                    help="auto (the autotuner), or fused:CTAS:G2P[:TIGHT], fused2:CTAS:G2P[:TIGHT], fused4:CTAS:G2P[:TIGHT], ws:CTAS:G2P[:TIGHT] or "
+                    help="auto (the autotuner), or fused:CTAS:G2P[:TIGHT], fused2:CTAS:G2P[:TIGHT], ws:CTAS:G2P[:TIGHT] or "
                          "split:CHUNK:BUFFERS:CTAS:G2P[:TIGHT] "
                          "(a fixed launch schedule)")
     return ap.parse_args()
@@ -294,8 +294,8 @@ def apply_schedule(obj, spec):
     if spec == "auto":
         return
     f = spec.split(":")
-    if f[0] in ("fused", "fused2", "ws", "fused4"):
-        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused={"fused": 1, "fused2": 2, "ws": 3, "fused4": 4}[f[0]],
+    if f[0] in ("fused", "fused2", "ws"):
+        obj.set_schedule(0, 0, int(f[1]), int(f[2]), fused={"fused": 1, "fused2": 2, "ws": 3}[f[0]],
                          g2p_tight=int(f[3]) if len(f) > 3 else 0)
     else:
         obj.set_schedule(int(f[1]), int(f[2]), int(f[3]), int(f[4]), g2p_tight=int(f[5]) if len(f) > 5 else 0)

@@ -75,7 +75,7 @@ def test_aniso_slab_fp64_matches_oracle(steps):
 def test_qr_stable_slab_matches_oracle(fiber):
     """QR-stable Neo-Hookean (the AnisoMPM demos' model, fibre stiffness kx = fiber mu as in
     examples/tubepull.h:104-107) with anisotropic damage: FP64 within 1e-12 of the FP64 oracle after 30
-    substeps, FP32 within 1e-5 after 30."""
+    substeps, FP32 within 1e-5 after 30; damage within 1e-9 (FP64) and 3e-4 (FP32, about 3x the measured 9e-5)."""
     d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0, model=zr.QR_STABLE_NEOHOOKEAN, fiber=fiber)
     o = scenes.oracle_scene(d, 8)
     o.step(30)
@@ -87,17 +87,19 @@ def test_qr_stable_slab_matches_oracle(fiber):
         e = scenes.errors(scenes.gpu_state(s), r)
         print(f"QR-stable slab, fibre {fiber}, precision {prec}: {e}")
         assert e["x"][0] < xtol, (prec, e)
-        assert e["d"][0] < (1e-9 if prec == zr.F64 else 2e-2), (prec, e)
+        assert e["d"][0] < (1e-9 if prec == zr.F64 else 3e-4), (prec, e)
 
 
 def test_aniso_slab_fp32_close_to_fp64_oracle():
+    """FP32 after 60 substeps of a damaging slab: positions within 1e-5; damage max within 1e-3 and RMS within 5e-5
+    (about 3x the measured 3.4e-4 and 1.7e-5: the damage threshold phi > 1 amplifies FP32 rounding)."""
     d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0)
     s, o, g, r = run_pair(d, zr.F32, 60)
     e = scenes.errors(g, r)
     print(f"slab FP32 after 60 substeps: {e}")
     assert e["x"][0] < 1e-5, e
-    assert e["d"][0] < 2e-2, e
-    assert e["d"][1] < 1e-3, e
+    assert e["d"][0] < 1e-3, e
+    assert e["d"][1] < 5e-5, e
 
 
 def test_conservation_fp64_reductions():

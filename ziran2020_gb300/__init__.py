@@ -388,8 +388,8 @@ class Scene:
     def set_schedule(self, chunk, buffers, p2g_ctas_per_sm, g2p_threads, fused=0, g2p_tight=0):
         """chunk/buffers select the split P2G form's staging; fused=1 selects the one-kernel P2G, fused=2 the
         same with registers cut for one more CTA per SM, fused=3 its warp-specialised form (producer and consumer
-        warps), fused=4 the one-kernel P2G cut for two more CTAs per SM (half-block chunks); g2p_tight=1 cuts G2P
-        registers likewise."""
+        warps); g2p_tight: +1 cuts G2P
+        registers likewise, +2 stages the velocities of the 8 neighbouring blocks by bulk asynchronous copies."""
         arr = (C.c_int32 * 6)(int(fused), chunk, buffers, p2g_ctas_per_sm, g2p_threads, int(g2p_tight))
         self._check(self.L.zr_scene_set_schedule(self.h, arr))
 

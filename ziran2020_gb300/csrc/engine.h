@@ -66,14 +66,14 @@ struct StepReport {
 struct Schedule {
     int fused = 0; // P2G: 1 = one kernel evaluating the stress itself, 2 = the same with registers cut for one more
                    // CTA per SM, 3 = the same split into producer warps (state loads, stress, payload) and consumer
-                   // warps (accumulation) working on alternating shared-memory buffers, 4 = form 1 cut for two more
-                   // CTAs per SM with half-block chunks; 0 = a stress kernel writing a
+                   // warps (accumulation) working on alternating shared-memory buffers; 0 = a stress kernel writing a
                    // payload that a scatter kernel streams into shared memory with bulk asynchronous copies
     int chunk = 0; // P2G: particles per chunk staged in shared memory by one bulk copy per payload field
     int buffers = 1; // P2G: staging buffers (2: the next chunk's copy overlaps the whole current chunk)
     int scatter_ctas_per_sm = 0; // P2G scatter: persistent CTAs per SM
     int g2p_threads = 0; // G2P: threads per CTA, i.e. particles per pass over a group
-    int g2p_tight = 0; // G2P: 1 = registers cut for more resident threads per SM
+    int g2p_tight = 0; // G2P: +1 = registers cut for more resident threads per SM; +2 = the velocities of the group's
+                       // 8 neighbouring blocks staged in shared memory by bulk asynchronous copies
     int tuned = 0; // 1 when chosen by the autotuner's measurements
 };
 

@@ -44,12 +44,12 @@ class Engine final : public EngineBase {
     // G2P register budgets: threads per SM (FP32 448: a ~146-register cap, under which ptxas settles at 128 with
     // little spilling; 512: a 128 cap, more spills; FP64: ~255 or ~200)
     static constexpr int G2P_RES[2] = { sizeof(T) == 4 ? 448 : 256, sizeof(T) == 4 ? 512 : 320 };
-    // fused P2G variants (schedule fused = 1, 2, 4): register budgets cut for 2, 3 or 4 CTAs per SM (FP32; 1, 2 or 3
-    // for FP64), the last with half-block chunks so that four CTAs' staging buffers fit in shared memory
-    static constexpr int FUSED_MINB[3] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2, sizeof(T) == 4 ? 4 : 3 };
-    static constexpr int FUSED_CH[3] = { FusedShape<T>::CHUNK, FusedShape<T>::CHUNK, FusedShape<T>::CHUNK / 2 };
-    static int fused_variant(int fused) { return fused == 4 ? 2 : fused - 1; }
-    static int fused_code(int fv) { return fv == 2 ? 4 : fv + 1; }
+    // fused P2G variants (schedule fused = 1, 2): register budgets cut for 2 or 3 CTAs per SM (FP32; 1 or 2 for FP64).
+    // (Cut for 4 CTAs, with half-block chunks so that the staging buffers fit, it spilled and ran 60% slower.)
+    static constexpr int FUSED_MINB[2] = { sizeof(T) == 4 ? 2 : 1, sizeof(T) == 4 ? 3 : 2 };
+    static constexpr int FUSED_CH[2] = { FusedShape<T>::CHUNK, FusedShape<T>::CHUNK };
+    static int fused_variant(int fused) { return fused - 1; }
+    static int fused_code(int fv) { return fv + 1; }
 
 public:
     Engine() { init_device(); }
@@ -650,8 +650,8 @@ public:
     Schedule schedule() const override { return sched_; }
     int set_schedule(const Schedule& sc) override
     {
-        if (sc.fused < 0 || sc.fused > 4 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
-            || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8 || sc.g2p_tight < 0 || sc.g2p_tight > 1)
+        if (sc.fused < 0 || sc.fused > 3 || (!sc.fused && variant_index(sc.chunk, sc.buffers) < 0) || g2p_index(sc.g2p_threads) < 0
+            || sc.scatter_ctas_per_sm < 1 || sc.scatter_ctas_per_sm > 8 || sc.g2p_tight < 0 || sc.g2p_tight > 3)
             return arg("schedule: unknown P2G form, (chunk, buffers) pair or G2P width, or CTAs per SM outside [1, 8]");
         sched_ = sc;
         if (sc.fused) {
@@ -691,8 +691,8 @@ private:
     DevStatus* hst_ = nullptr;
     void *sort_tmp_ = nullptr, *stage_ = nullptr;
     size_t sort_bytes_ = 0, stage_bytes_ = 0;
-    int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[2][3] = { { 1, 1, 1 }, { 1, 1, 1 } };
-    int occ_fused_[3][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [fused variant][model set]
+    int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[4][3] = { { 1, 1, 1 }, { 1, 1, 1 }, { 1, 1, 1 }, { 1, 1, 1 } };
+    int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [fused variant][model set]
     int occ_ws_[4] = { 1, 1, 1, 1 }; // warp-specialised P2G, per model set
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
@@ -938,7 +938,6 @@ private:
         scatter_setup<2>();
         fused_setup_all<0>();
         fused_setup_all<1>();
-        fused_setup_all<2>();
         ws_setup<1>(0);
         ws_setup<2>(1);
         ws_setup<4>(2);
@@ -953,6 +952,12 @@ private:
         g2p_setup<1, 0>();
         g2p_setup<1, 1>();
         g2p_setup<1, 2>();
+        g2p_setup<2, 0>();
+        g2p_setup<2, 1>();
+        g2p_setup<2, 2>();
+        g2p_setup<3, 0>();
+        g2p_setup<3, 1>();
+        g2p_setup<3, 2>();
         for (int& o : occ_scatter_) o = std::max(1, o);
         for (int& o : occ_stress_) o = std::max(1, o);
         for (auto& row : occ_g2p_)
@@ -1109,10 +1114,8 @@ private:
             const int fctas = nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_fused_[fv][models_slot()]);
             if (fv == 0)
                 launch_fused<0>(a, fctas);
-            else if (fv == 1)
-                launch_fused<1>(a, fctas);
             else
-                launch_fused<2>(a, fctas);
+                launch_fused<1>(a, fctas);
         }
         else {
             const int ms = models_slot();
@@ -1141,10 +1144,12 @@ private:
         }
         if (ev) ZR_CUDA(cudaEventRecord(ev[4], stream_));
         const int gi = std::max(0, g2p_index(sched_.g2p_threads));
-        if (sched_.g2p_tight)
-            launch_g2p<1>(a, gi);
-        else
-            launch_g2p<0>(a, gi);
+        switch (sched_.g2p_tight) {
+        case 1: launch_g2p<1>(a, gi); break;
+        case 2: launch_g2p<2>(a, gi); break;
+        case 3: launch_g2p<3>(a, gi); break;
+        default: launch_g2p<0>(a, gi);
+        }
         k_step_end<T><<<1, 256, 0, stream_>>>(d_scenes_, n_scenes(), st_);
         if (ev) ZR_CUDA(cudaEventRecord(ev[5], stream_));
         ZR_CUDA(cudaGetLastError());
@@ -1335,20 +1340,23 @@ private:
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_scatter_[V], k, S::NT, S::dyn_bytes);
     }
+    // G2P variant R = g2p_tight: bit 0 the register budget (G2P_RES), bit 1 the halo staged by bulk copies
     template <int R, int N>
     void g2p_setup()
     {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[R][N], k_g2p<T, G2P_NT[N], G2P_RES[R]>, G2P_NT[N], 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g2p_[R][N], k_g2p<T, G2P_NT[N], G2P_RES[R & 1], (R >> 1) != 0>, G2P_NT[N], 0);
     }
     template <int R>
     void launch_g2p(const StepArgs<T>& a, int gi)
     {
+        constexpr int RES = G2P_RES[R & 1];
+        constexpr bool BULK = (R >> 1) != 0;
         if (gi == 0)
-            k_g2p<T, G2P_NT[0], G2P_RES[R]><<<nsm_ * occ_g2p_[R][0], G2P_NT[0], 0, stream_>>>(a);
+            k_g2p<T, G2P_NT[0], RES, BULK><<<nsm_ * occ_g2p_[R][0], G2P_NT[0], 0, stream_>>>(a);
         else if (gi == 1)
-            k_g2p<T, G2P_NT[1], G2P_RES[R]><<<nsm_ * occ_g2p_[R][1], G2P_NT[1], 0, stream_>>>(a);
+            k_g2p<T, G2P_NT[1], RES, BULK><<<nsm_ * occ_g2p_[R][1], G2P_NT[1], 0, stream_>>>(a);
         else
-            k_g2p<T, G2P_NT[2], G2P_RES[R]><<<nsm_ * occ_g2p_[R][2], G2P_NT[2], 0, stream_>>>(a);
+            k_g2p<T, G2P_NT[2], RES, BULK><<<nsm_ * occ_g2p_[R][2], G2P_NT[2], 0, stream_>>>(a);
     }
     template <int M, int V>
     void fused_setup(int slot)
@@ -1502,7 +1510,7 @@ private:
         for (int vi = 0; vi < 3; vi++)
             for (int c = occ_scatter_[vi]; c >= std::max(1, occ_scatter_[vi] - 1); c--)
                 p2g_c.push_back(Schedule{ 0, VAR_CHUNK[vi], VAR_NBUF[vi], c, G2P_NT[1], 0, 1 });
-        for (int fv = 0; fv < 3; fv++) {
+        for (int fv = 0; fv < 2; fv++) {
             const int of = occ_fused_[fv][models_slot()];
             for (int c = of; c >= std::max(1, of - 1); c--) p2g_c.push_back(Schedule{ fused_code(fv), FUSED_CH[fv], 0, c, G2P_NT[1], 0, 1 });
         }
@@ -1532,7 +1540,7 @@ private:
                 best = sc;
             }
         }
-        for (int gc = 0; gc < 6; gc++) {
+        for (int gc = 0; gc < 12; gc++) {
             const int gi = gc % 3;
             Schedule sc = best;
             sc.g2p_threads = G2P_NT[gi];

@@ -275,10 +275,12 @@ struct SortBufs {
 
 static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* knew, const uint32_t* kold, SortBufs sb, DevStatus* st)
 {
-    __shared__ uint32_t s_cnt[SORT_NT / 32], s_first[SORT_NT / 32];
+    __shared__ uint32_t s_cnt[SORT_NT / 32], s_first[SORT_NT / 32], s_moff[SORT_NT / 32][SORT_PER];
+    __shared__ uint64_t s_base;
     const int j = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t t0 = (int64_t)j * SORT_TILE;
     uint32_t nst = 0, first = SORT_NOKEY;
+    unsigned moves = 0; // bit r: this thread's item of round r moved
     // items in storage order; a warp takes 256 consecutive ones, 32 at a time
     for (int r = 0; r < SORT_PER; r++) {
         const int64_t i = t0 + (int64_t)w * (32 * SORT_PER) + r * 32 + lane;
@@ -293,15 +295,8 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
         if (lane == 0 && i < sb.n) sb.stay_bits[i >> 5] = bs; // the merge reads these: it overwrites the old keys
         if (bs && first == SORT_NOKEY) first = __shfl_sync(0xffffffffu, k, __ffs(bs) - 1);
         nst += __popc(bs);
-        if (bm) {
-            uint64_t base = 0;
-            if (lane == 0) base = (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)__popc(bm));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (move) {
-                const uint64_t pos = base + __popc(bm & ((1u << lane) - 1u));
-                if (pos < (uint64_t)sb.mcap) sb.m_idx[pos] = (uint32_t)i;
-            }
-        }
+        if (move) moves |= 1u << r;
+        if (lane == 0) s_moff[w][r] = __popc(bm);
     }
     if (lane == 0) {
         s_cnt[w] = nst;
@@ -309,13 +304,29 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t c = 0, f = SORT_NOKEY;
+        uint32_t c = 0, f = SORT_NOKEY, m = 0;
         for (int q = 0; q < SORT_NT / 32; q++) {
             c += s_cnt[q];
             if (f == SORT_NOKEY) f = s_first[q];
+            for (int r = 0; r < SORT_PER; r++) { // the tile's movers in storage order: warp-major, then round
+                const uint32_t v = s_moff[q][r];
+                s_moff[q][r] = m;
+                m += v;
+            }
         }
         sb.t_stay[j] = c;
         sb.t_first[j] = f;
+        s_base = m ? (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)m) : 0ull; // one atomic per tile
+    }
+    __syncthreads();
+    const uint64_t base = s_base;
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const unsigned bm = __ballot_sync(0xffffffffu, (moves >> r) & 1u);
+        if ((moves >> r) & 1u) {
+            const uint64_t pos = base + s_moff[w][r] + __popc(bm & ((1u << lane) - 1u));
+            if (pos < (uint64_t)sb.mcap) sb.m_idx[pos] = (uint32_t)(t0 + (int64_t)w * (32 * SORT_PER) + r * 32 + lane);
+        }
     }
     (void)st;
 }
@@ -563,36 +574,50 @@ static __global__ void __launch_bounds__(SORT_NT) k_group_heads(const uint64_t* 
                 s_w[r][q] = run;
                 run += c;
             }
+        s_prefix = run; // the tile's head count until the look-back below replaces it by the prefix
         volatile uint64_t* vs = status;
+        vs[j] = (j == 0 ? LB_PREFIX : LB_AGG) | run;
+    }
+    __syncthreads();
+    if (w == 0) { // look-back by the first warp: 32 predecessors per step, back to the nearest published prefix
+        const uint32_t run = s_prefix;
         uint64_t prefix = 0;
-        if (j == 0)
-            vs[0] = LB_PREFIX | run;
-        else {
-            vs[j] = LB_AGG | run;
+        if (j > 0) {
+            volatile uint64_t* vs = status;
             int q = j - 1;
             uint32_t spins = 0;
-            while (q >= 0) {
-                const uint64_t v = vs[q];
-                if (v & LB_PREFIX) {
-                    prefix += v & LB_VALUE;
-                    break;
+            bool timed_out = false;
+            while (q >= 0 && !timed_out) {
+                const int idx = q - lane;
+                uint64_t v = LB_PREFIX + 0; // before tile 0: a prefix of zero
+                if (idx >= 0) v = vs[idx];
+                while (__any_sync(0xffffffffu, (v & (LB_AGG | LB_PREFIX)) == 0)) {
+                    if (++spins > (1u << 22)) { // a predecessor never published: give up (the substep is aborted)
+                        timed_out = true;
+                        break;
+                    }
+                    __nanosleep(64);
+                    if ((v & (LB_AGG | LB_PREFIX)) == 0) v = vs[idx];
                 }
-                if (v & LB_AGG) {
-                    prefix += v & LB_VALUE;
-                    q--;
-                    continue;
-                }
-                if (++spins > (1u << 22)) { // a predecessor never published: give up (the substep is aborted)
-                    raise_flag(st, FLAG_TIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
+                if (timed_out) break;
+                const unsigned pm = __ballot_sync(0xffffffffu, (v & LB_PREFIX) != 0);
+                const int stop = pm ? __ffs(pm) - 1 : 31; // lanes 0..stop count (lane 0 is the nearest predecessor)
+                uint64_t c = lane <= stop ? (v & LB_VALUE) : 0ull;
+                for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+                prefix += __shfl_sync(0xffffffffu, c, 0);
+                if (pm) break;
+                q -= 32;
             }
-            __threadfence();
-            vs[j] = LB_PREFIX | (prefix + run);
+            if (timed_out && lane == 0) raise_flag(st, FLAG_TIMEOUT);
+            if (lane == 0) {
+                __threadfence();
+                vs[j] = LB_PREFIX | (prefix + run);
+            }
         }
-        s_prefix = prefix;
-        if ((int64_t)(j + 1) * SORT_TILE >= n) st->n_groups = (uint32_t)(prefix + run); // the last tile
+        if (lane == 0) {
+            s_prefix = prefix;
+            if ((int64_t)(j + 1) * SORT_TILE >= n) st->n_groups = (uint32_t)(prefix + run); // the last tile
+        }
     }
     __syncthreads();
     const uint64_t prefix = s_prefix;
@@ -1679,11 +1704,18 @@ struct G2pStage {
     static constexpr int NS = ON ? 2 * G2P_SF * NT : 1, NP = ON ? 2 * NT : 1;
 };
 
-template <class T, int NT, int RESIDENT>
+// BULK: the 8 neighbouring blocks' velocities reach shared memory by bulk asynchronous copies (one 4-field block of
+// NVEL * nodes values per copy, completing on an mbarrier) and the node tile is built from there; otherwise each
+// thread loads its tile nodes from global memory
+template <class T, int NT, int RESIDENT, bool BULK = false>
 __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
     using GS = G2pStage<T, NT>;
+    constexpr int BLK = NVEL * L::nodes; // values of one block's velocity fields (1 KB in both precisions)
+    __shared__ __align__(128) T s_halo[BULK ? 8 * BLK : 1];
+    __shared__ __align__(8) uint64_t s_hbar;
+    uint32_t hphase = 0;
     // the grid velocities around the group's block as one dense node tile (the block plus 2 nodes on the
     // + side of every axis, the reach of the quadratic stencil): every stencil read is a fixed offset
     constexpr int TY = L::sy + 2, TZ = L::sz + 2, TN = (L::sx + 2) * TY * TZ;
@@ -1695,6 +1727,10 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
     __shared__ int s_g, s_nbr[8], s_scene, s_org[3];
     __shared__ uint16_t s_map[TN]; // tile node -> (neighbour block 0-7) << 8 | element in that block
     if (aborted_cta(a.st)) return;
+    if (BULK && threadIdx.x == 0) {
+        mbar_init(&s_hbar, 1);
+        mbar_init_fence();
+    }
     for (int node = threadIdx.x; node < TN; node += NT) {
         const int tx = node / (TY * TZ), ty = (node / TZ) % TY, tz = node % TZ;
         const int ax = tx >= L::sx, ay = ty >= L::sy, az = tz >= L::sz;
@@ -1745,17 +1781,43 @@ __global__ void __launch_bounds__(NT, RESIDENT / NT) k_g2p(StepArgs<T> a)
             cp_async<4>(s_pid + bf * NT + threadIdx.x, P.pid + j);
         };
         // stage the tile from the 8 neighbouring blocks (s_map was built before the first barrier)
-        for (int node = threadIdx.x; node < TN; node += NT) {
-            const int m = s_map[node], slot = s_nbr[m >> 8];
-            const bool ok = slot >= 0 && (uint32_t)slot < a.b_cap;
-            const T* src = a.vel + (size_t)(ok ? slot : 0) * NVEL * L::nodes + (m & 0xff);
-            Quad<T> qv;
-            qv.x = ok ? src[0] : (T)0;
-            qv.y = ok ? src[L::nodes] : (T)0;
-            qv.z = ok ? src[2 * L::nodes] : (T)0;
-            qv.w = ok ? src[3 * L::nodes] : (T)0;
-            tq[node] = qv;
+        if constexpr (BULK) {
+            if (threadIdx.x == 0) { // every thread is past the previous group's reads of s_halo (the barrier above)
+                uint32_t nvalid = 0;
+                for (int b = 0; b < 8; b++) nvalid += (s_nbr[b] >= 0 && (uint32_t)s_nbr[b] < a.b_cap) ? 1u : 0u;
+                fence_async_smem();
+                mbar_arrive_expect_tx(&s_hbar, nvalid * (uint32_t)(BLK * sizeof(T)));
+                for (int b = 0; b < 8; b++) {
+                    const int slot = s_nbr[b];
+                    if (slot >= 0 && (uint32_t)slot < a.b_cap) bulk_load(s_halo + b * BLK, a.vel + (size_t)slot * BLK, (uint32_t)(BLK * sizeof(T)), &s_hbar);
+                }
+            }
+            if (!mbar_wait(&s_hbar, hphase, WAIT_LIMIT_NS)) raise_flag(a.st, FLAG_TIMEOUT);
+            hphase ^= 1u;
+            for (int node = threadIdx.x; node < TN; node += NT) {
+                const int m = s_map[node], slot = s_nbr[m >> 8];
+                const bool ok = slot >= 0 && (uint32_t)slot < a.b_cap;
+                const T* src = s_halo + (m >> 8) * BLK + (m & 0xff);
+                Quad<T> qv;
+                qv.x = ok ? src[0] : (T)0;
+                qv.y = ok ? src[L::nodes] : (T)0;
+                qv.z = ok ? src[2 * L::nodes] : (T)0;
+                qv.w = ok ? src[3 * L::nodes] : (T)0;
+                tq[node] = qv;
+            }
         }
+        else
+            for (int node = threadIdx.x; node < TN; node += NT) {
+                const int m = s_map[node], slot = s_nbr[m >> 8];
+                const bool ok = slot >= 0 && (uint32_t)slot < a.b_cap;
+                const T* src = a.vel + (size_t)(ok ? slot : 0) * NVEL * L::nodes + (m & 0xff);
+                Quad<T> qv;
+                qv.x = ok ? src[0] : (T)0;
+                qv.y = ok ? src[L::nodes] : (T)0;
+                qv.z = ok ? src[2 * L::nodes] : (T)0;
+                qv.w = ok ? src[3 * L::nodes] : (T)0;
+                tq[node] = qv;
+            }
         {
             constexpr int MW = (int)(sizeof(Material<T>) / 4);
             const uint32_t* ms = reinterpret_cast<const uint32_t*>(sp.materials);
