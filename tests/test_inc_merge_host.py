@@ -41,6 +41,16 @@ def incremental_sort(knew, kold, T, mover_order_seed=0, maxm=None):
     boff = np.concatenate([[0], np.cumsum(bcnt)[:-1]]).astype(np.int64)
     out_k = np.full(n, -1, np.int64)
     out_i = np.full(n, -1, np.int64)
+    # the key before each tile's output (k_sort_scan1 / k_sort_scan2): the larger of the lower tiles' last stayer
+    # key and the lower buckets' largest mover key (None when nothing comes before)
+    preds, last_s, last_m = [], None, None
+    for j in range(tiles):
+        preds.append(None if last_s is None and last_m is None else max(v for v in (last_s, last_m) if v is not None))
+        sk_j = [int(knew[i]) for i in range(j * T, min(n, (j + 1) * T)) if stay[i]]
+        if sk_j:
+            last_s = sk_j[-1]
+        if bucket.get(j):
+            last_m = max(k for k, _ in bucket[j])
     for j in range(tiles):
         S = [(int(knew[i]), i) for i in range(j * T, min(n, (j + 1) * T)) if stay[i]]
         Mv = sorted(bucket.get(j, []))
@@ -56,6 +66,10 @@ def incremental_sort(knew, kold, T, mover_order_seed=0, maxm=None):
             p = base + r + bisect.bisect_right(sk, k)
             assert out_k[p] == -1
             out_k[p], out_i[p] = k, i
+    for j in range(tiles):  # the predecessor rule names the key the output actually holds before each tile
+        base = stay_off[j] + boff[j]
+        if base < n and (t_stay[j] or bcnt[j]):
+            assert preds[j] == (None if base == 0 else int(out_k[base - 1])), j
     return out_k, out_i
 
 

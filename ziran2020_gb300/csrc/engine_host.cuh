@@ -752,8 +752,9 @@ private:
 
     // tiles of the sort and of the group-head pass (SORT_TILE keys each) for up to cap particles
     static int64_t sort_tiles(int64_t n) { return std::max<int64_t>(1, (n + SORT_TILE - 1) / SORT_TILE); }
-    // sort_aux_: [stay bits: ceil(cap/32) u32][t_stay, t_first, b_cnt: tiles u32 each][look-back: tiles + 1 u64]
-    static size_t sort_aux_words(int64_t cap) { return (size_t)((cap + 31) / 32) + 3 * (size_t)sort_tiles(cap) + 1; }
+    // sort_aux_: [stay bits: ceil(cap/32) u32][t_stay, t_first, b_cnt, t_last, b_max, t_heads: tiles u32 each]
+    // [look-back: tiles + 1 u64]
+    static size_t sort_aux_words(int64_t cap) { return (size_t)((cap + 31) / 32) + 6 * (size_t)sort_tiles(cap) + 1; }
     static size_t sort_aux_bytes(int64_t cap) { return 4 * sort_aux_words(cap) + 8 * ((size_t)sort_tiles(cap) + 2); }
     uint64_t* lookback_words() const
     {
@@ -775,6 +776,9 @@ private:
         sb.t_stay = w + (cap_ + 31) / 32;
         sb.t_first = sb.t_stay + sort_tiles((int64_t)cap_);
         sb.b_cnt = sb.t_first + sort_tiles((int64_t)cap_);
+        sb.t_last = sb.b_cnt + sort_tiles((int64_t)cap_);
+        sb.b_max = sb.t_last + sort_tiles((int64_t)cap_);
+        sb.t_heads = sb.b_max + sort_tiles((int64_t)cap_);
         sb.m_idx = inc_move_;
         sb.m_bkt = inc_mkeys_;
         sb.m_tkt = inc_mvals_;
@@ -792,7 +796,10 @@ private:
         k_sort_bucket<<<mgrid, 256, 0, stream_>>>(nk, sb);
         k_sort_scan2<<<1, 1024, 0, stream_>>>(sb);
         k_sort_place<<<mgrid, 256, 0, stream_>>>(nk, sb, st_);
-        k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, st_);
+        k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, kl_, st_);
+        // group heads from the merge's per-tile counts: no look-back across tiles
+        k_sort_scan3<<<1, 1024, 0, stream_>>>(sb, st_);
+        k_heads_place<<<(unsigned)tiles, SORT_NT, 0, stream_>>>((const uint32_t*)keys_sorted_, sb, kl_, g_start_, (uint32_t)cap_, st_);
         return cudaGetLastError();
     }
 
@@ -1097,11 +1104,12 @@ private:
         StepArgs<T> a = args(parity);
         const int64_t n = N_;
         if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
-        if (full_sort || !inc_sort_usable())
+        if (full_sort || !inc_sort_usable()) {
             ZR_CUDA(sort_keys(n));
+            ZR_CUDA(group_heads(n));
+        }
         else
-            ZR_CUDA(sort_keys_incremental(n));
-        ZR_CUDA(group_heads(n));
+            ZR_CUDA(sort_keys_incremental(n)); // places the group heads itself
         if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
         k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
         k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);

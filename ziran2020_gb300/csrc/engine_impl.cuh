@@ -267,6 +267,9 @@ struct SortBufs {
     uint32_t* b_key; // [mcap] movers' keys grouped by bucket
     uint32_t* b_idx; // [mcap] movers' storage indices grouped by bucket
     uint32_t* stay_bits; // [ceil(n / 32)] bit i % 32 of word i / 32: storage index i keeps its key
+    uint32_t* t_last; // [tiles] last stayer key per tile, then (scan1) the largest stayer key of the lower tiles
+    uint32_t* b_max; // [tiles] largest mover key per bucket, then (scan2) the key before the tile's output
+    uint32_t* t_heads; // [tiles] group heads in the tile's output, then (scan3) their exclusive offsets
     int64_t* cnt; // [0] movers found, [1] unused
     int64_t mcap;
     int64_t n;
@@ -275,25 +278,30 @@ struct SortBufs {
 
 static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* knew, const uint32_t* kold, SortBufs sb, DevStatus* st)
 {
-    __shared__ uint32_t s_cnt[SORT_NT / 32], s_first[SORT_NT / 32], s_moff[SORT_NT / 32][SORT_PER];
+    __shared__ uint32_t s_cnt[SORT_NT / 32], s_first[SORT_NT / 32], s_last[SORT_NT / 32], s_moff[SORT_NT / 32][SORT_PER];
     __shared__ uint64_t s_base;
     const int j = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t t0 = (int64_t)j * SORT_TILE;
-    uint32_t nst = 0, first = SORT_NOKEY;
+    uint32_t nst = 0, first = SORT_NOKEY, last = SORT_NOKEY;
     unsigned moves = 0; // bit r: this thread's item of round r moved
-    // items in storage order; a warp takes 256 consecutive ones, 32 at a time
+    // items in storage order; a warp takes 256 consecutive ones, 32 at a time; every load issued first
+    uint32_t kn[SORT_PER], ko[SORT_PER];
+#pragma unroll
     for (int r = 0; r < SORT_PER; r++) {
         const int64_t i = t0 + (int64_t)w * (32 * SORT_PER) + r * 32 + lane;
-        bool stay = false, move = false;
-        uint32_t k = 0;
-        if (i < sb.n) {
-            k = knew[i];
-            stay = k == kold[i];
-            move = !stay;
-        }
+        kn[r] = i < sb.n ? knew[i] : 0u;
+        ko[r] = i < sb.n ? kold[i] : 1u;
+    }
+#pragma unroll
+    for (int r = 0; r < SORT_PER; r++) {
+        const int64_t i = t0 + (int64_t)w * (32 * SORT_PER) + r * 32 + lane;
+        const bool valid = i < sb.n, stay = valid && kn[r] == ko[r], move = valid && !stay;
         const unsigned bs = __ballot_sync(0xffffffffu, stay), bm = __ballot_sync(0xffffffffu, move);
-        if (lane == 0 && i < sb.n) sb.stay_bits[i >> 5] = bs; // the merge reads these: it overwrites the old keys
-        if (bs && first == SORT_NOKEY) first = __shfl_sync(0xffffffffu, k, __ffs(bs) - 1);
+        if (lane == 0 && valid) sb.stay_bits[i >> 5] = bs; // the merge reads these: it overwrites the old keys
+        if (bs) {
+            if (first == SORT_NOKEY) first = __shfl_sync(0xffffffffu, kn[r], __ffs(bs) - 1);
+            last = __shfl_sync(0xffffffffu, kn[r], 31 - __clz(bs));
+        }
         nst += __popc(bs);
         if (move) moves |= 1u << r;
         if (lane == 0) s_moff[w][r] = __popc(bm);
@@ -301,13 +309,15 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
     if (lane == 0) {
         s_cnt[w] = nst;
         s_first[w] = first;
+        s_last[w] = last;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t c = 0, f = SORT_NOKEY, m = 0;
+        uint32_t c = 0, f = SORT_NOKEY, l = SORT_NOKEY, m = 0;
         for (int q = 0; q < SORT_NT / 32; q++) {
             c += s_cnt[q];
             if (f == SORT_NOKEY) f = s_first[q];
+            if (s_last[q] != SORT_NOKEY) l = s_last[q];
             for (int r = 0; r < SORT_PER; r++) { // the tile's movers in storage order: warp-major, then round
                 const uint32_t v = s_moff[q][r];
                 s_moff[q][r] = m;
@@ -316,6 +326,7 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
         }
         sb.t_stay[j] = c;
         sb.t_first[j] = f;
+        sb.t_last[j] = l;
         s_base = m ? (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)m) : 0ull; // one atomic per tile
     }
     __syncthreads();
@@ -358,6 +369,26 @@ static __global__ void __launch_bounds__(1024) k_sort_scan1(SortBufs sb, DevStat
         sb.t_stay[q] = run;
         run += c;
         sb.b_cnt[q] = 0;
+        sb.b_max[q] = 0;
+    }
+    __syncthreads();
+    // the largest stayer key of the lower tiles (stayers ascend: the last one of the last tile that has any)
+    uint32_t lastk = SORT_NOKEY;
+    for (int q = lo; q < hi; q++)
+        if (sb.t_last[q] != SORT_NOKEY) lastk = sb.t_last[q];
+    s_part[tid] = lastk;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid >= o ? s_part[tid - o] : SORT_NOKEY;
+        __syncthreads();
+        if (s_part[tid] == SORT_NOKEY) s_part[tid] = v;
+        __syncthreads();
+    }
+    uint32_t before = tid ? s_part[tid - 1] : SORT_NOKEY;
+    for (int q = lo; q < hi; q++) {
+        const uint32_t l = sb.t_last[q];
+        sb.t_last[q] = before;
+        if (l != SORT_NOKEY) before = l;
     }
     __syncthreads();
     // suffix minimum of the first keys: per-thread block minima, scanned from the right
@@ -393,17 +424,23 @@ static __global__ void k_sort_bucket(const uint32_t* knew, SortBufs sb)
         const uint32_t b = lo > 0 ? (uint32_t)(lo - 1) : 0u;
         sb.m_bkt[m] = b;
         sb.m_tkt[m] = atomicAdd(&sb.b_cnt[b], 1u);
+        atomicMax(&sb.b_max[b], k);
     }
 }
 
-// one CTA: exclusive offsets of the buckets' movers
+// one CTA: exclusive offsets of the buckets' movers, and the key just before each tile's output: the larger of
+// the lower tiles' largest stayer key and the lower buckets' largest mover key (bucket key ranges ascend, so the
+// latter is the largest key of the last non-empty lower bucket); SORT_NOKEY when nothing comes before
 static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
 {
     __shared__ uint32_t s_part[1024];
     const int T = sb.tiles, tid = threadIdx.x;
     const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
-    uint32_t sum = 0;
-    for (int q = lo; q < hi; q++) sum += sb.b_cnt[q];
+    uint32_t sum = 0, lastm = SORT_NOKEY;
+    for (int q = lo; q < hi; q++) {
+        sum += sb.b_cnt[q];
+        if (sb.b_cnt[q]) lastm = sb.b_max[q];
+    }
     s_part[tid] = sum;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -413,10 +450,22 @@ static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
         __syncthreads();
     }
     uint32_t run = tid ? s_part[tid - 1] : 0u;
+    __syncthreads();
+    s_part[tid] = lastm;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid >= o ? s_part[tid - o] : SORT_NOKEY;
+        __syncthreads();
+        if (s_part[tid] == SORT_NOKEY) s_part[tid] = v;
+        __syncthreads();
+    }
+    uint32_t before = tid ? s_part[tid - 1] : SORT_NOKEY;
     for (int q = lo; q < hi; q++) {
-        const uint32_t c = sb.b_cnt[q];
+        const uint32_t c = sb.b_cnt[q], m = sb.b_max[q], ls = sb.t_last[q];
         sb.b_cnt[q] = run;
         run += c;
+        sb.b_max[q] = before == SORT_NOKEY ? ls : (ls == SORT_NOKEY ? before : max(before, ls));
+        if (c) before = m;
     }
 }
 
@@ -435,10 +484,13 @@ static __global__ void k_sort_place(const uint32_t* knew, SortBufs sb, DevStatus
     }
 }
 
-static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* knew, SortBufs sb, uint32_t* out_keys, uint32_t* out_vals, DevStatus* st)
+static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* knew, SortBufs sb, uint32_t* out_keys, uint32_t* out_vals, KeyLayout kl,
+    DevStatus* st)
 {
     __shared__ uint32_t s_key[SORT_TILE], s_idx[SORT_TILE]; // the tile's stayers in storage (= key) order
     __shared__ uint32_t m_key[SORT_MAXM], m_idx[SORT_MAXM], m_key2[SORT_MAXM], m_idx2[SORT_MAXM];
+    __shared__ uint32_t o_key[SORT_TILE + SORT_MAXM]; // the tile's output in order
+    __shared__ uint32_t s_heads;
     __shared__ uint32_t s_wcnt[SORT_PER][SORT_NT / 32];
     __shared__ int s_ns;
     const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -518,6 +570,7 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         }
         out_keys[pos] = k;
         out_vals[pos] = s_idx[t];
+        o_key[t + lo] = k;
     }
     for (int r = tid; r < nm; r += SORT_NT) { // mover: its rank + the tile's stayers with a key not above its own
         const uint32_t k = m_key2[r];
@@ -534,6 +587,83 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         }
         out_keys[pos] = k;
         out_vals[pos] = m_idx2[r];
+        o_key[r + lo] = k;
+    }
+    // group heads in the tile's output (the key before it is sb.b_max[j]): counted here, placed by k_heads_place
+    if (tid == 0) s_heads = 0;
+    __syncthreads();
+    const uint32_t pred = sb.b_max[j];
+    uint32_t h = 0;
+    for (int p = tid; p < ns + nm; p += SORT_NT) {
+        const uint32_t k = o_key[p];
+        const bool first = p == 0 ? pred == SORT_NOKEY : false;
+        const uint32_t kp = p == 0 ? pred : o_key[p - 1];
+        h += (first || kl.group(k) != kl.group(kp)) ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+    if (lane == 0 && h) atomicAdd(&s_heads, h);
+    __syncthreads();
+    if (tid == 0) sb.t_heads[j] = s_heads;
+}
+
+// one CTA: exclusive offsets of the tiles' group heads; their total is the number of groups
+static __global__ void __launch_bounds__(1024) k_sort_scan3(SortBufs sb, DevStatus* st)
+{
+    __shared__ uint32_t s_part[1024];
+    const int T = sb.tiles, tid = threadIdx.x;
+    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
+    uint32_t sum = 0;
+    for (int q = lo; q < hi; q++) sum += sb.t_heads[q];
+    s_part[tid] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
+        __syncthreads();
+        s_part[tid] += v;
+        __syncthreads();
+    }
+    uint32_t run = tid ? s_part[tid - 1] : 0u;
+    for (int q = lo; q < hi; q++) {
+        const uint32_t c = sb.t_heads[q];
+        sb.t_heads[q] = run;
+        run += c;
+    }
+    if (tid == 1023) st->n_groups = s_part[1023];
+}
+
+// the group heads of each tile's output (sorted positions [t_stay + b_cnt, next tile's), compared with the sorted
+// key before), written in order from the tile's offset
+static __global__ void __launch_bounds__(SORT_NT) k_heads_place(const uint32_t* keys, SortBufs sb, KeyLayout kl, uint32_t* g_start, uint32_t cap,
+    DevStatus* st)
+{
+    __shared__ uint32_t s_run;
+    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    __shared__ uint32_t s_w[SORT_NT / 32];
+    const int64_t M = min(sb.cnt[0], sb.mcap);
+    const int64_t b0 = (int64_t)sb.t_stay[j] + sb.b_cnt[j];
+    const int64_t b1 = j + 1 < sb.tiles ? (int64_t)sb.t_stay[j + 1] + sb.b_cnt[j + 1] : sb.n;
+    if (sb.cnt[0] > sb.mcap || b1 < b0 || b1 > sb.n) return; // FLAG_SORT raised: the substep is repeated with a full sort
+    if (tid == 0) s_run = sb.t_heads[j];
+    (void)M;
+    __syncthreads();
+    for (int64_t c0 = b0; c0 < b1; c0 += SORT_NT) {
+        const int64_t p = c0 + tid;
+        bool head = false;
+        if (p < b1) head = p == 0 || kl.group(keys[p]) != kl.group(keys[p - 1]);
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        if (lane == 0) s_w[w] = __popc(b);
+        __syncthreads();
+        uint32_t off = s_run;
+        for (int q = 0; q < w; q++) off += s_w[q];
+        if (head) {
+            const uint32_t pos = off + __popc(b & ((1u << lane) - 1u));
+            if (pos < cap) g_start[pos] = (uint32_t)p;
+            else check_failed(st, 9);
+        }
+        __syncthreads();
+        if (tid == 0)
+            for (int q = 0; q < SORT_NT / 32; q++) s_run += s_w[q];
+        __syncthreads();
     }
 }
 
