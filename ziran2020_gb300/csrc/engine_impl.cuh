@@ -992,6 +992,8 @@ struct alignas(4 * sizeof(T)) Quad {
     T x, y, z, w;
 };
 __device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) { return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y)); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
 template <class P, class T>
 __device__ __forceinline__ P pmake(T x, T y)
 {
@@ -1025,54 +1027,66 @@ struct NodeAcc {
 // Node (ii, jj, kk) receives, per momentum component r,
 //   wz_k al_r(j) + k wz_k be_r(j) + dwz_k ga_r(j)   with
 //   al = wx wy (A + j B1) + K0 dwx wy + K1 wx dwy,  be = wx wy B2,  ga = wx wy K2
+// Everything that does not depend on (jj, kk) is folded first, per particle and offset ii:
+//   U = wx (A + ii B0) + dwx K0,  V = wx B1,  Wk = wx K1,  X = wx B2,  Y = wx K2
+// so that al = wy_j U + j wy_j V + dwy_j Wk, be = wy_j X, ga = wy_j Y. All of it runs on pairs (two FP32 lanes
+// per instruction): (x, y) and (z, m), the mass lane carrying wx m through U and zeros elsewhere, and (d w, w).
 template <class T, int STRIDE, bool DAMAGE>
 __device__ __forceinline__ void accumulate_particle(NodeAcc<T>& acc, const T* y, int ii)
 {
     using P = typename NodeAcc<T>::P;
-    T w[3][3], dw[3][3];
+    T wy[3], dwy[3], wz[3], dwz[3];
+    T wx, dwx;
+    {
+        const T d0 = y[Y_F * STRIDE];
+        const T z = (T)1.5 - d0, d1 = d0 - (T)1, zz = d0 - (T)0.5;
+        wx = ii == 0 ? (T)0.5 * z * z : (ii == 1 ? (T)0.75 - d1 * d1 : (T)0.5 * zz * zz);
+        dwx = ii == 0 ? -z : (ii == 1 ? (T)-2 * d1 : zz);
+    }
 #pragma unroll
-    for (int e = 0; e < 3; e++) {
+    for (int e = 1; e < 3; e++) {
         const T d0 = y[(Y_F + e) * STRIDE];
         const T z = (T)1.5 - d0, d1 = d0 - (T)1, zz = d0 - (T)0.5;
-        w[e][0] = (T)0.5 * z * z;
-        w[e][1] = (T)0.75 - d1 * d1;
-        w[e][2] = (T)0.5 * zz * zz;
-        dw[e][0] = -z;
-        dw[e][1] = (T)-2 * d1;
-        dw[e][2] = zz;
+        T* w = e == 1 ? wy : wz;
+        T* dw = e == 1 ? dwy : dwz;
+        w[0] = (T)0.5 * z * z;
+        w[1] = (T)0.75 - d1 * d1;
+        w[2] = (T)0.5 * zz * zz;
+        dw[0] = -z;
+        dw[1] = (T)-2 * d1;
+        dw[2] = zz;
     }
-    const T wx = ii == 0 ? w[0][0] : (ii == 1 ? w[0][1] : w[0][2]);
-    const T dwx = ii == 0 ? dw[0][0] : (ii == 1 ? dw[0][1] : dw[0][2]);
     const T mass = y[Y_M * STRIDE];
     const T dd = DAMAGE ? y[Y_D * STRIDE] : (T)0;
-    T Ai[3], B1[3], B2[3], K0[3], K1[3], K2[3];
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-        Ai[r] = y[(Y_A + r) * STRIDE] + (T)ii * y[(Y_B + 3 * r) * STRIDE];
-        B1[r] = y[(Y_B + 3 * r + 1) * STRIDE];
-        B2[r] = y[(Y_B + 3 * r + 2) * STRIDE];
-        K0[r] = y[(Y_K + 3 * r) * STRIDE];
-        K1[r] = y[(Y_K + 3 * r + 1) * STRIDE];
-        K2[r] = y[(Y_K + 3 * r + 2) * STRIDE];
-    }
+    const T fi = (T)ii;
+    const P WX = pmake<P>(wx, wx), DWX = pmake<P>(dwx, dwx), FI = pmake<P>(fi, fi);
+    // pairs of payload fields: (x, y) and (z, mass lane)
+    auto pr = [&](int f0, int f1) { return pmake<P>(y[f0 * STRIDE], y[f1 * STRIDE]); };
+    auto pz = [&](int f0) { return pmake<P>(y[f0 * STRIDE], (T)0); };
+    const P A01 = pr(Y_A, Y_A + 1), A2 = pmake<P>(y[(Y_A + 2) * STRIDE], mass);
+    const P U01 = pfma(DWX, pr(Y_K, Y_K + 3), pmul(WX, pfma(FI, pr(Y_B, Y_B + 3), A01)));
+    const P U2 = pfma(DWX, pz(Y_K + 6), pmul(WX, pfma(FI, pz(Y_B + 6), A2)));
+    const P V01 = pmul(WX, pr(Y_B + 1, Y_B + 4)), V2 = pmul(WX, pz(Y_B + 7));
+    const P K01 = pmul(WX, pr(Y_K + 1, Y_K + 4)), K2 = pmul(WX, pz(Y_K + 7));
+    const P X01 = pmul(WX, pr(Y_B + 2, Y_B + 5)), X2 = pmul(WX, pz(Y_B + 8));
+    const P Y01 = pmul(WX, pr(Y_K + 2, Y_K + 5)), Y2 = pmul(WX, pz(Y_K + 8));
+    const P D = pmake<P>(wx * dd, wx);
 #pragma unroll
     for (int jj = 0; jj < 3; jj++) {
-        const T c0 = wx * w[1][jj], gx = dwx * w[1][jj], gy = wx * dw[1][jj];
-        T al[3], be[3], ga[3];
-#pragma unroll
-        for (int r = 0; r < 3; r++) {
-            al[r] = c0 * (jj ? Ai[r] + (T)jj * B1[r] : Ai[r]) + (K0[r] * gx + K1[r] * gy);
-            be[r] = c0 * B2[r];
-            ga[r] = c0 * K2[r];
+        const P WY = pmake<P>(wy[jj], wy[jj]), DWY = pmake<P>(dwy[jj], dwy[jj]);
+        P AL0 = pfma(DWY, K01, pmul(WY, U01)), AL1 = pfma(DWY, K2, pmul(WY, U2));
+        if (jj) {
+            const T jw = (T)jj * wy[jj];
+            const P JW = pmake<P>(jw, jw);
+            AL0 = pfma(JW, V01, AL0);
+            AL1 = pfma(JW, V2, AL1);
         }
-        // (p_x, p_y) and (p_z, m): the mass lane takes wz_k m c0 and zero for the other two terms
-        const P AL0 = pmake<P>(al[0], al[1]), AL1 = pmake<P>(al[2], mass * c0);
-        const P BE0 = pmake<P>(be[0], be[1]), BE1 = pmake<P>(be[2], (T)0);
-        const P GA0 = pmake<P>(ga[0], ga[1]), GA1 = pmake<P>(ga[2], (T)0);
-        const P DW = pmake<P>(dd * c0, c0);
+        const P BE0 = pmul(WY, X01), BE1 = pmul(WY, X2);
+        const P GA0 = pmul(WY, Y01), GA1 = pmul(WY, Y2);
+        const P DW = pmul(WY, D);
 #pragma unroll
         for (int kk = 0; kk < 3; kk++) {
-            const T wk = w[2][kk], dwk = dw[2][kk];
+            const T wk = wz[kk], dwk = dwz[kk];
             const P W = pmake<P>(wk, wk), DWK = pmake<P>(dwk, dwk);
             P* ac = acc.a[jj * 3 + kk];
             ac[0] = pfma(W, AL0, ac[0]);
