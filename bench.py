@@ -110,10 +110,13 @@ def allreduce_sum(world, v):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples while the GPU works (started before, stopped after)."""
+    """nvidia-smi clock / throttle samples while the GPU works (started before, stopped after). The SM clock reported
+    is the median over samples taken under load (GPU utilisation >= 50%); a timed region of a few milliseconds is
+    shorter than the 100 ms sampling period, so the window also covers the measurement passes that follow it."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+              "utilization.gpu")
 
     def __init__(self):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
@@ -139,17 +142,20 @@ class ClockSampler:
         with open(self.f.name) as fh:
             for line in fh:
                 parts = [t.strip() for t in line.split(",")]
-                if len(parts) == 9 and parts[0] == vis:
+                if len(parts) == 10 and parts[0] == vis:
                     rows.append(parts)
         os.unlink(self.f.name)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        num = lambda t: t.replace(".", "").isdigit()  # noqa: E731
+        loaded = [r for r in rows if num(r[9]) and float(r[9]) >= 50.0]
+        sm = [float(r[1]) for r in (loaded or rows) if num(r[1])]
+        mx = [float(r[2]) for r in rows if num(r[2])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows), "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+                "samples": len(rows), "samples_under_load": len(loaded),
+                "power_w_max": max((float(r[3]) for r in rows if num(r[3])), default=None)}
 
 
 def measured_peaks():
@@ -324,7 +330,6 @@ def measure_batch(recs, steps, warmup, world=1, fp64_steps=10):
     b.step(steps)
     ms = b.last_step_ms
     barrier(world)
-    clock_info = clocks.stop()
     stats = b.stats()
     b.set_timing(True)
     b.step(min(steps, 20))
@@ -349,6 +354,8 @@ def measure_batch(recs, steps, warmup, world=1, fp64_steps=10):
     b64.step(fp64_steps)
     fp64_value = n * fp64_steps / (b64.last_step_ms / 1e3)
     del b64
+    clock_info = clocks.stop()
+    clock_info["window"] = "warm-up, timed substeps, per-phase timing pass, FP64 path"
     return {"particles": int(n), "ms": ms, "stats": stats, "clocks": clock_info, "roofline": roof, "schedule": schedule, "fp64_value": fp64_value}
 
 
@@ -499,7 +506,6 @@ def run_ours(args, world, rank):
     s.step(args.steps)
     ms = s.last_step_ms
     barrier(world)
-    clock_info = clocks.stop()
     ms_max = allreduce_max(world, ms)
     n_total = allreduce_sum(world, n)
     value = n_total * args.steps / (ms_max / 1e3)
@@ -557,6 +563,8 @@ def run_ours(args, world, rank):
     s64.step(args.fp64_steps)
     fp64_value = n * args.fp64_steps / (s64.last_step_ms / 1e3)
     del s64
+    clock_info = clocks.stop()
+    clock_info["window"] = "warm-up, timed substeps, per-phase timing pass, end-to-end steps, FP64 path"
 
     # FP32 against the FP64 GPU path at the --accuracy-steps marks, and both GPU paths against the FP64 oracle
     # on the whole workload (the same inputs) after --oracle-slab-steps substeps; that oracle run, timed over

@@ -798,7 +798,6 @@ private:
         k_sort_place<<<mgrid, 256, 0, stream_>>>(nk, sb, st_);
         k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, kl_, st_);
         // group heads from the merge's per-tile counts: no look-back across tiles
-        k_sort_scan3<<<1, 1024, 0, stream_>>>(sb, st_);
         k_heads_place<<<(unsigned)tiles, SORT_NT, 0, stream_>>>((const uint32_t*)keys_sorted_, sb, kl_, g_start_, (uint32_t)cap_, st_);
         return cudaGetLastError();
     }

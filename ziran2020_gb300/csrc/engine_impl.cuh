@@ -244,12 +244,14 @@ struct GroupHead {
 // in the bucket plus the tile's stayers with a key not above its own. The order is fully determined by the keys
 // and storage indices (no dependence on the order in which movers were found).
 //
-//   k_sort_tiles    per tile: stayer count and first stayer key; movers appended to a list (overflow: FLAG_SORT)
-//   k_sort_scan1    one CTA: stayer offsets per tile, B, bucket counters cleared
-//   k_sort_bucket   per mover: bucket (binary search over B) and a ticket within it
-//   k_sort_scan2    one CTA: mover offsets per bucket
+//   k_sort_tiles    per tile: stayer count, first and last stayer key; movers appended to a list (one atomic per tile)
+//   k_sort_scan1    one CTA: stayer offsets per tile, B, the largest stayer key below each tile, bucket counters cleared
+//   k_sort_bucket   per mover: bucket (binary search over B), a ticket within it, the bucket's largest key
+//   k_sort_scan2    one CTA: mover offsets per bucket; the key just before each tile's output
 //   k_sort_place    per mover: (key, storage index) into its bucket
-//   k_sort_merge    per tile: the tile's stayers and its bucket's movers (sorted in shared memory) to their places
+//   k_sort_merge    per tile: the tile's stayers and its bucket's movers (sorted in shared memory) to their places;
+//                   the group heads in the tile's output counted
+//   k_heads_place   per tile: the group heads of its output written to g_start after the lower tiles' heads
 //
 // More movers than the list holds, or a bucket larger than SORT_MAXM, raises FLAG_SORT: the host repeats the
 // substep with a full radix sort (and grows the list).
@@ -269,7 +271,7 @@ struct SortBufs {
     uint32_t* stay_bits; // [ceil(n / 32)] bit i % 32 of word i / 32: storage index i keeps its key
     uint32_t* t_last; // [tiles] last stayer key per tile, then (scan1) the largest stayer key of the lower tiles
     uint32_t* b_max; // [tiles] largest mover key per bucket, then (scan2) the key before the tile's output
-    uint32_t* t_heads; // [tiles] group heads in the tile's output, then (scan3) their exclusive offsets
+    uint32_t* t_heads; // [tiles] group heads in the tile's output (the merge counts them)
     int64_t* cnt; // [0] movers found, [1] unused
     int64_t mcap;
     int64_t n;
@@ -312,22 +314,31 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
         s_last[w] = last;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t c = 0, f = SORT_NOKEY, l = SORT_NOKEY, m = 0;
-        for (int q = 0; q < SORT_NT / 32; q++) {
-            c += s_cnt[q];
-            if (f == SORT_NOKEY) f = s_first[q];
-            if (s_last[q] != SORT_NOKEY) l = s_last[q];
-            for (int r = 0; r < SORT_PER; r++) { // the tile's movers in storage order: warp-major, then round
-                const uint32_t v = s_moff[q][r];
-                s_moff[q][r] = m;
-                m += v;
-            }
+    if (w == 0) {
+        // the tile's movers in storage order (warp-major, then round): 64 counts, two per lane, one warp scan
+        static_assert(SORT_PER * (SORT_NT / 32) == 64, "two counts per lane");
+        uint32_t* mo = &s_moff[0][0];
+        const uint32_t a0 = mo[2 * lane], a1 = mo[2 * lane + 1];
+        uint32_t x = a0 + a1;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        sb.t_stay[j] = c;
-        sb.t_first[j] = f;
-        sb.t_last[j] = l;
-        s_base = m ? (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)m) : 0ull; // one atomic per tile
+        mo[2 * lane] = x - a0 - a1;
+        mo[2 * lane + 1] = x - a1;
+        const uint32_t m = __shfl_sync(0xffffffffu, x, 31);
+        if (lane == 0) {
+            uint32_t c = 0, f = SORT_NOKEY, l = SORT_NOKEY;
+            for (int q = 0; q < SORT_NT / 32; q++) {
+                c += s_cnt[q];
+                if (f == SORT_NOKEY) f = s_first[q];
+                if (s_last[q] != SORT_NOKEY) l = s_last[q];
+            }
+            sb.t_stay[j] = c;
+            sb.t_first[j] = f;
+            sb.t_last[j] = l;
+            s_base = m ? (uint64_t)atomicAdd((unsigned long long*)&sb.cnt[0], (unsigned long long)m) : 0ull; // one atomic per tile
+        }
     }
     __syncthreads();
     const uint64_t base = s_base;
@@ -342,67 +353,81 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
     (void)st;
 }
 
+// Scans of one CTA of 1024 threads (32 warps): shuffles inside each warp, then over the warp totals. op(a, b) combines
+// an earlier a with a later b; the result is the exclusive prefix of v in thread order, *total the combination of all.
+struct OpAdd {
+    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
+};
+struct OpMin {
+    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return min(a, b); }
+};
+struct OpLast { // the latest value that is not SORT_NOKEY
+    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return b != SORT_NOKEY ? b : a; }
+};
+template <class Op>
+__device__ uint32_t cta_scan1024(uint32_t v, Op op, uint32_t identity, uint32_t* total)
+{
+    __shared__ uint32_t s_w[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = op(y, x);
+    }
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = s_w[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t = op(y, t);
+        }
+        s_w[lane] = t;
+    }
+    __syncthreads();
+    uint32_t ex = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) ex = identity;
+    const uint32_t r = op(w ? s_w[w - 1] : identity, ex);
+    if (total) *total = s_w[31];
+    __syncthreads(); // s_w is reused by the next call
+    return r;
+}
+
 // one CTA: exclusive offsets of the tiles' stayers, B = suffix minimum of the first stayer keys (stayers ascend in
-// storage order, so this is the first stayer key at or after each tile), bucket counters cleared; too many movers
-// raise FLAG_SORT
+// storage order, so this is the first stayer key at or after each tile), the largest stayer key of the lower tiles,
+// bucket counters cleared; too many movers raise FLAG_SORT
 static __global__ void __launch_bounds__(1024) k_sort_scan1(SortBufs sb, DevStatus* st)
 {
-    __shared__ uint32_t s_part[1024];
+    __shared__ uint32_t s_x[1024];
     const int T = sb.tiles, tid = threadIdx.x;
     const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
     const int64_t M = sb.cnt[0];
     if (tid == 0) atomicMax(&st->max_movers, (uint32_t)(M < 0xffffffffLL ? M : 0xffffffffLL));
     if (tid == 0 && M > sb.mcap) raise_flag(st, FLAG_SORT);
-    uint32_t sum = 0;
-    for (int q = lo; q < hi; q++) sum += sb.t_stay[q];
-    s_part[tid] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) { // inclusive scan of the per-thread sums
-        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
-        __syncthreads();
-        s_part[tid] += v;
-        __syncthreads();
-    }
-    uint32_t run = tid ? s_part[tid - 1] : 0u;
+    uint32_t sum = 0, lastk = SORT_NOKEY, mn = SORT_NOKEY;
     for (int q = lo; q < hi; q++) {
-        const uint32_t c = sb.t_stay[q];
+        sum += sb.t_stay[q];
+        if (sb.t_last[q] != SORT_NOKEY) lastk = sb.t_last[q];
+        mn = min(mn, sb.t_first[q]);
+    }
+    uint32_t run = cta_scan1024(sum, OpAdd{}, 0u, nullptr);
+    uint32_t before = cta_scan1024(lastk, OpLast{}, SORT_NOKEY, nullptr);
+    // suffix minimum: scan the block minima in reverse thread order
+    s_x[tid] = mn;
+    __syncthreads();
+    const uint32_t rev = cta_scan1024(s_x[1023 - tid], OpMin{}, SORT_NOKEY, nullptr); // minimum over the blocks after block 1023 - tid
+    s_x[1023 - tid] = rev;
+    __syncthreads();
+    uint32_t suf = s_x[tid];
+    for (int q = lo; q < hi; q++) {
+        const uint32_t c = sb.t_stay[q], l = sb.t_last[q];
         sb.t_stay[q] = run;
         run += c;
+        sb.t_last[q] = before;
+        if (l != SORT_NOKEY) before = l;
         sb.b_cnt[q] = 0;
         sb.b_max[q] = 0;
     }
-    __syncthreads();
-    // the largest stayer key of the lower tiles (stayers ascend: the last one of the last tile that has any)
-    uint32_t lastk = SORT_NOKEY;
-    for (int q = lo; q < hi; q++)
-        if (sb.t_last[q] != SORT_NOKEY) lastk = sb.t_last[q];
-    s_part[tid] = lastk;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = tid >= o ? s_part[tid - o] : SORT_NOKEY;
-        __syncthreads();
-        if (s_part[tid] == SORT_NOKEY) s_part[tid] = v;
-        __syncthreads();
-    }
-    uint32_t before = tid ? s_part[tid - 1] : SORT_NOKEY;
-    for (int q = lo; q < hi; q++) {
-        const uint32_t l = sb.t_last[q];
-        sb.t_last[q] = before;
-        if (l != SORT_NOKEY) before = l;
-    }
-    __syncthreads();
-    // suffix minimum of the first keys: per-thread block minima, scanned from the right
-    uint32_t mn = SORT_NOKEY;
-    for (int q = lo; q < hi; q++) mn = min(mn, sb.t_first[q]);
-    s_part[tid] = mn;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = tid + o < 1024 ? s_part[tid + o] : SORT_NOKEY;
-        __syncthreads();
-        s_part[tid] = min(s_part[tid], v);
-        __syncthreads();
-    }
-    uint32_t suf = tid + 1 < 1024 ? s_part[tid + 1] : SORT_NOKEY;
     for (int q = hi - 1; q >= lo; q--) {
         suf = min(suf, sb.t_first[q]);
         sb.t_first[q] = suf;
@@ -433,7 +458,6 @@ static __global__ void k_sort_bucket(const uint32_t* knew, SortBufs sb)
 // latter is the largest key of the last non-empty lower bucket); SORT_NOKEY when nothing comes before
 static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
 {
-    __shared__ uint32_t s_part[1024];
     const int T = sb.tiles, tid = threadIdx.x;
     const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
     uint32_t sum = 0, lastm = SORT_NOKEY;
@@ -441,25 +465,8 @@ static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
         sum += sb.b_cnt[q];
         if (sb.b_cnt[q]) lastm = sb.b_max[q];
     }
-    s_part[tid] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
-        __syncthreads();
-        s_part[tid] += v;
-        __syncthreads();
-    }
-    uint32_t run = tid ? s_part[tid - 1] : 0u;
-    __syncthreads();
-    s_part[tid] = lastm;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = tid >= o ? s_part[tid - o] : SORT_NOKEY;
-        __syncthreads();
-        if (s_part[tid] == SORT_NOKEY) s_part[tid] = v;
-        __syncthreads();
-    }
-    uint32_t before = tid ? s_part[tid - 1] : SORT_NOKEY;
+    uint32_t run = cta_scan1024(sum, OpAdd{}, 0u, nullptr);
+    uint32_t before = cta_scan1024(lastm, OpLast{}, SORT_NOKEY, nullptr);
     for (int q = lo; q < hi; q++) {
         const uint32_t c = sb.b_cnt[q], m = sb.b_max[q], ls = sb.t_last[q];
         sb.b_cnt[q] = run;
@@ -524,15 +531,19 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         m_idx[q] = sb.b_idx[bo + q];
     }
     __syncthreads();
-    if (tid == 0) { // exclusive offsets of the (round, warp) groups, in storage order
-        uint32_t run = 0;
-        for (int r = 0; r < SORT_PER; r++)
-            for (int q = 0; q < SORT_NT / 32; q++) {
-                const uint32_t c = s_wcnt[r][q];
-                s_wcnt[r][q] = run;
-                run += c;
-            }
-        s_ns = (int)run;
+    if (w == 0) { // exclusive offsets of the 64 (round, warp) groups in storage order: two per lane, one warp scan
+        static_assert(SORT_PER * (SORT_NT / 32) == 64, "two groups per lane");
+        uint32_t* c = &s_wcnt[0][0];
+        const uint32_t a0 = c[2 * lane], a1 = c[2 * lane + 1];
+        uint32_t x = a0 + a1;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t ex = x - a0 - a1;
+        c[2 * lane] = ex;
+        c[2 * lane + 1] = ex + a0;
+        if (lane == 31) s_ns = (int)x;
     }
     __syncthreads();
 #pragma unroll
@@ -606,64 +617,76 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
     if (tid == 0) sb.t_heads[j] = s_heads;
 }
 
-// one CTA: exclusive offsets of the tiles' group heads; their total is the number of groups
-static __global__ void __launch_bounds__(1024) k_sort_scan3(SortBufs sb, DevStatus* st)
-{
-    __shared__ uint32_t s_part[1024];
-    const int T = sb.tiles, tid = threadIdx.x;
-    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
-    uint32_t sum = 0;
-    for (int q = lo; q < hi; q++) sum += sb.t_heads[q];
-    s_part[tid] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = tid >= o ? s_part[tid - o] : 0u;
-        __syncthreads();
-        s_part[tid] += v;
-        __syncthreads();
-    }
-    uint32_t run = tid ? s_part[tid - 1] : 0u;
-    for (int q = lo; q < hi; q++) {
-        const uint32_t c = sb.t_heads[q];
-        sb.t_heads[q] = run;
-        run += c;
-    }
-    if (tid == 1023) st->n_groups = s_part[1023];
-}
-
-// the group heads of each tile's output (sorted positions [t_stay + b_cnt, next tile's), compared with the sorted
-// key before), written in order from the tile's offset
+// The group heads of each tile's output (sorted positions [t_stay + b_cnt of the tile, of the next tile), compared
+// with the sorted key before), written in order from the tile's offset: the heads of the lower tiles, summed by the
+// CTA itself from the merge's counts. The last tile stores the number of groups.
 static __global__ void __launch_bounds__(SORT_NT) k_heads_place(const uint32_t* keys, SortBufs sb, KeyLayout kl, uint32_t* g_start, uint32_t cap,
     DevStatus* st)
 {
-    __shared__ uint32_t s_run;
+    constexpr int RMAX = (SORT_TILE + SORT_MAXM) / SORT_NT;
+    __shared__ uint32_t s_c[RMAX][SORT_NT / 32], s_part[SORT_NT / 32];
     const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    __shared__ uint32_t s_w[SORT_NT / 32];
-    const int64_t M = min(sb.cnt[0], sb.mcap);
+    if (sb.cnt[0] > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
     const int64_t b0 = (int64_t)sb.t_stay[j] + sb.b_cnt[j];
     const int64_t b1 = j + 1 < sb.tiles ? (int64_t)sb.t_stay[j + 1] + sb.b_cnt[j + 1] : sb.n;
-    if (sb.cnt[0] > sb.mcap || b1 < b0 || b1 > sb.n) return; // FLAG_SORT raised: the substep is repeated with a full sort
-    if (tid == 0) s_run = sb.t_heads[j];
-    (void)M;
-    __syncthreads();
-    for (int64_t c0 = b0; c0 < b1; c0 += SORT_NT) {
-        const int64_t p = c0 + tid;
-        bool head = false;
-        if (p < b1) head = p == 0 || kl.group(keys[p]) != kl.group(keys[p - 1]);
+    if (b1 < b0 || b1 > sb.n) {
+        if (tid == 0) check_failed(st, 9);
+        return;
+    }
+    if (b1 - b0 > (int64_t)RMAX * SORT_NT) return; // a bucket beyond the merge's capacity: the merge raised FLAG_SORT
+    // heads of the lower tiles
+    uint32_t pre = 0;
+    for (int q = tid; q < j; q += SORT_NT) pre += sb.t_heads[q];
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_down_sync(0xffffffffu, pre, o);
+    if (lane == 0) s_part[w] = pre;
+    // the range's keys and head flags, items (r, w, lane) = b0 + r*256 + w*32 + lane, every load issued first
+    const int R = (int)((b1 - b0 + SORT_NT - 1) / SORT_NT);
+    uint32_t k[RMAX], kl0[RMAX]; // the item's key; for lane 0 also the key before it (another warp's item)
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        const int64_t p = b0 + r * SORT_NT + tid;
+        const bool in = r < R && p < b1;
+        k[r] = in ? keys[p] : 0u;
+        kl0[r] = (in && lane == 0 && p > 0) ? keys[p - 1] : 0u;
+    }
+    unsigned mine = 0;
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        if (r >= R) break;
+        const int64_t p = b0 + r * SORT_NT + tid;
+        uint32_t prev = __shfl_up_sync(0xffffffffu, k[r], 1);
+        if (lane == 0) prev = kl0[r];
+        const bool head = p < b1 && (p == 0 || kl.group(k[r]) != kl.group(prev));
         const unsigned b = __ballot_sync(0xffffffffu, head);
-        if (lane == 0) s_w[w] = __popc(b);
-        __syncthreads();
-        uint32_t off = s_run;
-        for (int q = 0; q < w; q++) off += s_w[q];
-        if (head) {
-            const uint32_t pos = off + __popc(b & ((1u << lane) - 1u));
-            if (pos < cap) g_start[pos] = (uint32_t)p;
+        if (head) mine |= 1u << r;
+        if (lane == 0) s_c[r][w] = __popc(b);
+    }
+    __syncthreads();
+    if (w == 0) { // exclusive offsets of the (row, warp) counts in order, after the lower tiles' heads
+        uint32_t base = 0;
+        for (int q = 0; q < SORT_NT / 32; q++) base += s_part[q];
+        uint32_t carry = base;
+        for (int r = 0; r < R; r++) {
+            uint32_t c = lane < SORT_NT / 32 ? s_c[r][lane] : 0u, x = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane < SORT_NT / 32) s_c[r][lane] = carry + x - c;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (lane == 0 && j + 1 == sb.tiles) st->n_groups = carry;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        if (r >= R) break;
+        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
+        if ((mine >> r) & 1u) {
+            const uint32_t pos = s_c[r][w] + __popc(b & ((1u << lane) - 1u));
+            if (pos < cap) g_start[pos] = (uint32_t)(b0 + r * SORT_NT + tid);
             else check_failed(st, 9);
         }
-        __syncthreads();
-        if (tid == 0)
-            for (int q = 0; q < SORT_NT / 32; q++) s_run += s_w[q];
-        __syncthreads();
     }
 }
 
