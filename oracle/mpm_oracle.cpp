@@ -1925,6 +1925,40 @@ void orc_collide(int precision, int n_obj, const double* objs, double time, cons
         run(0.0);
 }
 
+// The damage drive D~ = zeta <phi - 1> of one particle (AnisoFractureSimulation.h:224-270) with a damaged model
+// (1 Neo-Hookean Borden, 2 QR-stable with fibre stiffness kx_scale mu), for unit tests and fixtures.
+double orc_damage_drive(int precision, int model, double E, double nu, double kx_scale, double alpha, double zeta, double sigma_c, const double* F)
+{
+    double out = 0;
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        Scene<T> sc;
+        Material<T> mt{};
+        mt.model = model;
+        T Et = (T)E, nut = (T)nu;
+        mt.lambda = Et * nut / (((T)1 + nut) * ((T)1 - (T)2 * nut));
+        mt.mu = Et / ((T)2 * ((T)1 + nut));
+        mt.kappa = (T).666666 * mt.mu + mt.lambda;
+        mt.kx = (T)kx_scale * mt.mu;
+        mt.damage = 1;
+        mt.alpha = (T)alpha;
+        mt.zeta = (T)zeta;
+        sc.materials.push_back(mt);
+        M3<T> f;
+        for (int i = 0; i < 9; i++) f.a[i] = (T)F[i];
+        sc.F.push_back(f);
+        sc.sigc.push_back((T)sigma_c);
+        sc.mat.push_back(0);
+        sc.n = 1;
+        out = (double)sc.dtilde_of(0);
+    };
+    if (precision == 4)
+        run(0.0f);
+    else
+        run(0.0);
+    return out;
+}
+
 int orc_num_threads()
 {
 #ifdef _OPENMP

@@ -136,4 +136,23 @@ void shim_collide(int prec, int n_obj, const double* objs, double time, const do
     else
         run(0.0);
 }
+
+// the damage drive D~ = zeta <phi - 1> of one particle (damage_drive) for model 1 (Borden) or 2 (QR-stable, fibre
+// stiffness kx = kx_scale mu)
+double shim_drive(int prec, int model, double E, double nu, double kx_scale, double alpha, double zeta, double sigma_c, const double* F)
+{
+    auto run = [&](auto zero) -> double {
+        using T = decltype(zero);
+        Material<T> m = mat<T>(model, E, nu);
+        m.kx = (T)kx_scale * m.mu;
+        m.damage = 1;
+        m.alpha = (T)alpha;
+        m.zeta = (T)zeta;
+        T f[9];
+        for (int i = 0; i < 9; i++) f[i] = (T)F[i];
+        bool fb = false;
+        return (double)damage_drive(m, f, (T)sigma_c, fb);
+    };
+    return prec == 4 ? run(0.0f) : run(0.0);
+}
 }
