@@ -365,3 +365,14 @@ def test_collide_parallel_normals_add_nothing_to_the_basis(shim):
     objs = _objects(rows)
     g = _collide(shim.shim_collide, 8, objs, 0.0, x, v)
     assert np.allclose(g, (0.3, 0.0, 0.0))  # two basis vectors only: the moving STICKY plane applies
+
+
+def test_fully_damaged_particle_stays_at_one(shim):
+    """d = 1: the update d + dt/eta <(1 - d) D~ - (d - l0^2 lap)> is at least 1 and capped at 1 (AnisoFractureSimulation.h:
+    276-281), so the drive is not evaluated; the result equals the formula's for any F and Laplacian."""
+    rng = np.random.default_rng(11)
+    E, nu, alpha, l0, eta, zeta, k = 5e4, 0.25, -1.0, 0.002, 0.1, 1.0, 0.01
+    for _ in range(50):
+        F = np.ascontiguousarray(np.eye(3) + 0.3 * rng.normal(size=(3, 3)))
+        lap = rng.normal() * 1e6
+        assert shim.shim_damage(E, nu, alpha, l0, eta, zeta, k, p(F), 1.0, lap, 10.0, 5e-5) == 1.0

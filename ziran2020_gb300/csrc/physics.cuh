@@ -625,6 +625,11 @@ ZR_HD T damage_drive(const Material<T>& mt, const T* F, T sigma_c, bool& fallbac
 template <class T>
 ZR_HD T damage_update(const Material<T>& mt, const T* F, T d, T lap, T sigma_c, T dt, bool& fallback)
 {
+    // fully damaged: d + (dt/eta) <...> >= d >= 1 and the update is capped at 1, whatever the drive is
+    if (d >= (T)1) {
+        fallback = false;
+        return (T)1;
+    }
     T geo = d - mt.l0 * mt.l0 * lap;
     T dtilde = damage_drive(mt, F, sigma_c, fallback);
     T diff = ((T)1 - d) * dtilde - geo;
