@@ -658,6 +658,7 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         out_vals[pos] = m_idx2[r];
         o_key[r + lo] = k;
     }
+    __syncthreads(); // every element of the tile's output is in o_key
     // group heads in the tile's output (the key before it is sb.b_max[j]): items (r, w, lane) = r*256 + w*32 + lane
     const uint32_t pred = sb.b_max[j];
     const int L = ns + nm, R = (L + SORT_NT - 1) / SORT_NT;
