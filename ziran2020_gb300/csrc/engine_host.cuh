@@ -796,13 +796,9 @@ private:
         k_sort_bucket<<<mgrid, 256, 0, stream_>>>(nk, sb);
         k_sort_scan2<<<1, 1024, 0, stream_>>>(sb);
         k_sort_place<<<mgrid, 256, 0, stream_>>>(nk, sb, st_);
-        // the merge also places the group heads (decoupled look-back over the tiles: status words and tile counter
-        // cleared first)
-        uint64_t* lb = lookback_words();
-        e = cudaMemsetAsync(lb, 0, 8 * ((size_t)tiles + 1), stream_);
-        if (e != cudaSuccess) return e;
-        k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, kl_, lb,
-            reinterpret_cast<uint32_t*>(lb + tiles), g_start_, (uint32_t)cap_, st_);
+        k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, kl_, st_);
+        // group heads from the merge's per-tile counts: no look-back across tiles
+        k_heads_place<<<(unsigned)tiles, SORT_NT, 0, stream_>>>((const uint32_t*)keys_sorted_, sb, kl_, g_start_, (uint32_t)cap_, st_);
         return cudaGetLastError();
     }
 

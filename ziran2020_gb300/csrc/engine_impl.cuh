@@ -250,15 +250,13 @@ struct GroupHead {
 //   k_sort_scan2    one CTA: mover offsets per bucket; the key just before each tile's output
 //   k_sort_place    per mover: (key, storage index) into its bucket
 //   k_sort_merge    per tile: the tile's stayers and its bucket's movers (sorted in shared memory) to their places;
-//                   the group heads of the tile's output written to g_start after the lower tiles' heads, found by a
-//                   decoupled look-back
+//                   the group heads in the tile's output counted
+//   k_heads_place   per tile: the group heads of its output written to g_start after the lower tiles' heads
 //
 // More movers than the list holds, or a bucket larger than SORT_MAXM, raises FLAG_SORT: the host repeats the
 // substep with a full radix sort (and grows the list).
 // ---------------------------------------------------------------------------------------------------
 constexpr int SORT_NT = 256, SORT_PER = 8, SORT_TILE = SORT_NT * SORT_PER, SORT_MAXM = 1024;
-// decoupled look-back status words: a flag in the top two bits, a count below
-constexpr uint64_t LB_AGG = 1ull << 62, LB_PREFIX = 2ull << 62, LB_VALUE = (1ull << 62) - 1;
 constexpr uint32_t SORT_NOKEY = 0xffffffffu; // keys of the incremental sort hold at most 31 bits
 
 struct SortBufs {
@@ -493,77 +491,21 @@ static __global__ void k_sort_place(const uint32_t* knew, SortBufs sb, DevStatus
     }
 }
 
-// Group heads in the same kernel: the tile's head count is published for the tiles after it, its offset found by a
-// decoupled look-back (tiles taken in order from a counter, so a tile's predecessors have started and publish
-// without waiting on it; a warp reads 32 predecessors per step; waits bounded, FLAG_TIMEOUT after ~0.3 s).
-constexpr int MERGE_RMAX = (SORT_TILE + SORT_MAXM) / SORT_NT;
-
-static __device__ void lookback_publish(uint64_t* status, int j, uint64_t flag_value)
-{
-    __threadfence();
-    volatile uint64_t* vs = status;
-    vs[j] = flag_value;
-}
-
-// the sum of the head counts of tiles < j (warp 0 calls it; every lane returns it)
-static __device__ uint64_t lookback_prefix(const uint64_t* status, int j, DevStatus* st)
-{
-    const int lane = threadIdx.x & 31;
-    volatile const uint64_t* vs = status;
-    uint64_t prefix = 0;
-    int q = j - 1;
-    uint32_t spins = 0;
-    while (q >= 0) {
-        const int idx = q - lane;
-        uint64_t v = LB_PREFIX + 0; // before tile 0: a prefix of zero
-        if (idx >= 0) v = vs[idx];
-        bool timed_out = false;
-        while (__any_sync(0xffffffffu, (v & (LB_AGG | LB_PREFIX)) == 0)) {
-            if (++spins > (1u << 22)) { // a predecessor never published: give up (the substep is aborted)
-                timed_out = true;
-                break;
-            }
-            __nanosleep(64);
-            if ((v & (LB_AGG | LB_PREFIX)) == 0) v = vs[idx];
-        }
-        if (timed_out) {
-            if (lane == 0) raise_flag(st, FLAG_TIMEOUT);
-            break;
-        }
-        const unsigned pm = __ballot_sync(0xffffffffu, (v & LB_PREFIX) != 0);
-        const int stop = pm ? __ffs(pm) - 1 : 31; // lanes 0..stop count (lane 0 is the nearest predecessor)
-        uint64_t c = lane <= stop ? (v & LB_VALUE) : 0ull;
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-        prefix += __shfl_sync(0xffffffffu, c, 0);
-        if (pm) break;
-        q -= 32;
-    }
-    return prefix;
-}
-
 static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* knew, SortBufs sb, uint32_t* out_keys, uint32_t* out_vals, KeyLayout kl,
-    uint64_t* lb_status, uint32_t* lb_counter, uint32_t* g_start, uint32_t cap, DevStatus* st)
+    DevStatus* st)
 {
     __shared__ uint32_t s_key[SORT_TILE], s_idx[SORT_TILE]; // the tile's stayers in storage (= key) order
     __shared__ uint32_t m_key[SORT_MAXM], m_idx[SORT_MAXM], m_key2[SORT_MAXM], m_idx2[SORT_MAXM];
     __shared__ uint32_t o_key[SORT_TILE + SORT_MAXM]; // the tile's output in order
-    __shared__ uint32_t s_hc[MERGE_RMAX][SORT_NT / 32];
-    __shared__ uint64_t s_prefix;
+    __shared__ uint32_t s_heads;
     __shared__ uint32_t s_wcnt[SORT_PER][SORT_NT / 32];
-    __shared__ int s_ns, s_tile;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) s_tile = (int)atomicAdd(lb_counter, 1u);
-    __syncthreads();
-    const int j = s_tile;
+    __shared__ int s_ns;
+    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t M = sb.cnt[0];
-    const uint32_t bo = M > sb.mcap ? 0u : sb.b_cnt[j], be = M > sb.mcap ? 0u : (j + 1 < sb.tiles ? sb.b_cnt[j + 1] : (uint32_t)M);
-    if (M > sb.mcap || be < bo || be - bo > (uint32_t)SORT_MAXM) {
-        // FLAG_SORT (raised by k_sort_scan1, or here for a bucket beyond the shared memory): the substep is repeated
-        // with a full sort; the tile still publishes, so that no later tile waits for it
-        if (tid == 0) {
-            if (M <= sb.mcap) raise_flag(st, FLAG_SORT);
-            lookback_publish(lb_status, j, (j == 0 ? LB_PREFIX : LB_AGG) | 0ull);
-        }
+    if (M > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
+    const uint32_t bo = sb.b_cnt[j], be = j + 1 < sb.tiles ? sb.b_cnt[j + 1] : (uint32_t)M;
+    if (be < bo || be - bo > (uint32_t)SORT_MAXM) {
+        if (tid == 0) raise_flag(st, FLAG_SORT);
         return;
     }
     const int nm = (int)(be - bo);
@@ -658,55 +600,91 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         out_vals[pos] = m_idx2[r];
         o_key[r + lo] = k;
     }
-    __syncthreads(); // every element of the tile's output is in o_key
-    // group heads in the tile's output (the key before it is sb.b_max[j]): items (r, w, lane) = r*256 + w*32 + lane
+    // group heads in the tile's output (the key before it is sb.b_max[j]): counted here, placed by k_heads_place
+    if (tid == 0) s_heads = 0;
+    __syncthreads();
     const uint32_t pred = sb.b_max[j];
-    const int L = ns + nm, R = (L + SORT_NT - 1) / SORT_NT;
-    unsigned heads = 0;
+    uint32_t h = 0;
+    for (int p = tid; p < ns + nm; p += SORT_NT) {
+        const uint32_t k = o_key[p];
+        const bool first = p == 0 ? pred == SORT_NOKEY : false;
+        const uint32_t kp = p == 0 ? pred : o_key[p - 1];
+        h += (first || kl.group(k) != kl.group(kp)) ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+    if (lane == 0 && h) atomicAdd(&s_heads, h);
+    __syncthreads();
+    if (tid == 0) sb.t_heads[j] = s_heads;
+}
+
+// The group heads of each tile's output (sorted positions [t_stay + b_cnt of the tile, of the next tile), compared
+// with the sorted key before), written in order from the tile's offset: the heads of the lower tiles, summed by the
+// CTA itself from the merge's counts. The last tile stores the number of groups.
+static __global__ void __launch_bounds__(SORT_NT) k_heads_place(const uint32_t* keys, SortBufs sb, KeyLayout kl, uint32_t* g_start, uint32_t cap,
+    DevStatus* st)
+{
+    constexpr int RMAX = (SORT_TILE + SORT_MAXM) / SORT_NT;
+    __shared__ uint32_t s_c[RMAX][SORT_NT / 32], s_part[SORT_NT / 32];
+    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (sb.cnt[0] > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
+    const int64_t b0 = (int64_t)sb.t_stay[j] + sb.b_cnt[j];
+    const int64_t b1 = j + 1 < sb.tiles ? (int64_t)sb.t_stay[j + 1] + sb.b_cnt[j + 1] : sb.n;
+    if (b1 < b0 || b1 > sb.n) {
+        if (tid == 0) check_failed(st, 9);
+        return;
+    }
+    if (b1 - b0 > (int64_t)RMAX * SORT_NT) return; // a bucket beyond the merge's capacity: the merge raised FLAG_SORT
+    // heads of the lower tiles
+    uint32_t pre = 0;
+    for (int q = tid; q < j; q += SORT_NT) pre += sb.t_heads[q];
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_down_sync(0xffffffffu, pre, o);
+    if (lane == 0) s_part[w] = pre;
+    // the range's keys and head flags, items (r, w, lane) = b0 + r*256 + w*32 + lane, every load issued first
+    const int R = (int)((b1 - b0 + SORT_NT - 1) / SORT_NT);
+    uint32_t k[RMAX], kl0[RMAX]; // the item's key; for lane 0 also the key before it (another warp's item)
 #pragma unroll
-    for (int r = 0; r < MERGE_RMAX; r++) {
+    for (int r = 0; r < RMAX; r++) {
+        const int64_t p = b0 + r * SORT_NT + tid;
+        const bool in = r < R && p < b1;
+        k[r] = in ? keys[p] : 0u;
+        kl0[r] = (in && lane == 0 && p > 0) ? keys[p - 1] : 0u;
+    }
+    unsigned mine = 0;
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
         if (r >= R) break;
-        const int p = r * SORT_NT + tid;
-        bool h = false;
-        if (p < L) {
-            const uint32_t k = o_key[p];
-            h = p == 0 ? (pred == SORT_NOKEY || kl.group(k) != kl.group(pred)) : kl.group(k) != kl.group(o_key[p - 1]);
-        }
-        const unsigned b = __ballot_sync(0xffffffffu, h);
-        if (h) heads |= 1u << r;
-        if (lane == 0) s_hc[r][w] = __popc(b);
+        const int64_t p = b0 + r * SORT_NT + tid;
+        uint32_t prev = __shfl_up_sync(0xffffffffu, k[r], 1);
+        if (lane == 0) prev = kl0[r];
+        const bool head = p < b1 && (p == 0 || kl.group(k[r]) != kl.group(prev));
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        if (head) mine |= 1u << r;
+        if (lane == 0) s_c[r][w] = __popc(b);
     }
     __syncthreads();
-    if (w == 0) {
-        // local offsets of the (row, warp) counts in order, the tile's total published, then its prefix looked up
-        uint32_t carry = 0;
+    if (w == 0) { // exclusive offsets of the (row, warp) counts in order, after the lower tiles' heads
+        uint32_t base = 0;
+        for (int q = 0; q < SORT_NT / 32; q++) base += s_part[q];
+        uint32_t carry = base;
         for (int r = 0; r < R; r++) {
-            const uint32_t c = lane < SORT_NT / 32 ? s_hc[r][lane] : 0u;
-            uint32_t x = c;
+            uint32_t c = lane < SORT_NT / 32 ? s_c[r][lane] : 0u, x = c;
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
-            if (lane < SORT_NT / 32) s_hc[r][lane] = carry + x - c;
+            if (lane < SORT_NT / 32) s_c[r][lane] = carry + x - c;
             carry += __shfl_sync(0xffffffffu, x, 31);
         }
-        if (lane == 0) lookback_publish(lb_status, j, (j == 0 ? LB_PREFIX : LB_AGG) | carry);
-        const uint64_t prefix = j == 0 ? 0ull : lookback_prefix(lb_status, j, st);
-        if (lane == 0) {
-            if (j > 0) lookback_publish(lb_status, j, LB_PREFIX | (prefix + carry));
-            s_prefix = prefix;
-            if (j + 1 == sb.tiles) st->n_groups = (uint32_t)(prefix + carry);
-        }
+        if (lane == 0 && j + 1 == sb.tiles) st->n_groups = carry;
     }
     __syncthreads();
-    const uint64_t prefix = s_prefix;
 #pragma unroll
-    for (int r = 0; r < MERGE_RMAX; r++) {
+    for (int r = 0; r < RMAX; r++) {
         if (r >= R) break;
-        const unsigned b = __ballot_sync(0xffffffffu, (heads >> r) & 1u);
-        if ((heads >> r) & 1u) {
-            const uint64_t pos = prefix + s_hc[r][w] + __popc(b & ((1u << lane) - 1u));
-            if (pos < cap) g_start[pos] = (uint32_t)(base + r * SORT_NT + tid);
+        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
+        if ((mine >> r) & 1u) {
+            const uint32_t pos = s_c[r][w] + __popc(b & ((1u << lane) - 1u));
+            if (pos < cap) g_start[pos] = (uint32_t)(b0 + r * SORT_NT + tid);
             else check_failed(st, 9);
         }
     }
@@ -718,6 +696,7 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
 // (a tile's predecessors have started, so they publish), each publishes its head count, then the running total
 // once its predecessors' is known. Waits are bounded; a wait that runs out raises FLAG_TIMEOUT.
 // ---------------------------------------------------------------------------------------------------
+constexpr uint64_t LB_AGG = 1ull << 62, LB_PREFIX = 2ull << 62, LB_VALUE = (1ull << 62) - 1;
 
 static __global__ void __launch_bounds__(SORT_NT) k_group_heads(const uint64_t* keys, int64_t n, KeyLayout kl, uint64_t* status, uint32_t* counter,
     uint32_t* g_start, uint32_t cap, DevStatus* st)
