@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per arrival rate")
     ap.add_argument("--tick", type=int, default=25, help="serve: substeps per serving tick")
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-e2e-sequential", dest="e2e_sequential", action="store_false",
+                    help="skip the end-to-end variant that uploads and downloads one after the other")
     ap.add_argument("--accuracy-steps", default="100,500", help="substeps at which FP32 is compared with the FP64 path")
     ap.add_argument("--oracle-steps", type=int, default=200, help="substeps of the elastic-cube check against the FP64 oracle")
     ap.add_argument("--fp64-steps", type=int, default=10)
@@ -537,20 +539,37 @@ def run_ours(args, world, rank):
         import torch
 
         host = torch.empty((n, 25), dtype=torch.float32).pin_memory().numpy()
+        res = torch.empty((n, 25), dtype=torch.float32).pin_memory().numpy()
         s.get_state(host)
         s.set_state(host)
         s.step(1)
-        s.get_state(host)
+        s.exchange_state(host, res)
+        s.step(1)
+        s.get_state(res)
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            s.set_state(host)
+        s.set_state(host)  # step 0's input
+        for k in range(args.e2e_steps):
             s.step(1)
-            s.get_state(host)
+            if k + 1 < args.e2e_steps:
+                s.exchange_state(host, res)  # step k's result out while step k+1's input comes in
+            else:
+                s.get_state(res)  # the last result
         el = time.perf_counter() - t0
         nbytes = n * 25 * 4
+        e2e_seq = None
+        if args.e2e_sequential:
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                s.set_state(host)
+                s.step(1)
+                s.get_state(res)
+            e2e_seq = allreduce_sum(world, n) * args.e2e_steps / allreduce_max(world, time.perf_counter() - t0)
         e2e = {"value": allreduce_sum(world, n) * args.e2e_steps / allreduce_max(world, el), "unit": "particle-substeps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-               "what": "per step: zr_scene_set_state from pinned FP32 host memory (x,v,C,F,d), zr_scene_step(1), zr_scene_get_state"}
+               "what": "every step's FP32 state (x,v,C,F,d) uploaded from pinned host memory and its result downloaded: "
+                       "zr_scene_set_state, then per step zr_scene_step(1) and zr_scene_exchange_state (this step's result out, the "
+                       "next step's input in, both link directions at once), the last result by zr_scene_get_state",
+               "sequential_value": e2e_seq}
     except Exception as ex:  # pinned memory needs torch; report instead of failing the line
         e2e = {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None, "error": str(ex)}
     cg_iterations = s.cg_iterations

@@ -123,6 +123,12 @@ int zr_scene_set_field(zr_scene* s, int field, const void* in, int dtype);
 /* Whole dynamic state, 25 values per particle: x(3) v(3) C(9) F(9) d(1). */
 int zr_scene_get_state(zr_scene* s, void* out, int dtype);
 int zr_scene_set_state(zr_scene* s, const void* in, int dtype);
+/* get_state into out, then set_state from in, in one call (the two buffers must not overlap). With both buffers
+ * in pinned host memory one kernel moves the two directions over the host link at the same time, so a pipeline
+ * that streams states through the GPU downloads one result while it uploads the next input. The reference has
+ * no counterpart (its state never leaves host memory); it replaces a writeState/readState pair
+ * (MpmSimulationBase.cpp:1060-1114) between two scenes that share one device. */
+int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype);
 /* FP64-accumulated reductions (MpmSimulationDataAnalysis.h:67-151): total mass, momentum x/y/z, kinetic
  * energy, max particle speed, grid mass of the last substep. */
 int zr_scene_reductions(zr_scene* s, double out[7]);

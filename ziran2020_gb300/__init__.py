@@ -80,6 +80,7 @@ def load_library(build_if_needed=True):
         "zr_scene_set_field": (i32, [vp, i32, vp, i32]),
         "zr_scene_get_state": (i32, [vp, vp, i32]),
         "zr_scene_set_state": (i32, [vp, vp, i32]),
+        "zr_scene_exchange_state": (i32, [vp, vp, vp, i32]),
         "zr_scene_reductions": (i32, [vp, pd]),
         "zr_scene_set_dt": (i32, [vp, d]),
         "zr_scene_set_implicit_damage": (i32, [vp, i32]),
@@ -291,6 +292,18 @@ class Scene:
     def set_state(self, a):
         dt = F32 if a.dtype == np.float32 else F64
         self._check(self.L.zr_scene_set_state(self.h, a.ctypes.data_as(C.c_void_p), dt))
+
+    def exchange_state(self, a, out):
+        """Download the state into out and upload a as the new state, in one call (a and out of one dtype, not
+        overlapping; with both in pinned memory the two directions of the host link run at once)."""
+        if a.dtype != out.dtype:
+            raise ValueError("exchange_state: input and output buffers must have the same dtype")
+        for b in (a, out):
+            if b.size != self.count * 25 or not b.flags.c_contiguous:
+                raise ValueError("exchange_state: buffers of count x 25 contiguous values expected")
+        dt = F32 if a.dtype == np.float32 else F64
+        self._check(self.L.zr_scene_exchange_state(self.h, a.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p), dt))
+        return out
 
     def reductions(self):
         out = np.zeros(7)

@@ -101,6 +101,9 @@ public:
     // Dynamic state in one call: x,v,C,F,d interleaved per particle as 25 values (d = 0 without damage).
     virtual int get_state(int scene, void* out25, int out_is_f32) = 0;
     virtual int set_state(int scene, const void* in25, int in_is_f32) = 0;
+    // get_state into out25, then set_state from in25 (disjoint buffers of one precision); with both in pinned host
+    // memory one kernel moves the two directions over the host link at the same time.
+    virtual int exchange_state(int scene, const void* in25, void* out25, int is_f32) = 0;
     // FP64-accumulated reductions: mass, momentum(3), kinetic energy, max speed, grid mass
     virtual int reductions(int scene, double* out7) = 0;
     virtual int set_dt(int scene, double dt) = 0;

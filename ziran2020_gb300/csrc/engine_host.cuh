@@ -359,13 +359,9 @@ public:
         return 0;
     }
 
-    // Rows of scene s between the pool and a caller's row-major buffer (rf: which fields). A buffer in pinned host
-    // memory is read or written by the kernel itself over the host link; any other goes through the staging buffer
-    // with one copy. Synchronises.
-    int transfer_rows(int s, const RowFields& rf, void* host, int f32, bool exporting)
+    // storage slot of every particle of scene s in the caller's order (inv_), for the row transfers
+    int fill_inv(int s)
     {
-        const int64_t n = h_scenes_[s].count;
-        const size_t bytes = (size_t)n * rf.W * (f32 ? 4 : 8);
         if (!inv_ || inv_cap_ < cap_) {
             void* old = inv_;
             dfree(old);
@@ -374,34 +370,56 @@ public:
             if (alloc((void**)&inv_, 4 * (size_t)cap_)) return ZR_ERR_CUDA_;
             inv_cap_ = cap_;
         }
-        k_inv<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, n, inv_);
+        k_inv<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), h_scenes_[s].first, h_scenes_[s].count, inv_);
+        ZR_CUDA(cudaGetLastError());
+        return 0;
+    }
+    // the device address of a buffer in pinned host memory, or null for any other buffer
+    static void* mapped(const void* host)
+    {
         cudaPointerAttributes at;
         void* dev = nullptr;
         if (cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) dev = at.devicePointer;
-        cudaGetLastError(); // an unknown pointer only means: stage it
+        cudaGetLastError(); // an unknown pointer only means: not mapped
+        return dev;
+    }
+    template <int MODE>
+    int launch_rows(int s, const RowFields& rf, const void* in, void* out, int f32)
+    {
+        const int64_t n = h_scenes_[s].count;
+        const int grid = (int)std::min<int64_t>((n + IO_ROWS - 1) / IO_ROWS, (int64_t)nsm_ * 16);
+        const size_t sm = (size_t)IO_ROWS * rf.W * (f32 ? 4 : 8) * (MODE == ROWS_EXCHANGE ? 2 : 1);
+        if (grid > 0) {
+            if (f32) {
+                if (sm > 48 * 1024) ZR_CUDA(cudaFuncSetAttribute(k_rows<T, float, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                k_rows<T, float, MODE><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (const float*)in, (float*)out);
+            }
+            else {
+                if (sm > 48 * 1024) ZR_CUDA(cudaFuncSetAttribute(k_rows<T, double, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                k_rows<T, double, MODE><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (const double*)in, (double*)out);
+            }
+        }
+        ZR_CUDA(cudaGetLastError());
+        return 0;
+    }
+
+    // Rows of scene s between the pool and a caller's row-major buffer (rf: which fields). A buffer in pinned host
+    // memory is read or written by the kernel itself over the host link; any other goes through the staging buffer
+    // with one copy. Synchronises.
+    int transfer_rows(int s, const RowFields& rf, void* host, int f32, bool exporting)
+    {
+        const size_t bytes = (size_t)h_scenes_[s].count * rf.W * (f32 ? 4 : 8);
+        int rc = fill_inv(s);
+        if (rc) return rc;
+        void* dev = mapped(host);
         if (!dev) {
-            int rc = ensure_stage(bytes);
+            rc = ensure_stage(bytes);
             if (rc) return rc;
             dev = stage_;
             if (!exporting) ZR_CUDA(cudaMemcpyAsync(stage_, host, bytes, cudaMemcpyHostToDevice, stream_));
         }
-        const int grid = (int)std::min<int64_t>((n + IO_ROWS - 1) / IO_ROWS, (int64_t)nsm_ * 16);
-        const size_t sm = (size_t)IO_ROWS * rf.W * (f32 ? 4 : 8);
-        if (grid > 0) {
-            if (f32) {
-                if (exporting)
-                    k_rows<T, float, true><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (float*)dev);
-                else
-                    k_rows<T, float, false><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (float*)dev);
-            }
-            else {
-                if (exporting)
-                    k_rows<T, double, true><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (double*)dev);
-                else
-                    k_rows<T, double, false><<<grid, IO_ROWS, sm, stream_>>>(pool(cur_), inv_, n, rf, (double*)dev);
-            }
-        }
-        ZR_CUDA(cudaGetLastError());
+        rc = exporting ? launch_rows<ROWS_EXPORT>(s, rf, nullptr, dev, f32) : launch_rows<ROWS_IMPORT>(s, rf, dev, nullptr, f32);
+        if (rc) return rc;
         if (exporting && dev == stage_) ZR_CUDA(cudaMemcpyAsync(host, stage_, bytes, cudaMemcpyDeviceToHost, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
         return 0;
@@ -454,6 +472,27 @@ public:
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
         int rc = transfer_rows(s, state_fields(), const_cast<void*>(in), f32, false);
         if (rc) return rc;
+        ZR_CUDA(forget_drive(s));
+        return rekey();
+    }
+
+    int exchange_state(int s, const void* in, void* out, int f32) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        const RowFields rf = state_fields();
+        const size_t bytes = (size_t)h_scenes_[s].count * rf.W * (f32 ? 4 : 8);
+        const char *i0 = (const char*)in, *o0 = (const char*)out;
+        if (bytes && i0 < o0 + bytes && o0 < i0 + bytes) return arg("exchange_state: the input and output buffers overlap");
+        void *din = mapped(in), *dout = mapped(out);
+        if (!din || !dout) { // not both mapped: one direction after the other
+            int rc = get_state(s, out, f32);
+            return rc ? rc : set_state(s, in, f32);
+        }
+        int rc = fill_inv(s);
+        if (rc) return rc;
+        rc = launch_rows<ROWS_EXCHANGE>(s, rf, din, dout, f32);
+        if (rc) return rc;
+        ZR_CUDA(cudaStreamSynchronize(stream_));
         ZR_CUDA(forget_drive(s));
         return rekey();
     }

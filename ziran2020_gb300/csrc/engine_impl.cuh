@@ -2783,41 +2783,53 @@ struct RowFields {
 };
 constexpr int IO_ROWS = 128; // rows per CTA (one per thread)
 
-// Rows of a scene between the particle pool and a row-major buffer (host memory mapped into the device, or a
+// Rows of a scene between the particle pool and row-major buffers (host memory mapped into the device, or a
 // staging buffer). A CTA moves IO_ROWS consecutive rows: pool <-> shared memory per row (thread per row, slot from
 // inv), shared memory <-> buffer as one contiguous run of IO_ROWS * W values (coalesced, whole lines over the
-// host link).
-template <class T, class O, bool EXPORT>
-__global__ void __launch_bounds__(IO_ROWS) k_rows(Pool<T> p, const uint32_t* inv, int64_t n, RowFields rf, O* buf)
+// host link). MODE: ROWS_IMPORT (in -> pool), ROWS_EXPORT (pool -> out), ROWS_EXCHANGE (pool -> out, then in ->
+// pool, row by row: a CTA reads its rows out of the pool before it overwrites them, and CTAs own disjoint rows,
+// so out receives the state from before the call; with many CTAs in flight both directions of the link are busy
+// at once).
+enum { ROWS_IMPORT = 0, ROWS_EXPORT = 1, ROWS_EXCHANGE = 2 };
+template <class T, class O, int MODE>
+__global__ void __launch_bounds__(IO_ROWS) k_rows(Pool<T> p, const uint32_t* inv, int64_t n, RowFields rf, const O* in, O* out)
 {
     extern __shared__ __align__(16) unsigned char rows_dyn[];
-    O* sm = reinterpret_cast<O*>(rows_dyn);
     const int W = rf.W;
+    O* sm_o = reinterpret_cast<O*>(rows_dyn); // rows leaving the pool
+    O* sm_i = MODE == ROWS_EXCHANGE ? sm_o + IO_ROWS * W : sm_o; // rows entering it
     for (int64_t base = (int64_t)blockIdx.x * IO_ROWS; base < n; base += (int64_t)gridDim.x * IO_ROWS) {
         const int rows = (int)min((int64_t)IO_ROWS, n - base);
-        O* run = buf + base * W;
-        if (!EXPORT) {
-            for (int q = threadIdx.x; q < rows * W; q += IO_ROWS) sm[q] = run[q];
+        const uint32_t slot = threadIdx.x < rows ? inv[base + threadIdx.x] : 0u;
+        if (MODE != ROWS_IMPORT) {
+            if (threadIdx.x < rows) {
+                O* r = sm_o + threadIdx.x * W;
+                int c0 = 0;
+                for (int k = 0; k < rf.count; k++) {
+                    for (int c = 0; c < rf.nc[k]; c++) r[c0 + c] = (O)p.f[(int64_t)(rf.f0[k] + c) * p.stride + slot];
+                    c0 += rf.nc[k];
+                }
+            }
             __syncthreads();
         }
-        if (threadIdx.x < rows) {
-            const uint32_t slot = inv[base + threadIdx.x];
-            O* r = sm + threadIdx.x * W;
-            int c0 = 0;
-            for (int k = 0; k < rf.count; k++) {
-                for (int c = 0; c < rf.nc[k]; c++) {
-                    T* f = p.f + (int64_t)(rf.f0[k] + c) * p.stride + slot;
-                    if (EXPORT)
-                        r[c0 + c] = (O)*f;
-                    else
-                        *f = (T)r[c0 + c];
-                }
-                c0 += rf.nc[k];
+        {
+            O* run_o = MODE != ROWS_IMPORT ? out + base * W : nullptr;
+            const O* run_i = MODE != ROWS_EXPORT ? in + base * W : nullptr;
+            for (int q = threadIdx.x; q < rows * W; q += IO_ROWS) {
+                if (MODE != ROWS_IMPORT) run_o[q] = sm_o[q];
+                if (MODE != ROWS_EXPORT) sm_i[q] = run_i[q];
             }
+            __syncthreads();
         }
-        __syncthreads();
-        if (EXPORT) {
-            for (int q = threadIdx.x; q < rows * W; q += IO_ROWS) run[q] = sm[q];
+        if (MODE != ROWS_EXPORT) {
+            if (threadIdx.x < rows) {
+                const O* r = sm_i + threadIdx.x * W;
+                int c0 = 0;
+                for (int k = 0; k < rf.count; k++) {
+                    for (int c = 0; c < rf.nc[k]; c++) p.f[(int64_t)(rf.f0[k] + c) * p.stride + slot] = (T)r[c0 + c];
+                    c0 += rf.nc[k];
+                }
+            }
             __syncthreads();
         }
     }
