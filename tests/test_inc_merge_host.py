@@ -1,6 +1,6 @@
-"""CPU restatement of the hand-written incremental sort (engine_impl.cuh: k_sort_tiles, k_sort_scan1,
-k_sort_bucket, k_sort_scan2, k_sort_place, k_sort_merge) and of the group-head pass (k_group_heads), checked
-against numpy's stable sort on seeded inputs and edge cases.
+"""CPU restatement of the hand-written incremental sort (engine_impl.cuh: k_sort_tiles, k_sort_bucket, k_sort_merge
+and the head placement of k_heads_activate) and of the group-head pass (k_group_heads), checked against numpy's
+stable sort on seeded inputs and edge cases.
 
 Storage index i holds the key the particle was sorted by in the previous substep (kold, ascending) and its new
 key (knew). Stayers (knew == kold) are already in key order. Storage is cut into tiles of T indices; B[j] is the
@@ -29,7 +29,15 @@ def incremental_sort(knew, kold, T, mover_order_seed=0, maxm=None):
         idx = np.nonzero(stay[j * T:(j + 1) * T])[0]
         t_first.append(int(knew[j * T + idx[0]]) if len(idx) else NOKEY)
     stay_off = np.concatenate([[0], np.cumsum(t_stay)[:-1]]).astype(np.int64)
-    B = list(np.minimum.accumulate(np.array(t_first[::-1], dtype=np.uint64))[::-1])
+    # B[q]: the first stayer key at or after tile q (k_sort_bucket walks past tiles without a stayer); it equals the
+    # suffix minimum of the tiles' first stayer keys because the stayers keep their sorted order
+    B = []
+    for q in range(tiles):
+        r = q
+        while t_first[r] == NOKEY and r + 1 < tiles:
+            r += 1
+        B.append(t_first[r])
+    assert B == [int(v) for v in np.minimum.accumulate(np.array(t_first[::-1], dtype=np.uint64))[::-1]]
     movers = list(np.nonzero(~stay)[0])
     np.random.default_rng(mover_order_seed).shuffle(movers)  # the device's list order is arbitrary
     bucket = {}
@@ -41,16 +49,16 @@ def incremental_sort(knew, kold, T, mover_order_seed=0, maxm=None):
     boff = np.concatenate([[0], np.cumsum(bcnt)[:-1]]).astype(np.int64)
     out_k = np.full(n, -1, np.int64)
     out_i = np.full(n, -1, np.int64)
-    # the key before each tile's output (k_sort_scan1 / k_sort_scan2): the larger of the lower tiles' last stayer
-    # key and the lower buckets' largest mover key (None when nothing comes before)
-    preds, last_s, last_m = [], None, None
+    # the key before each tile's output (k_sort_merge): the largest of the lower tiles' last stayer keys and the lower
+    # buckets' largest mover keys (None when nothing comes before)
+    t_last = []
     for j in range(tiles):
-        preds.append(None if last_s is None and last_m is None else max(v for v in (last_s, last_m) if v is not None))
-        sk_j = [int(knew[i]) for i in range(j * T, min(n, (j + 1) * T)) if stay[i]]
-        if sk_j:
-            last_s = sk_j[-1]
-        if bucket.get(j):
-            last_m = max(k for k, _ in bucket[j])
+        idx = np.nonzero(stay[j * T:(j + 1) * T])[0]
+        t_last.append(int(knew[j * T + idx[-1]]) if len(idx) else NOKEY)
+    preds = []
+    for j in range(tiles):
+        below = [v for v in t_last[:j] if v != NOKEY] + [max(k for k, _ in bucket[q]) for q in range(j) if bucket.get(q)]
+        preds.append(max(below) if below else None)
     for j in range(tiles):
         S = [(int(knew[i]), i) for i in range(j * T, min(n, (j + 1) * T)) if stay[i]]
         Mv = sorted(bucket.get(j, []))

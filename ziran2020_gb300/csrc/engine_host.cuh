@@ -139,7 +139,7 @@ public:
             }
             ZR_CUDA(cudaStreamSynchronize(stream_));
             void* olds[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, sort_tmp_, pay_,
-                sort_aux_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_ };
+                sort_aux_, inc_move_, inc_bkey_, inc_bidx_ };
             for (void* p : olds)
                 if (p) cudaFree(p);
             pool_[0] = grown_pool[0];
@@ -149,15 +149,13 @@ public:
             cap_ = (uint64_t)cap;
             pay_ = nullptr;
             sort_aux_ = nullptr;
-            inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
-            inc_cnt_ = nullptr;
+            inc_move_ = inc_bkey_ = inc_bidx_ = nullptr;
             // P2G payload: NPAY fields of sorted particles at q + q/8, plus the copy granularity at the end
             pstride_ = (int64_t)((pay_pos((uint64_t)cap) + 64 + 63) & ~(uint64_t)63);
             if (alloc((void**)&keys_in_, 8 * cap) || alloc((void**)&keys_sorted_, 8 * cap) || alloc((void**)&iota_, 4 * cap)
                 || alloc((void**)&vals_sorted_, 4 * cap) || alloc((void**)&g_start_, 4 * cap) || alloc((void**)&pay_, sizeof(T) * NPAY * (size_t)pstride_)
-                || alloc((void**)&sort_aux_, sort_aux_bytes(cap)) || alloc((void**)&inc_move_, 4 * cap) || alloc((void**)&inc_mkeys_, 4 * cap)
-                || alloc((void**)&inc_mvals_, 4 * cap) || alloc((void**)&inc_mkeys2_, 4 * cap) || alloc((void**)&inc_mvals2_, 4 * cap)
-                || alloc((void**)&inc_cnt_, 16))
+                || alloc((void**)&sort_aux_, sort_aux_bytes(cap)) || alloc((void**)&inc_move_, 4 * cap)
+                || alloc((void**)&inc_bkey_, 4 * bucket_slots(cap)) || alloc((void**)&inc_bidx_, 4 * bucket_slots(cap)))
                 return ZR_ERR_CUDA_;
             mcap_ = std::min<int64_t>(cap, std::max<int64_t>(MCAP_MIN, cap / 32));
             ZR_CUDA(cudaMemsetAsync(pay_, 0, sizeof(T) * NPAY * (size_t)pstride_, stream_));
@@ -759,8 +757,7 @@ private:
     // the sort's tile arrays (stayer bits, per-tile counts and keys, bucket counts, group-head look-back words);
     // the movers' list, buckets and tickets, and their keys and storage indices grouped by bucket
     unsigned char* sort_aux_ = nullptr;
-    uint32_t *inc_move_ = nullptr, *inc_mkeys_ = nullptr, *inc_mvals_ = nullptr, *inc_mkeys2_ = nullptr, *inc_mvals2_ = nullptr;
-    int64_t* inc_cnt_ = nullptr; // [0] movers found
+    uint32_t *inc_move_ = nullptr, *inc_bkey_ = nullptr, *inc_bidx_ = nullptr; // mover list; movers by bucket (fixed slots)
     int64_t mcap_ = 0; // movers the incremental sort takes per substep
     void *ck_pool_ = nullptr, *ck_pid_ = nullptr, *ck_scenes_ = nullptr; // device checkpoint
     uint64_t ck_cap_ = 0;
@@ -791,9 +788,12 @@ private:
 
     // tiles of the sort and of the group-head pass (SORT_TILE keys each) for up to cap particles
     static int64_t sort_tiles(int64_t n) { return std::max<int64_t>(1, (n + SORT_TILE - 1) / SORT_TILE); }
-    // sort_aux_: [stay bits: ceil(cap/32) u32][t_stay, t_first, b_cnt, t_last, b_max, t_heads: tiles u32 each]
-    // [look-back: tiles + 1 u64]
-    static size_t sort_aux_words(int64_t cap) { return (size_t)((cap + 31) / 32) + 6 * (size_t)sort_tiles(cap) + 1; }
+    // movers' fixed bucket slots: SORT_MAXM per tile
+    static int64_t bucket_slots(int64_t cap) { return sort_tiles(cap) * SORT_MAXM; }
+    // sort_aux_: [zeroed every substep: movers found (i64), unused (3 x i64), b_cnt, b_max (tiles u32 each)]
+    // [stay bits: ceil(cap/32) u32][t_stay, t_first, t_last, t_base, t_heads: tiles u32 each][look-back: tiles + 1 u64]
+    static size_t sort_zero_bytes(int64_t cap) { return 32 + 8 * (size_t)sort_tiles(cap); }
+    static size_t sort_aux_words(int64_t cap) { return sort_zero_bytes(cap) / 4 + (size_t)((cap + 31) / 32) + 5 * (size_t)sort_tiles(cap) + 1; }
     static size_t sort_aux_bytes(int64_t cap) { return 4 * sort_aux_words(cap) + 8 * ((size_t)sort_tiles(cap) + 2); }
     uint64_t* lookback_words() const
     {
@@ -803,41 +803,38 @@ private:
     bool inc_sort_usable() const { return inc_sort_on_ && !kl_.wide && kl_.total() <= 31 && inc_move_; }
 
     // The sorted keys and storage indices of keys_in_ from the previous substep's sorted keys (keys_sorted_), by
-    // the hand-written kernels of the incremental sort (stayers in place, movers bucketed by stayer tile and merged).
-    cudaError_t sort_keys_incremental(int64_t n)
+    // the hand-written kernels of the incremental sort (stayers in place, movers bucketed by stayer tile and merged),
+    // then the group heads placed and their blocks activated (k_heads_activate).
+    // ev_sorted (may be null) is recorded between the merge and the head placement.
+    cudaError_t sort_and_activate_incremental(int64_t n, const StepArgs<T>& a, cudaEvent_t ev_sorted)
     {
         const uint32_t* nk = (const uint32_t*)keys_in_;
         const uint32_t* ok = (const uint32_t*)keys_sorted_;
         SortBufs sb;
-        const int64_t tiles = sort_tiles(n);
-        uint32_t* w = reinterpret_cast<uint32_t*>(sort_aux_);
-        sb.stay_bits = w;
-        sb.t_stay = w + (cap_ + 31) / 32;
-        sb.t_first = sb.t_stay + sort_tiles((int64_t)cap_);
-        sb.b_cnt = sb.t_first + sort_tiles((int64_t)cap_);
-        sb.t_last = sb.b_cnt + sort_tiles((int64_t)cap_);
-        sb.b_max = sb.t_last + sort_tiles((int64_t)cap_);
-        sb.t_heads = sb.b_max + sort_tiles((int64_t)cap_);
+        const int64_t tiles = sort_tiles(n), tcap = sort_tiles((int64_t)cap_);
+        sb.cnt = reinterpret_cast<int64_t*>(sort_aux_);
+        sb.b_cnt = reinterpret_cast<uint32_t*>(sort_aux_ + 32);
+        sb.b_max = sb.b_cnt + tcap;
+        sb.stay_bits = sb.b_max + tcap;
+        sb.t_stay = sb.stay_bits + (cap_ + 31) / 32;
+        sb.t_first = sb.t_stay + tcap;
+        sb.t_last = sb.t_first + tcap;
+        sb.t_base = sb.t_last + tcap;
+        sb.t_heads = sb.t_base + tcap;
         sb.m_idx = inc_move_;
-        sb.m_bkt = inc_mkeys_;
-        sb.m_tkt = inc_mvals_;
-        sb.b_key = inc_mkeys2_;
-        sb.b_idx = inc_mvals2_;
-        sb.cnt = inc_cnt_;
+        sb.b_key = inc_bkey_;
+        sb.b_idx = inc_bidx_;
         sb.mcap = mcap_;
         sb.n = n;
         sb.tiles = (int)tiles;
-        cudaError_t e = cudaMemsetAsync(inc_cnt_, 0, 16, stream_);
+        cudaError_t e = cudaMemsetAsync(sort_aux_, 0, sort_zero_bytes((int64_t)cap_), stream_);
         if (e != cudaSuccess) return e;
-        const int mgrid = (int)std::min<int64_t>(nsm_ * 4, (mcap_ + 255) / 256);
+        const int mgrid = (int)std::max<int64_t>(1, std::min<int64_t>(nsm_ * 4, (mcap_ + SORT_NT - 1) / SORT_NT));
         k_sort_tiles<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, ok, sb, st_);
-        k_sort_scan1<<<1, 1024, 0, stream_>>>(sb, st_);
-        k_sort_bucket<<<mgrid, 256, 0, stream_>>>(nk, sb);
-        k_sort_scan2<<<1, 1024, 0, stream_>>>(sb);
-        k_sort_place<<<mgrid, 256, 0, stream_>>>(nk, sb, st_);
+        k_sort_bucket<<<mgrid, SORT_NT, 0, stream_>>>(nk, sb, st_);
         k_sort_merge<<<(unsigned)tiles, SORT_NT, 0, stream_>>>(nk, sb, (uint32_t*)keys_sorted_, vals_sorted_, kl_, st_);
-        // group heads from the merge's per-tile counts: no look-back across tiles
-        k_heads_place<<<(unsigned)tiles, SORT_NT, 0, stream_>>>((const uint32_t*)keys_sorted_, sb, kl_, g_start_, (uint32_t)cap_, st_);
+        if (ev_sorted && (e = cudaEventRecord(ev_sorted, stream_)) != cudaSuccess) return e;
+        k_heads_activate<T><<<(unsigned)tiles, SORT_NT, 0, stream_>>>(a, sb, g_start_, (uint32_t)cap_);
         return cudaGetLastError();
     }
 
@@ -1131,12 +1128,13 @@ private:
         a.st = st_;
         a.n_total = N_;
         a.b_cap = b_cap_;
+        a.n_scenes = n_scenes();
         a.kl = kl_;
         return a;
     }
 
     // Enqueue one substep reading buffer `parity`. With ev != nullptr, events are recorded between the
-    // phases (sort+groups | activate | p2g | grid | g2p+end).
+    // phases (sort | group heads, activate, neighbour slots | p2g | grid | g2p+end).
     int enqueue_step(int parity, cudaEvent_t* ev, bool full_sort = false)
     {
         StepArgs<T> a = args(parity);
@@ -1144,14 +1142,13 @@ private:
         if (ev) ZR_CUDA(cudaEventRecord(ev[0], stream_));
         if (full_sort || !inc_sort_usable()) {
             ZR_CUDA(sort_keys(n));
+            if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
             ZR_CUDA(group_heads(n));
+            k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         }
-        else
-            ZR_CUDA(sort_keys_incremental(n)); // places the group heads itself
-        if (ev) ZR_CUDA(cudaEventRecord(ev[1], stream_));
-        k_zero_grid_mass<T><<<1, 256, 0, stream_>>>(grid_mass_, n_scenes());
-        k_activate<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
-        k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
+        else // its last kernel places the group heads and activates their blocks (after ev[1]: the activate phase)
+            ZR_CUDA(sort_and_activate_incremental(n, a, ev ? ev[1] : nullptr));
+        k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a); // also zeroes the per-scene grid mass
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
         if (sched_.fused == 3)
             launch_ws(a, nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_ws_[models_slot()]));
@@ -1637,7 +1634,7 @@ private:
         drop_graphs();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
             d_scenes_, grid_mass_, st_, sort_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
-            sort_aux_, inc_move_, inc_mkeys_, inc_mvals_, inc_mkeys2_, inc_mvals2_, inc_cnt_, inv_ };
+            sort_aux_, inc_move_, inc_bkey_, inc_bidx_, inv_ };
         for (void* p : ps)
             if (p) cudaFree(p);
         pool_[0] = pool_[1] = nullptr;
@@ -1660,8 +1657,7 @@ private:
         cgs_ = nullptr;
         implicit_ = false;
         sort_aux_ = nullptr;
-        inc_move_ = inc_mkeys_ = inc_mvals_ = inc_mkeys2_ = inc_mvals2_ = nullptr;
-        inc_cnt_ = nullptr;
+        inc_move_ = inc_bkey_ = inc_bidx_ = nullptr;
         mcap_ = 0;
         inv_ = nullptr;
         inv_cap_ = 0;

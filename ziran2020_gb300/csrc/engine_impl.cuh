@@ -109,6 +109,7 @@ struct StepArgs {
     DevStatus* st;
     uint32_t n_total;
     uint32_t b_cap;
+    int n_scenes;
     KeyLayout kl;
 };
 
@@ -244,14 +245,15 @@ struct GroupHead {
 // in the bucket plus the tile's stayers with a key not above its own. The order is fully determined by the keys
 // and storage indices (no dependence on the order in which movers were found).
 //
-//   k_sort_tiles    per tile: stayer count, first and last stayer key; movers appended to a list (one atomic per tile)
-//   k_sort_scan1    one CTA: stayer offsets per tile, B, the largest stayer key below each tile, bucket counters cleared
-//   k_sort_bucket   per mover: bucket (binary search over B), a ticket within it, the bucket's largest key
-//   k_sort_scan2    one CTA: mover offsets per bucket; the key just before each tile's output
-//   k_sort_place    per mover: (key, storage index) into its bucket
-//   k_sort_merge    per tile: the tile's stayers and its bucket's movers (sorted in shared memory) to their places;
-//                   the group heads in the tile's output counted
-//   k_heads_place   per tile: the group heads of its output written to g_start after the lower tiles' heads
+//   k_sort_tiles      per tile: stayer count, first and last stayer key; movers appended to a list (one atomic per
+//                     tile)
+//   k_sort_bucket     per mover: bucket (binary search over B, read from the tiles' first stayer keys), a ticket
+//                     within it, the bucket's largest key, and (key, storage index) into the bucket's fixed slots
+//   k_sort_merge      per tile: where its output starts and the key just before it (sums and maxima over the lower
+//                     tiles and buckets, by the CTA itself), then the tile's stayers and its bucket's movers (sorted
+//                     in shared memory) to their places; the group heads in the tile's output counted
+//   k_heads_activate  per tile: the group heads of its output written to g_start after the lower tiles' heads, and
+//                     their blocks and +1 neighbours activated in the grid hash
 //
 // More movers than the list holds, or a bucket larger than SORT_MAXM, raises FLAG_SORT: the host repeats the
 // substep with a full radix sort (and grows the list).
@@ -260,19 +262,18 @@ constexpr int SORT_NT = 256, SORT_PER = 8, SORT_TILE = SORT_NT * SORT_PER, SORT_
 constexpr uint32_t SORT_NOKEY = 0xffffffffu; // keys of the incremental sort hold at most 31 bits
 
 struct SortBufs {
-    uint32_t* t_stay; // [tiles] stayers per tile, then (scan1) their exclusive offsets
-    uint32_t* t_first; // [tiles] first stayer key per tile, then (scan1) B (non-decreasing)
-    uint32_t* b_cnt; // [tiles] movers per bucket, then (scan2) their exclusive offsets
-    uint32_t* m_idx; // [mcap] movers' storage indices (list order)
-    uint32_t* m_bkt; // [mcap] bucket of each listed mover
-    uint32_t* m_tkt; // [mcap] ticket of each listed mover inside its bucket
-    uint32_t* b_key; // [mcap] movers' keys grouped by bucket
-    uint32_t* b_idx; // [mcap] movers' storage indices grouped by bucket
+    int64_t* cnt; // [0] movers found (zeroed per substep)
+    uint32_t* b_cnt; // [tiles] movers per bucket (zeroed per substep)
+    uint32_t* b_max; // [tiles] largest mover key per bucket (zeroed per substep)
     uint32_t* stay_bits; // [ceil(n / 32)] bit i % 32 of word i / 32: storage index i keeps its key
-    uint32_t* t_last; // [tiles] last stayer key per tile, then (scan1) the largest stayer key of the lower tiles
-    uint32_t* b_max; // [tiles] largest mover key per bucket, then (scan2) the key before the tile's output
+    uint32_t* t_stay; // [tiles] stayers per tile
+    uint32_t* t_first; // [tiles] first stayer key per tile (SORT_NOKEY: none)
+    uint32_t* t_last; // [tiles] last stayer key per tile (SORT_NOKEY: none)
+    uint32_t* t_base; // [tiles] sorted position of the tile's first output (the merge writes it)
     uint32_t* t_heads; // [tiles] group heads in the tile's output (the merge counts them)
-    int64_t* cnt; // [0] movers found, [1] unused
+    uint32_t* m_idx; // [mcap] movers' storage indices (list order)
+    uint32_t* b_key; // [tiles * SORT_MAXM] movers' keys: bucket j's at j * SORT_MAXM + ticket
+    uint32_t* b_idx; // [tiles * SORT_MAXM] movers' storage indices, likewise
     int64_t mcap;
     int64_t n;
     int tiles;
@@ -353,141 +354,38 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_tiles(const uint32_t* k
     (void)st;
 }
 
-// Scans of one CTA of 1024 threads (32 warps): shuffles inside each warp, then over the warp totals. op(a, b) combines
-// an earlier a with a later b; the result is the exclusive prefix of v in thread order, *total the combination of all.
-struct OpAdd {
-    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
-};
-struct OpMin {
-    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return min(a, b); }
-};
-struct OpLast { // the latest value that is not SORT_NOKEY
-    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return b != SORT_NOKEY ? b : a; }
-};
-template <class Op>
-__device__ uint32_t cta_scan1024(uint32_t v, Op op, uint32_t identity, uint32_t* total)
+static __global__ void __launch_bounds__(SORT_NT) k_sort_bucket(const uint32_t* knew, SortBufs sb, DevStatus* st)
 {
-    __shared__ uint32_t s_w[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x = op(y, x);
+    const int64_t Mall = sb.cnt[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicMax(&st->max_movers, (uint32_t)(Mall < 0xffffffffLL ? Mall : 0xffffffffLL));
+        if (Mall > sb.mcap) raise_flag(st, FLAG_SORT);
     }
-    if (lane == 31) s_w[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        uint32_t t = s_w[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-            if (lane >= o) t = op(y, t);
-        }
-        s_w[lane] = t;
-    }
-    __syncthreads();
-    uint32_t ex = __shfl_up_sync(0xffffffffu, x, 1);
-    if (lane == 0) ex = identity;
-    const uint32_t r = op(w ? s_w[w - 1] : identity, ex);
-    if (total) *total = s_w[31];
-    __syncthreads(); // s_w is reused by the next call
-    return r;
-}
-
-// one CTA: exclusive offsets of the tiles' stayers, B = suffix minimum of the first stayer keys (stayers ascend in
-// storage order, so this is the first stayer key at or after each tile), the largest stayer key of the lower tiles,
-// bucket counters cleared; too many movers raise FLAG_SORT
-static __global__ void __launch_bounds__(1024) k_sort_scan1(SortBufs sb, DevStatus* st)
-{
-    __shared__ uint32_t s_x[1024];
-    const int T = sb.tiles, tid = threadIdx.x;
-    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
-    const int64_t M = sb.cnt[0];
-    if (tid == 0) atomicMax(&st->max_movers, (uint32_t)(M < 0xffffffffLL ? M : 0xffffffffLL));
-    if (tid == 0 && M > sb.mcap) raise_flag(st, FLAG_SORT);
-    uint32_t sum = 0, lastk = SORT_NOKEY, mn = SORT_NOKEY;
-    for (int q = lo; q < hi; q++) {
-        sum += sb.t_stay[q];
-        if (sb.t_last[q] != SORT_NOKEY) lastk = sb.t_last[q];
-        mn = min(mn, sb.t_first[q]);
-    }
-    uint32_t run = cta_scan1024(sum, OpAdd{}, 0u, nullptr);
-    uint32_t before = cta_scan1024(lastk, OpLast{}, SORT_NOKEY, nullptr);
-    // suffix minimum: scan the block minima in reverse thread order
-    s_x[tid] = mn;
-    __syncthreads();
-    const uint32_t rev = cta_scan1024(s_x[1023 - tid], OpMin{}, SORT_NOKEY, nullptr); // minimum over the blocks after block 1023 - tid
-    s_x[1023 - tid] = rev;
-    __syncthreads();
-    uint32_t suf = s_x[tid];
-    for (int q = lo; q < hi; q++) {
-        const uint32_t c = sb.t_stay[q], l = sb.t_last[q];
-        sb.t_stay[q] = run;
-        run += c;
-        sb.t_last[q] = before;
-        if (l != SORT_NOKEY) before = l;
-        sb.b_cnt[q] = 0;
-        sb.b_max[q] = 0;
-    }
-    for (int q = hi - 1; q >= lo; q--) {
-        suf = min(suf, sb.t_first[q]);
-        sb.t_first[q] = suf;
-    }
-}
-
-static __global__ void k_sort_bucket(const uint32_t* knew, SortBufs sb)
-{
-    const int64_t M = min(sb.cnt[0], sb.mcap);
+    const int64_t M = min(Mall, sb.mcap);
+    const int T = sb.tiles;
+    // B[q] = the first stayer key at or after tile q: a tile without a stayer takes the next tile's (emptying a tile
+    // takes 2048 listed movers, so these walks are short); non-decreasing, as the stayers keep their order
+    auto B = [&](int q) {
+        uint32_t v = sb.t_first[q];
+        while (v == SORT_NOKEY && ++q < T) v = sb.t_first[q];
+        return v;
+    };
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t i = sb.m_idx[m];
         const uint32_t k = i < (uint64_t)sb.n ? knew[i] : SORT_NOKEY;
-        int lo = 0, hi = sb.tiles; // first j with B[j] > k
+        int lo = 0, hi = T; // first j with B[j] > k
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
-            if (sb.t_first[mid] <= k) lo = mid + 1;
+            if (B(mid) <= k) lo = mid + 1;
             else hi = mid;
         }
         const uint32_t b = lo > 0 ? (uint32_t)(lo - 1) : 0u;
-        sb.m_bkt[m] = b;
-        sb.m_tkt[m] = atomicAdd(&sb.b_cnt[b], 1u);
+        const uint32_t t = atomicAdd(&sb.b_cnt[b], 1u);
         atomicMax(&sb.b_max[b], k);
-    }
-}
-
-// one CTA: exclusive offsets of the buckets' movers, and the key just before each tile's output: the larger of
-// the lower tiles' largest stayer key and the lower buckets' largest mover key (bucket key ranges ascend, so the
-// latter is the largest key of the last non-empty lower bucket); SORT_NOKEY when nothing comes before
-static __global__ void __launch_bounds__(1024) k_sort_scan2(SortBufs sb)
-{
-    const int T = sb.tiles, tid = threadIdx.x;
-    const int per = (T + 1023) / 1024, lo = tid * per, hi = min(T, lo + per);
-    uint32_t sum = 0, lastm = SORT_NOKEY;
-    for (int q = lo; q < hi; q++) {
-        sum += sb.b_cnt[q];
-        if (sb.b_cnt[q]) lastm = sb.b_max[q];
-    }
-    uint32_t run = cta_scan1024(sum, OpAdd{}, 0u, nullptr);
-    uint32_t before = cta_scan1024(lastm, OpLast{}, SORT_NOKEY, nullptr);
-    for (int q = lo; q < hi; q++) {
-        const uint32_t c = sb.b_cnt[q], m = sb.b_max[q], ls = sb.t_last[q];
-        sb.b_cnt[q] = run;
-        run += c;
-        sb.b_max[q] = before == SORT_NOKEY ? ls : (ls == SORT_NOKEY ? before : max(before, ls));
-        if (c) before = m;
-    }
-}
-
-static __global__ void k_sort_place(const uint32_t* knew, SortBufs sb, DevStatus* st)
-{
-    const int64_t M = min(sb.cnt[0], sb.mcap);
-    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t i = sb.m_idx[m];
-        const uint64_t pos = (uint64_t)sb.b_cnt[sb.m_bkt[m]] + sb.m_tkt[m];
-        if (pos >= (uint64_t)M || i >= (uint64_t)sb.n) {
-            check_failed(st, 8);
-            continue;
+        if (t < (uint32_t)SORT_MAXM) { // a fuller bucket makes the merge raise FLAG_SORT
+            sb.b_key[(size_t)b * SORT_MAXM + t] = k;
+            sb.b_idx[(size_t)b * SORT_MAXM + t] = i;
         }
-        sb.b_key[pos] = knew[i];
-        sb.b_idx[pos] = i;
     }
 }
 
@@ -499,16 +397,35 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
     __shared__ uint32_t o_key[SORT_TILE + SORT_MAXM]; // the tile's output in order
     __shared__ uint32_t s_heads;
     __shared__ uint32_t s_wcnt[SORT_PER][SORT_NT / 32];
+    __shared__ uint32_t s_red[2][SORT_NT / 32];
     __shared__ int s_ns;
     const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t M = sb.cnt[0];
     if (M > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
-    const uint32_t bo = sb.b_cnt[j], be = j + 1 < sb.tiles ? sb.b_cnt[j + 1] : (uint32_t)M;
-    if (be < bo || be - bo > (uint32_t)SORT_MAXM) {
+    const uint32_t bc = sb.b_cnt[j];
+    if (bc > (uint32_t)SORT_MAXM) {
         if (tid == 0) raise_flag(st, FLAG_SORT);
         return;
     }
-    const int nm = (int)(be - bo);
+    const int nm = (int)bc;
+    // the lower tiles and buckets: their element count (where this tile's output starts) and their largest key (the
+    // key just before the output: stayer and bucket key ranges ascend with the tile). pk holds key + 1, 0 for none.
+    uint32_t below = 0, pk = 0;
+#pragma unroll 4
+    for (int q = tid; q < j; q += SORT_NT) {
+        const uint32_t c = sb.b_cnt[q], l = sb.t_last[q], mk = sb.b_max[q];
+        below += sb.t_stay[q] + c;
+        if (l != SORT_NOKEY) pk = max(pk, l + 1);
+        if (c) pk = max(pk, mk + 1);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        below += __shfl_down_sync(0xffffffffu, below, o);
+        pk = max(pk, __shfl_down_sync(0xffffffffu, pk, o));
+    }
+    if (lane == 0) {
+        s_red[0][w] = below;
+        s_red[1][w] = pk;
+    }
     // the tile's stayers, compacted in storage order: item (r, w, lane) = t0 + r*256 + w*32 + lane
     const int64_t t0 = (int64_t)j * SORT_TILE;
     unsigned mine = 0; // bit r: this thread's item of round r stays
@@ -527,8 +444,8 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         if (lane == 0) s_wcnt[r][w] = __popc(b);
     }
     for (int q = tid; q < nm; q += SORT_NT) {
-        m_key[q] = sb.b_key[bo + q];
-        m_idx[q] = sb.b_idx[bo + q];
+        m_key[q] = sb.b_key[(size_t)j * SORT_MAXM + q];
+        m_idx[q] = sb.b_idx[(size_t)j * SORT_MAXM + q];
     }
     __syncthreads();
     if (w == 0) { // exclusive offsets of the 64 (round, warp) groups in storage order: two per lane, one warp scan
@@ -565,7 +482,14 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
     }
     __syncthreads();
     const int ns = s_ns;
-    const int64_t base = (int64_t)sb.t_stay[j] + bo; // elements of lower tiles and buckets
+    uint32_t below_all = 0, pk_all = 0;
+#pragma unroll
+    for (int q = 0; q < SORT_NT / 32; q++) {
+        below_all += s_red[0][q];
+        pk_all = max(pk_all, s_red[1][q]);
+    }
+    const int64_t base = below_all; // elements of lower tiles and buckets
+    if (tid == 0) sb.t_base[j] = below_all;
     for (int t = tid; t < ns; t += SORT_NT) { // stayer: its rank + the bucket's movers with a smaller key
         const uint32_t k = s_key[t];
         int lo = 0, hi = nm;
@@ -600,10 +524,10 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
         out_vals[pos] = m_idx2[r];
         o_key[r + lo] = k;
     }
-    // group heads in the tile's output (the key before it is sb.b_max[j]): counted here, placed by k_heads_place
+    // group heads in the tile's output (compared with the key before it): counted here, placed by k_heads_activate
     if (tid == 0) s_heads = 0;
     __syncthreads();
-    const uint32_t pred = sb.b_max[j];
+    const uint32_t pred = pk_all ? pk_all - 1 : SORT_NOKEY;
     uint32_t h = 0;
     for (int p = tid; p < ns + nm; p += SORT_NT) {
         const uint32_t k = o_key[p];
@@ -615,79 +539,6 @@ static __global__ void __launch_bounds__(SORT_NT) k_sort_merge(const uint32_t* k
     if (lane == 0 && h) atomicAdd(&s_heads, h);
     __syncthreads();
     if (tid == 0) sb.t_heads[j] = s_heads;
-}
-
-// The group heads of each tile's output (sorted positions [t_stay + b_cnt of the tile, of the next tile), compared
-// with the sorted key before), written in order from the tile's offset: the heads of the lower tiles, summed by the
-// CTA itself from the merge's counts. The last tile stores the number of groups.
-static __global__ void __launch_bounds__(SORT_NT) k_heads_place(const uint32_t* keys, SortBufs sb, KeyLayout kl, uint32_t* g_start, uint32_t cap,
-    DevStatus* st)
-{
-    constexpr int RMAX = (SORT_TILE + SORT_MAXM) / SORT_NT;
-    __shared__ uint32_t s_c[RMAX][SORT_NT / 32], s_part[SORT_NT / 32];
-    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (sb.cnt[0] > sb.mcap) return; // FLAG_SORT raised: the substep is repeated with a full sort
-    const int64_t b0 = (int64_t)sb.t_stay[j] + sb.b_cnt[j];
-    const int64_t b1 = j + 1 < sb.tiles ? (int64_t)sb.t_stay[j + 1] + sb.b_cnt[j + 1] : sb.n;
-    if (b1 < b0 || b1 > sb.n) {
-        if (tid == 0) check_failed(st, 9);
-        return;
-    }
-    if (b1 - b0 > (int64_t)RMAX * SORT_NT) return; // a bucket beyond the merge's capacity: the merge raised FLAG_SORT
-    // heads of the lower tiles
-    uint32_t pre = 0;
-    for (int q = tid; q < j; q += SORT_NT) pre += sb.t_heads[q];
-    for (int o = 16; o > 0; o >>= 1) pre += __shfl_down_sync(0xffffffffu, pre, o);
-    if (lane == 0) s_part[w] = pre;
-    // the range's keys and head flags, items (r, w, lane) = b0 + r*256 + w*32 + lane, every load issued first
-    const int R = (int)((b1 - b0 + SORT_NT - 1) / SORT_NT);
-    uint32_t k[RMAX], kl0[RMAX]; // the item's key; for lane 0 also the key before it (another warp's item)
-#pragma unroll
-    for (int r = 0; r < RMAX; r++) {
-        const int64_t p = b0 + r * SORT_NT + tid;
-        const bool in = r < R && p < b1;
-        k[r] = in ? keys[p] : 0u;
-        kl0[r] = (in && lane == 0 && p > 0) ? keys[p - 1] : 0u;
-    }
-    unsigned mine = 0;
-#pragma unroll
-    for (int r = 0; r < RMAX; r++) {
-        if (r >= R) break;
-        const int64_t p = b0 + r * SORT_NT + tid;
-        uint32_t prev = __shfl_up_sync(0xffffffffu, k[r], 1);
-        if (lane == 0) prev = kl0[r];
-        const bool head = p < b1 && (p == 0 || kl.group(k[r]) != kl.group(prev));
-        const unsigned b = __ballot_sync(0xffffffffu, head);
-        if (head) mine |= 1u << r;
-        if (lane == 0) s_c[r][w] = __popc(b);
-    }
-    __syncthreads();
-    if (w == 0) { // exclusive offsets of the (row, warp) counts in order, after the lower tiles' heads
-        uint32_t base = 0;
-        for (int q = 0; q < SORT_NT / 32; q++) base += s_part[q];
-        uint32_t carry = base;
-        for (int r = 0; r < R; r++) {
-            uint32_t c = lane < SORT_NT / 32 ? s_c[r][lane] : 0u, x = c;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            if (lane < SORT_NT / 32) s_c[r][lane] = carry + x - c;
-            carry += __shfl_sync(0xffffffffu, x, 31);
-        }
-        if (lane == 0 && j + 1 == sb.tiles) st->n_groups = carry;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RMAX; r++) {
-        if (r >= R) break;
-        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
-        if ((mine >> r) & 1u) {
-            const uint32_t pos = s_c[r][w] + __popc(b & ((1u << lane) - 1u));
-            if (pos < cap) g_start[pos] = (uint32_t)(b0 + r * SORT_NT + tid);
-            else check_failed(st, 9);
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -785,10 +636,54 @@ static __global__ void __launch_bounds__(SORT_NT) k_group_heads(const uint64_t* 
     }
 }
 
+// Block dl (x*4 + y*2 + z, at +1 block) of the group whose first sorted key is key0, into the block hash; a block
+// seen for the first time takes the next grid slot (one slot counter atomic per group of converged lanes).
+template <class T>
+__device__ __forceinline__ void activate_block(const StepArgs<T>& a, uint64_t key0, uint32_t dl)
+{
+    using L = typename LayoutOf<T>::type;
+    const uint64_t scene = a.kl.scene(key0);
+    uint32_t bi, bj, bk;
+    L::block_of_page(a.kl.page(key0), bi, bj, bk);
+    const uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
+    uint32_t h = (uint32_t)hash64(hk) & a.h_mask;
+    bool done = false, fresh = false;
+    for (int p = 0; p < HASH_PROBES && !done; p++) {
+        const unsigned long long prev = atomicCAS((unsigned long long*)&a.h_keys[h], (unsigned long long)HASH_EMPTY, (unsigned long long)hk);
+        if (prev == HASH_EMPTY)
+            done = fresh = true;
+        else if (prev == hk)
+            done = true;
+        else
+            h = (h + 1) & a.h_mask;
+    }
+    if (!done) raise_flag(a.st, FLAG_CAPACITY);
+    // the entry's slot is written after the probe: nothing reads h_vals before the next kernel (k_nbr)
+    const unsigned am = __activemask();
+    const unsigned nw = __ballot_sync(am, fresh);
+    if (nw) {
+        const int lane = threadIdx.x & 31, leader = __ffs(nw) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&a.st->n_blocks, (uint32_t)__popc(nw));
+        base = __shfl_sync(am, base, leader);
+        if (fresh) {
+            const uint32_t slot = base + (uint32_t)__popc(nw & ((1u << lane) - 1u));
+            if (slot >= a.b_cap) {
+                raise_flag(a.st, FLAG_CAPACITY);
+                a.h_vals[h] = -1;
+            }
+            else {
+                a.h_vals[h] = (int32_t)slot;
+                a.b_key[slot] = hk;
+            }
+        }
+    }
+}
+
+// the blocks of every group (after a full sort and k_group_heads), 8 per group
 template <class T>
 __global__ void k_activate(StepArgs<T> a)
 {
-    using L = typename LayoutOf<T>::type;
     if (aborted(a.st)) return;
     const uint32_t G = a.st->n_groups;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_groups_seen = max(a.st->max_groups_seen, G);
@@ -796,35 +691,101 @@ __global__ void k_activate(StepArgs<T> a)
         if (blockIdx.x == 0 && threadIdx.x == 0) raise_flag(a.st, FLAG_CAPACITY);
         return;
     }
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
-        uint32_t g = t >> 3, dl = t & 7;
-        uint64_t key0 = a.kl.at(a.keys_sorted, a.g_start[g]);
-        uint64_t scene = a.kl.scene(key0);
-        uint32_t bi, bj, bk;
-        L::block_of_page(a.kl.page(key0), bi, bj, bk);
-        uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
-        uint32_t h = (uint32_t)hash64(hk) & a.h_mask;
-        bool done = false;
-        for (int p = 0; p < HASH_PROBES && !done; p++) {
-            unsigned long long prev = atomicCAS((unsigned long long*)&a.h_keys[h], (unsigned long long)HASH_EMPTY, (unsigned long long)hk);
-            if (prev == HASH_EMPTY) {
-                uint32_t slot = atomicAdd(&a.st->n_blocks, 1u);
-                if (slot >= a.b_cap) {
-                    raise_flag(a.st, FLAG_CAPACITY);
-                    a.h_vals[h] = -1;
-                }
-                else {
-                    a.h_vals[h] = (int32_t)slot;
-                    a.b_key[slot] = hk;
-                }
-                done = true;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x)
+        activate_block(a, a.kl.at(a.keys_sorted, a.g_start[t >> 3]), t & 7);
+}
+
+// After the incremental sort's merge, per tile: the group heads of the tile's output (sorted positions
+// [t_base of the tile, of the next tile), each compared with the sorted key before it) written in order into
+// g_start after the heads of the lower tiles (summed by the CTA itself from the merge's counts), then the 8 blocks
+// of each of these groups activated. The last tile stores the number of groups.
+template <class T>
+__global__ void __launch_bounds__(SORT_NT) k_heads_activate(StepArgs<T> a, SortBufs sb, uint32_t* g_start, uint32_t cap)
+{
+    constexpr int RMAX = (SORT_TILE + SORT_MAXM) / SORT_NT;
+    __shared__ uint32_t s_c[RMAX][SORT_NT / 32], s_part[SORT_NT / 32];
+    __shared__ uint32_t s_pos[RMAX * SORT_NT]; // sorted positions of the tile's heads, in order
+    __shared__ uint32_t s_g0, s_nh;
+    if (aborted_cta(a.st)) return; // FLAG_SORT from the merge, or an earlier failure: the substep is repeated
+    const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t* keys = reinterpret_cast<const uint32_t*>(a.keys_sorted); // the incremental sort's keys are 32-bit
+    const int64_t b0 = sb.t_base[j];
+    const int64_t b1 = j + 1 < sb.tiles ? (int64_t)sb.t_base[j + 1] : sb.n;
+    if (b1 < b0 || b1 > sb.n || b1 - b0 > (int64_t)RMAX * SORT_NT) { // the merge's outputs cannot give this range
+        if (tid == 0) check_failed(a.st, 9);
+        return;
+    }
+    // heads of the lower tiles
+    uint32_t pre = 0;
+    for (int q = tid; q < j; q += SORT_NT) pre += sb.t_heads[q];
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_down_sync(0xffffffffu, pre, o);
+    if (lane == 0) s_part[w] = pre;
+    // the range's keys and head flags, items (r, w, lane) = b0 + r*256 + w*32 + lane, every load issued first
+    const int R = (int)((b1 - b0 + SORT_NT - 1) / SORT_NT);
+    uint32_t k[RMAX], kl0[RMAX]; // the item's key; for lane 0 also the key before it (another warp's item)
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        const int64_t p = b0 + r * SORT_NT + tid;
+        const bool in = r < R && p < b1;
+        k[r] = in ? keys[p] : 0u;
+        kl0[r] = (in && lane == 0 && p > 0) ? keys[p - 1] : 0u;
+    }
+    unsigned mine = 0;
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        if (r >= R) break;
+        const int64_t p = b0 + r * SORT_NT + tid;
+        uint32_t prev = __shfl_up_sync(0xffffffffu, k[r], 1);
+        if (lane == 0) prev = kl0[r];
+        const bool head = p < b1 && (p == 0 || a.kl.group(k[r]) != a.kl.group(prev));
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        if (head) mine |= 1u << r;
+        if (lane == 0) s_c[r][w] = __popc(b);
+    }
+    __syncthreads();
+    if (w == 0) { // exclusive offsets of the (row, warp) counts in order, after the lower tiles' heads
+        uint32_t base = 0;
+        for (int q = 0; q < SORT_NT / 32; q++) base += s_part[q];
+        uint32_t carry = base;
+        for (int r = 0; r < R; r++) {
+            uint32_t c = lane < SORT_NT / 32 ? s_c[r][lane] : 0u, x = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
             }
-            else if (prev == hk)
-                done = true;
-            else
-                h = (h + 1) & a.h_mask;
+            if (lane < SORT_NT / 32) s_c[r][lane] = carry + x - c;
+            carry += __shfl_sync(0xffffffffu, x, 31);
         }
-        if (!done) raise_flag(a.st, FLAG_CAPACITY);
+        if (lane == 0) {
+            s_g0 = base;
+            s_nh = carry - base;
+            if (j + 1 == sb.tiles) {
+                a.st->n_groups = carry;
+                a.st->max_groups_seen = max(a.st->max_groups_seen, carry);
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t g0 = s_g0;
+#pragma unroll
+    for (int r = 0; r < RMAX; r++) {
+        if (r >= R) break;
+        const unsigned b = __ballot_sync(0xffffffffu, (mine >> r) & 1u);
+        if ((mine >> r) & 1u) {
+            const uint32_t pos = s_c[r][w] + __popc(b & ((1u << lane) - 1u)), p = (uint32_t)(b0 + r * SORT_NT + tid);
+            s_pos[pos - g0] = p; // pos - g0 < the tile's item count <= RMAX * SORT_NT
+            if (pos < cap) g_start[pos] = p;
+            else check_failed(a.st, 9);
+        }
+    }
+    __syncthreads();
+    const uint32_t nh = s_nh;
+    for (uint32_t t = tid; t < nh * 8; t += SORT_NT) {
+        if (g0 + (t >> 3) >= a.b_cap) { // more groups than grid blocks: the host grows the grid and repeats the substep
+            raise_flag(a.st, FLAG_CAPACITY);
+            continue;
+        }
+        activate_block(a, (uint64_t)keys[s_pos[t >> 3]], t & 7);
     }
 }
 
@@ -836,6 +797,8 @@ template <class T>
 __global__ void k_nbr(StepArgs<T> a)
 {
     using L = typename LayoutOf<T>::type;
+    if (blockIdx.x == 0) // the per-scene grid mass k_grid accumulates
+        for (int s = threadIdx.x; s < a.n_scenes; s += blockDim.x) a.grid_mass[s] = 0;
     if (aborted(a.st)) return;
     const uint32_t G = a.st->n_groups;
     if (G > a.b_cap) return; // activation already raised FLAG_CAPACITY
@@ -2755,12 +2718,6 @@ __global__ void k_step_end(SceneParams<T>* scenes, int n_scenes, DevStatus* st)
         st->work_g2p = 0;
         st->work_dmg = 0;
     }
-}
-
-template <class T>
-__global__ void k_zero_grid_mass(double* gm, int n)
-{
-    for (int s = threadIdx.x; s < n; s += blockDim.x) gm[s] = 0;
 }
 
 // ---------------------------------------------------------------------------------------------------
