@@ -731,6 +731,7 @@ private:
     int occ_stress_[4] = { 1, 1, 1, 1 }, occ_scatter_[3] = { 1, 1, 1 }, occ_g2p_[4][3] = { { 1, 1, 1 }, { 1, 1, 1 }, { 1, 1, 1 }, { 1, 1, 1 } };
     int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [fused variant][model set]
     int occ_ws_[4] = { 1, 1, 1, 1 }; // warp-specialised P2G, per model set
+    int occ_grid_ = 1; // grid update CTAs per SM
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
     bool implicit_ = false; // some scene solves its damage implicitly
@@ -988,6 +989,8 @@ private:
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[1], k_stress<T, 2>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[2], k_stress<T, 4>, 256, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_stress_[3], k_stress<T, 7>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_grid_, k_grid<T>, GRID_NT, 0);
+        occ_grid_ = std::max(1, occ_grid_);
         g2p_setup<0, 0>();
         g2p_setup<0, 1>();
         g2p_setup<0, 2>();
@@ -1180,7 +1183,7 @@ private:
                 launch_scatter<2>(a, sctas);
         }
         if (ev) ZR_CUDA(cudaEventRecord(ev[3], stream_));
-        k_grid<T><<<nsm_ * 8, GRID_NT, 0, stream_>>>(a);
+        k_grid<T><<<nsm_ * occ_grid_, GRID_NT, 0, stream_>>>(a); // one resident wave, striding over the blocks
         if (implicit_) {
             int rc = enqueue_damage_solve(a);
             if (rc) return rc;
