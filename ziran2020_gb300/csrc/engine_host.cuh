@@ -754,6 +754,7 @@ private:
     // writes, aborts and autotuner trials: the next substep sorts in full)
     bool sort_base_stale_ = true;
     bool inc_sort_on_ = true; // ZR_SORT=full turns the incremental sort off
+    bool prefetch_ = true; // P2G's L2 prefetch of the groups ahead (ZR_PREFETCH=0 turns it off)
     static constexpr int64_t MCAP_MIN = 4096;
     // the sort's tile arrays (stayer bits, per-tile counts and keys, bucket counts, group-head look-back words);
     // the movers' list, buckets and tickets, and their keys and storage indices grouped by bucket
@@ -1011,6 +1012,7 @@ private:
         sched_.tuned = 0;
         if (const char* e = std::getenv("ZR_AUTOTUNE")) autotune_mode_ = std::atoi(e);
         if (const char* e = std::getenv("ZR_SORT")) inc_sort_on_ = std::string(e) != "full";
+        if (const char* e = std::getenv("ZR_PREFETCH")) prefetch_ = std::atoi(e) != 0;
     }
 
     int alloc(void** p, size_t bytes)
@@ -1132,6 +1134,7 @@ private:
         a.n_total = N_;
         a.b_cap = b_cap_;
         a.n_scenes = n_scenes();
+        a.opts = prefetch_ ? OPT_PREFETCH : 0u;
         a.kl = kl_;
         return a;
     }

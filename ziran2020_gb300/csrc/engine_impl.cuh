@@ -110,8 +110,11 @@ struct StepArgs {
     uint32_t n_total;
     uint32_t b_cap;
     int n_scenes;
+    uint32_t opts; // OPT_* bits
     KeyLayout kl;
 };
+// OPT_PREFETCH: P2G prefetches the state of the groups ahead into L2
+enum : uint32_t { OPT_PREFETCH = 1u };
 
 __host__ __device__ inline uint64_t hash64(uint64_t k)
 {
@@ -1436,6 +1439,17 @@ struct FusedShape {
     static constexpr size_t dyn_bytes = sizeof(T) * Y_CELL * CPAD; // fields Y_F..Y_D
 };
 
+// Elements [lo, hi] of one array, prefetched into L2 (widened to 16-byte boundaries, kept inside [base, end)).
+template <class E>
+__device__ __forceinline__ void prefetch_l2_range(const E* arr, int64_t lo, int64_t hi, const void* base, const void* end)
+{
+    uintptr_t b0 = (uintptr_t)(arr + lo) & ~(uintptr_t)15, b1 = ((uintptr_t)(arr + hi + 1) + 15) & ~(uintptr_t)15;
+    const uintptr_t lo_lim = ((uintptr_t)base + 15) & ~(uintptr_t)15, hi_lim = (uintptr_t)end & ~(uintptr_t)15;
+    b0 = b0 < lo_lim ? lo_lim : b0;
+    b1 = b1 > hi_lim ? hi_lim : b1;
+    if (b1 > b0) bulk_prefetch_l2((const void*)b0, (uint32_t)(b1 - b0));
+}
+
 // MINB: CTAs per SM the register budget is cut for (more CTAs hide more load latency; fewer registers may spill)
 template <class T, int MODELS, int MINB, int CH = FusedShape<T>::CHUNK>
 __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepArgs<T> a)
@@ -1484,6 +1498,19 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
         const bool bad = s_bad != 0;
         const SceneParams<T>& sp = a.scenes[s_scene];
         const int nf = sp.damage ? NACC : 4;
+        // The state of the group one round of claims ahead (whichever CTA takes it) is prefetched into L2 while this
+        // group runs, so that its phase 1 reads L2: the lanes of warp 1 take one array each (state fields P_X .. P_D
+        // and the particle ids). Its storage range is that of its first and last sorted particles (storage keeps the
+        // previous substep's sorted order; a range that does not look like one group is skipped). The loads are
+        // spread over the group so that none of them is waited for.
+        constexpr int NPF = P_D + 2;
+        const int gpf = g + (int)gridDim.x, pfl = tid - 32;
+        const bool pf = (a.opts & OPT_PREFETCH) && pfl >= 0 && pfl < NPF && gpf < (int)G;
+        uint32_t pf_a = 0, pf_b = 0, pf_j0 = 0, pf_j1 = 0;
+        if (pf) {
+            pf_a = a.g_start[gpf];
+            pf_b = gpf + 1 < (int)G ? a.g_start[gpf + 1] : a.n_total;
+        }
         for (uint32_t c0 = start; c0 < end && !bad; c0 += CHUNK) {
             const int cnt = (int)min((uint32_t)CHUNK, end - c0);
             // ---- phase 1: per particle
@@ -1526,7 +1553,18 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
             add_to_offset_tile<T, L>(acc, tile, cx, cy, cz, ii, nf); // all lanes (an empty cell adds zeros)
             __syncthreads();
         }
+        if (pf && pf_b > pf_a && pf_b <= a.n_total) {
+            pf_j0 = a.vals_sorted[pf_a];
+            pf_j1 = a.vals_sorted[pf_b - 1];
+        }
         if (!bad) flush_offset_tiles<T, L>(a, tile, s_nbr, nf, tid, NT);
+        if (pf && pf_j1 >= pf_j0 && pf_j1 - pf_j0 < 2 * (pf_b - pf_a) + 64) {
+            const Pool<T>& P = a.pin;
+            if (pfl < NPF - 1)
+                prefetch_l2_range(P.f + (int64_t)pfl * P.stride, pf_j0, pf_j1, P.f, P.f + (int64_t)P_NF * P.stride);
+            else
+                prefetch_l2_range(P.pid, pf_j0, pf_j1, P.pid, P.pid + P.stride);
+        }
         __syncthreads();
     }
     if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);

@@ -66,6 +66,13 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint3
                  : "memory");
 }
 
+// L2 prefetch of `bytes` at src by the bulk-copy engine (src 16-byte aligned, bytes a multiple of 16); a hint, it
+// completes on its own and nothing waits for it
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // one element global -> shared without a register round trip (sm_80+ asynchronous copy; BYTES 4, 8 or 16,
 // both addresses aligned to BYTES); complete once cp_async_wait_all returns in the issuing thread. G2P stages
 // the next particle's state this way while it computes the current one.
