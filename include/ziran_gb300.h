@@ -129,6 +129,16 @@ int zr_scene_set_state(zr_scene* s, const void* in, int dtype);
  * no counterpart (its state never leaves host memory); it replaces a writeState/readState pair
  * (MpmSimulationBase.cpp:1060-1114) between two scenes that share one device. */
 int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype);
+/* nsteps independent jobs through the scene: job i sets the state from in[i] (as zr_scene_set_state), advances one
+ * substep and writes the result to out[i] (as zr_scene_get_state); all buffers hold count x 25 values of dtype.
+ * The host-to-device copies of the next inputs and the device-to-host copies of the last results run on the copy
+ * engines while the GPU computes (pinned buffers give the overlap; the buffers stay in use until the call
+ * returns). A job that fails (a substep that aborts, a position outside the domain) is run again as
+ * zr_scene_set_state, zr_scene_step and zr_scene_get_state would run it, with the same retries; if it still fails,
+ * the error code is returned, the results of the earlier jobs are written, the state is that of the failing job
+ * and the later output buffers hold unspecified values. The reference has no counterpart (one scene per process, frames written to files); it serves a
+ * pipeline that runs many independent states (ensembles, parameter sweeps, a host-side coupler) through one GPU. */
+int zr_scene_step_stream(zr_scene* s, int nsteps, const void* const* in, void* const* out, int dtype);
 /* FP64-accumulated reductions (MpmSimulationDataAnalysis.h:67-151): total mass, momentum x/y/z, kinetic
  * energy, max particle speed, grid mass of the last substep. */
 int zr_scene_reductions(zr_scene* s, double out[7]);

@@ -56,3 +56,82 @@ def test_exchange_refuses_overlapping_buffers():
         s.exchange_state(a, a)
     with pytest.raises(ValueError):
         s.exchange_state(a, np.zeros((s.count, 25), np.float64))
+
+
+@pytest.mark.parametrize("prec", [zr.F32, zr.F64])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_stream_equals_set_step_get(prec, pinned):
+    """Four jobs with different input states: each result equals zr_scene_set_state, one substep and
+    zr_scene_get_state run one after the other (up to the order of the atomic grid sums)."""
+    dtype = np.float32 if prec == zr.F32 else np.float64
+    d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(20.0, 2.0), pull=1.0)
+    src = scenes.gpu_scene(d, prec)
+    n = src.count
+    states = []
+    for k in range(4):
+        src.step(2)
+        states.append(src.get_state(np.zeros((n, 25), dtype)))
+    ins = [_buf(n, dtype, pinned) for _ in range(4)]
+    outs = [_buf(n, dtype, pinned) for _ in range(4)]
+    for a, st in zip(ins, states):
+        a[:] = st
+    s = scenes.gpu_scene(d, prec)
+    s.step_stream(ins, outs)
+    ref = scenes.gpu_scene(d, prec)
+    tol = 1e-12 if prec == zr.F64 else 1e-5
+    for a, o in zip(ins, outs):
+        ref.set_state(a)
+        ref.step(1)
+        want = ref.get_state(np.zeros((n, 25), dtype))
+        assert np.abs(o[:, :3] - want[:, :3]).max() < tol  # positions
+        assert np.abs(o - want).max() < (1e-9 if prec == zr.F64 else 2e-3)  # every field (F, C carry the sum order more)
+    # the scene holds the last job's result
+    assert np.abs(s.get_state(np.zeros((n, 25), dtype)) - outs[-1]).max() == 0
+
+
+def test_step_stream_stops_at_a_failing_job():
+    """A job whose input leaves the domain fails; the earlier results are written, the error is reported and the
+    scene holds the failing job's input."""
+    d = scenes.elastic_box(size=0.0625)
+    s = scenes.gpu_scene(d, zr.F32)
+    n = s.count
+    good = s.get_state(np.zeros((n, 25), np.float32))
+    bad = good.copy()
+    bad[:, 0] += 2.0  # positions past the domain
+    ins = [_buf(n, np.float32, True) for _ in range(3)]
+    outs = [_buf(n, np.float32, True) for _ in range(3)]
+    ins[0][:] = good
+    ins[1][:] = bad
+    ins[2][:] = good
+    with pytest.raises(Exception):
+        s.step_stream(ins, outs)
+    assert np.abs(outs[0][:, :3] - good[:, :3]).max() < 1e-2  # the first job ran
+    assert 0 < np.abs(outs[0] - good).max()
+    assert np.array_equal(s.get_state(np.zeros((n, 25), np.float32)), bad)
+
+
+@pytest.mark.parametrize("bad_job", [2, 5])
+def test_step_stream_recovers_the_jobs_after_a_failure_inside_the_pipeline(bad_job):
+    """Jobs after the first run without a host check between them; a job whose substep aborts (a particle pushed
+    more than a cell in one substep) makes the later ones run again the safe way. Every job before the failing one
+    matches the one-by-one result, and the failure is reported."""
+    d = scenes.elastic_box(size=0.0625)
+    s = scenes.gpu_scene(d, zr.F64)
+    n = s.count
+    good = s.get_state(np.zeros((n, 25)))
+    ref = scenes.gpu_scene(d, zr.F64)
+    want = []
+    for k in range(6):
+        ref.set_state(good)
+        ref.step(1)
+        want.append(ref.get_state(np.zeros((n, 25))))
+    fast = good.copy()
+    fast[:, 4] = -300.0  # v_y: 3e-2 per substep, more than a cell of 1/64
+    ins = [_buf(n, np.float64, True) for _ in range(6)]
+    outs = [_buf(n, np.float64, True) for _ in range(6)]
+    for k in range(6):
+        ins[k][:] = fast if k == bad_job else good
+    with pytest.raises(Exception):
+        s.step_stream(ins, outs)
+    for k in range(bad_job):
+        assert np.abs(outs[k] - want[k]).max() < 1e-9, k

@@ -81,6 +81,7 @@ def load_library(build_if_needed=True):
         "zr_scene_get_state": (i32, [vp, vp, i32]),
         "zr_scene_set_state": (i32, [vp, vp, i32]),
         "zr_scene_exchange_state": (i32, [vp, vp, vp, i32]),
+        "zr_scene_step_stream": (i32, [vp, i32, vp, vp, i32]),
         "zr_scene_reductions": (i32, [vp, pd]),
         "zr_scene_set_dt": (i32, [vp, d]),
         "zr_scene_set_implicit_damage": (i32, [vp, i32]),
@@ -304,6 +305,24 @@ class Scene:
         dt = F32 if a.dtype == np.float32 else F64
         self._check(self.L.zr_scene_exchange_state(self.h, a.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p), dt))
         return out
+
+    def step_stream(self, inputs, outputs):
+        """len(inputs) independent jobs: job i sets the state from inputs[i], advances one substep and writes the result
+        to outputs[i] (count x 25 arrays of one dtype); copies of the next inputs and the last results overlap the
+        computation (pinned arrays give the overlap)."""
+        n = len(inputs)
+        if len(outputs) != n:
+            raise ValueError("step_stream: as many outputs as inputs")
+        if n == 0:
+            return outputs
+        dtype = inputs[0].dtype
+        for b in list(inputs) + list(outputs):
+            if b.dtype != dtype or b.size != self.count * 25 or not b.flags.c_contiguous:
+                raise ValueError("step_stream: buffers of count x 25 contiguous values of one dtype expected")
+        pin = (C.c_void_p * n)(*[b.ctypes.data for b in inputs])
+        pout = (C.c_void_p * n)(*[b.ctypes.data for b in outputs])
+        self._check(self.L.zr_scene_step_stream(self.h, n, C.cast(pin, C.c_void_p), C.cast(pout, C.c_void_p), F32 if dtype == np.float32 else F64))
+        return outputs
 
     def reductions(self):
         out = np.zeros(7)

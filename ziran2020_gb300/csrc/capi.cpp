@@ -483,6 +483,15 @@ int zr_scene_set_state(zr_scene* s, const void* in, int dtype)
     return rc;
 }
 
+int zr_scene_step_stream(zr_scene* s, int nsteps, const void* const* in, void* const* out, int dtype)
+{
+    NEED_ENGINE(s);
+    if (nsteps < 0 || (nsteps > 0 && (!in || !out)) || (dtype != ZR_F32 && dtype != ZR_F64)) return ZR_ERR_ARG;
+    int rc = s->eng->stream_steps(0, nsteps, in, out, dtype == ZR_F32);
+    if (rc) s->err = s->eng->last_error();
+    return rc;
+}
+
 int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype)
 {
     NEED_ENGINE(s);

@@ -104,6 +104,9 @@ public:
     // get_state into out25, then set_state from in25 (disjoint buffers of one precision); with both in pinned host
     // memory one kernel moves the two directions over the host link at the same time.
     virtual int exchange_state(int scene, const void* in25, void* out25, int is_f32) = 0;
+    // nsteps jobs, each: set_state(in25[i]), one substep, get_state(out25[i]); the host copies of the next inputs and
+    // the last outputs run on copy engines while the GPU computes (the buffers stay in use until the call returns)
+    virtual int stream_steps(int scene, int nsteps, const void* const* in25, void* const* out25, int is_f32) = 0;
     // FP64-accumulated reductions: mass, momentum(3), kinetic energy, max speed, grid mass
     virtual int reductions(int scene, double* out7) = 0;
     virtual int set_dt(int scene, double dt) = 0;

@@ -495,6 +495,129 @@ public:
         return rekey();
     }
 
+    // Pipelined jobs. Job 0 runs the safe way (set_state, step, get_state: it tunes the schedule, builds the one-substep
+    // graphs and leaves a valid sort base). Jobs 1.. run without a host check between them: input i is copied host ->
+    // device (copy engine, stream h2d_) into one of two device slots two jobs ahead, imported by a kernel, keyed, stepped
+    // by the one-substep graph, exported into one of two output slots and copied device -> host (stream d2h_) while the
+    // next jobs compute. The status is read once at the end; the status flags accumulate, so after the first aborted
+    // job every later substep returns at once, and the jobs from the aborted one on are run again the safe way (its
+    // retries and errors are those of step()). Events order slot reuse: 0-1 input copied, 2-3 input imported, 4-5
+    // output exported, 6-7 output copied.
+    int stream_steps(int s, int nsteps, const void* const* in, void* const* out, int f32) override
+    {
+        if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
+        if (nsteps < 0 || (nsteps > 0 && (!in || !out))) return arg("stream_steps: bad step count or buffer lists");
+        for (int i = 0; i < nsteps; i++)
+            if (!in[i] || !out[i]) return arg("stream_steps: a null buffer");
+        const RowFields rf = state_fields();
+        const size_t bytes = (size_t)h_scenes_[s].count * rf.W * (f32 ? 4 : 8);
+        auto safe_job = [&](int i) -> int {
+            int rc = set_state(s, in[i], f32);
+            StepReport r;
+            if (!rc) rc = step(1, &r);
+            if (!rc) rc = get_state(s, out[i], f32);
+            return rc;
+        };
+        if (nsteps <= 1 || timing_ || !graphs_on_) {
+            for (int i = 0; i < nsteps; i++)
+                if (int rc = safe_job(i)) return rc;
+            return 0;
+        }
+        int rc = ensure_io(bytes);
+        if (rc) return rc;
+        auto issue_in = [&](int i) -> cudaError_t {
+            const int b = i & 1;
+            cudaError_t e = cudaStreamWaitEvent(h2d_, io_ev_[2 + b], 0); // the slot's previous input was imported
+            if (e == cudaSuccess) e = cudaMemcpyAsync(io_in_[b], in[i], bytes, cudaMemcpyHostToDevice, h2d_);
+            if (e == cudaSuccess) e = cudaEventRecord(io_ev_[b], h2d_);
+            return e;
+        };
+        // the caller's buffers are in use until every copy has finished, also after a failure
+        auto drain = [&]() -> cudaError_t {
+            const cudaError_t e1 = cudaStreamSynchronize(h2d_), e2 = cudaStreamSynchronize(d2h_), e3 = cudaStreamSynchronize(stream_);
+            return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+        };
+        cudaError_t e = issue_in(1);
+        if (e != cudaSuccess) {
+            drain();
+            return cuda_fail(e);
+        }
+        rc = safe_job(0);
+        if (!rc && nsteps > 2 && (e = issue_in(2)) != cudaSuccess) rc = cuda_fail(e);
+        if (!rc) rc = prepare_graphs(1);
+        if (rc) {
+            drain();
+            return rc;
+        }
+        const int cur1 = cur_; // the parity job 1 reads
+        e = cudaMemsetAsync(st_, 0, sizeof(DevStatus), stream_);
+        for (int i = 1; i < nsteps && e == cudaSuccess && !rc; i++) {
+            const int b = i & 1;
+            if ((e = cudaStreamWaitEvent(stream_, io_ev_[b], 0)) != cudaSuccess) break;
+            if ((rc = fill_inv(s)) || (rc = launch_rows<ROWS_IMPORT>(s, rf, io_in_[b], nullptr, f32))) break;
+            if ((e = cudaEventRecord(io_ev_[2 + b], stream_)) != cudaSuccess) break;
+            k_keys<T><<<nsm_ * 4, 256, 0, stream_>>>(pool(cur_), d_scenes_, n_scenes(), keys_in_, N_, kl_, st_); // raises FLAG_OUT_OF_DOMAIN
+            forget_drive(s);
+            if ((rc = refresh_drive())) break;
+            if (i + 2 < nsteps && (e = issue_in(i + 2)) != cudaSuccess) break;
+            if ((e = cudaGraphLaunch(g1_[cur_ & 1], stream_)) != cudaSuccess) break;
+            cur_ ^= 1;
+            if ((e = cudaStreamWaitEvent(stream_, io_ev_[6 + b], 0)) != cudaSuccess) break; // the slot's previous output was copied
+            if ((rc = fill_inv(s)) || (rc = launch_rows<ROWS_EXPORT>(s, rf, nullptr, io_out_[b], f32))) break;
+            if ((e = cudaEventRecord(io_ev_[4 + b], stream_)) != cudaSuccess || (e = cudaStreamWaitEvent(d2h_, io_ev_[4 + b], 0)) != cudaSuccess
+                || (e = cudaMemcpyAsync(out[i], io_out_[b], bytes, cudaMemcpyDeviceToHost, d2h_)) != cudaSuccess
+                || (e = cudaEventRecord(io_ev_[6 + b], d2h_)) != cudaSuccess)
+                break;
+        }
+        const cudaError_t ed = drain();
+        if (!rc && e != cudaSuccess) rc = cuda_fail(e);
+        if (!rc && ed != cudaSuccess) rc = cuda_fail(ed);
+        if (rc) return rc;
+        ZR_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        sorted_storage_ = true;
+        if (!(hst_->flags & FLAG_ABORT)) return 0;
+        // job k aborted (substeps are counted from job 1): its input pool (parity) was intact when it started; the later
+        // jobs' imports and the aborted substep may have left partial grid sums, hash entries and a broken sort base
+        const int k = 1 + std::max(0, (int)hst_->abort_step);
+        cur_ = (cur1 + k - 1) & 1;
+        sort_base_stale_ = true;
+        sorted_storage_ = false;
+        ZR_CUDA(cudaMemsetAsync(acc_, 0, sizeof(T) * (size_t)b_cap_ * NACC * L::nodes, stream_));
+        ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
+        if (cg_) ZR_CUDA(cudaMemsetAsync(cg_, 0, sizeof(T) * CG_NF * (size_t)b_cap_ * L::nodes, stream_));
+        ZR_CUDA(cudaStreamSynchronize(stream_));
+        for (int i = k; i < nsteps; i++)
+            if ((rc = safe_job(i))) return rc;
+        return 0;
+    }
+    int ensure_io(size_t bytes)
+    {
+        if (!h2d_) {
+            if (cudaStreamCreateWithFlags(&h2d_, cudaStreamNonBlocking) != cudaSuccess || cudaStreamCreateWithFlags(&d2h_, cudaStreamNonBlocking) != cudaSuccess)
+                return fail(ZR_ERR_CUDA_, "copy stream creation failed");
+            for (auto& ev : io_ev_)
+                if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(ZR_ERR_CUDA_, "event creation failed");
+        }
+        if (bytes <= io_bytes_) return 0;
+        ZR_CUDA(cudaStreamSynchronize(h2d_));
+        ZR_CUDA(cudaStreamSynchronize(d2h_));
+        free_io();
+        for (int b = 0; b < 2; b++)
+            if (alloc(&io_in_[b], bytes) || alloc(&io_out_[b], bytes)) return ZR_ERR_CUDA_;
+        io_bytes_ = bytes;
+        return 0;
+    }
+    void free_io()
+    {
+        for (int b = 0; b < 2; b++) {
+            dfree(io_in_[b]);
+            dfree(io_out_[b]);
+            io_in_[b] = io_out_[b] = nullptr;
+        }
+        io_bytes_ = 0;
+    }
+
     int reductions(int s, double* out7) override
     {
         if (s < 0 || s >= n_scenes()) return arg("scene index out of range");
@@ -739,6 +862,12 @@ private:
     T* cg_ = nullptr; // the damage solve's node vectors (CG_NF x b_cap_ blocks), allocated when implicit_
     CgScalars* cgs_ = nullptr; // per scene (scene_cap_)
     cudaStream_t side_ = nullptr; // captures the damage solve's loop body
+    // stream_steps: two device slots for inputs and two for outputs, the copy streams and their events
+    void* io_in_[2] = { nullptr, nullptr };
+    void* io_out_[2] = { nullptr, nullptr };
+    size_t io_bytes_ = 0;
+    cudaStream_t h2d_ = nullptr, d2h_ = nullptr;
+    cudaEvent_t io_ev_[8] = {};
     cudaGraphExec_t cg_exec_ = nullptr; // the damage solve's loop alone, for substeps launched outside graphs
     int occ_dmg_[2] = { 1, 1 };
     uint32_t* inv_ = nullptr; // storage slot of each particle of a scene in the caller's order (row transfers)
@@ -1026,6 +1155,11 @@ private:
         }
         dev_bytes_ += (int64_t)bytes;
         return 0;
+    }
+    int cuda_fail(cudaError_t e)
+    {
+        err_ = std::string("CUDA error: ") + cudaGetErrorString(e);
+        return ZR_ERR_CUDA_;
     }
     void dfree(void*& p)
     {
@@ -1638,6 +1772,9 @@ private:
     void release_batch()
     {
         drop_graphs();
+        if (h2d_) cudaStreamSynchronize(h2d_);
+        if (d2h_) cudaStreamSynchronize(d2h_);
+        free_io();
         void* ps[] = { pool_[0], pool_[1], pid_[0], pid_[1], keys_in_, keys_sorted_, iota_, vals_sorted_, g_start_, g_nbr_, b_key_, acc_, vel_, h_keys_, h_vals_,
             d_scenes_, grid_mass_, st_, sort_tmp_, stage_, pay_, scenes_backup_, ck_pool_, ck_pid_, ck_scenes_, cg_, cgs_,
             sort_aux_, inc_move_, inc_bkey_, inc_bidx_, inv_ };
@@ -1697,6 +1834,12 @@ private:
         stream_ = nullptr;
         if (side_) cudaStreamDestroy(side_);
         side_ = nullptr;
+        for (auto& ev : io_ev_)
+            if (ev) cudaEventDestroy(ev);
+        for (auto& ev : io_ev_) ev = nullptr;
+        if (h2d_) cudaStreamDestroy(h2d_);
+        if (d2h_) cudaStreamDestroy(d2h_);
+        h2d_ = d2h_ = nullptr;
     }
 };
 
