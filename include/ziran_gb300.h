@@ -131,6 +131,7 @@ int zr_scene_set_state(zr_scene* s, const void* in, int dtype);
 int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype);
 /* nsteps independent jobs through the scene: job i sets the state from in[i] (as zr_scene_set_state), advances one
  * substep and writes the result to out[i] (as zr_scene_get_state); all buffers hold count x 25 values of dtype.
+ * out[i] may be in[i], but no output may overlap the input of a later job (ZR_ERR_ARG).
  * The host-to-device copies of the next inputs and the device-to-host copies of the last results run on the copy
  * engines while the GPU computes (pinned buffers give the overlap; the buffers stay in use until the call
  * returns). A job that fails (a substep that aborts, a position outside the domain) is run again as

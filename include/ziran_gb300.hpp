@@ -192,6 +192,17 @@ public:
         return restarts;
     }
     int64_t particleCount() const { return zr_scene_count(h_); }
+    // The dynamic state (x, v, C, F, d: 25 values per particle in T) in and out, and jobs of one substep each
+    // (state in, substep, result out) pipelined with their host copies; buffers of particleCount() * 25 values
+    void getState(T* out) { check(zr_scene_get_state(h_, out, sizeof(T) == 4 ? ZR_F32 : ZR_F64)); }
+    void setState(const T* in) { check(zr_scene_set_state(h_, in, sizeof(T) == 4 ? ZR_F32 : ZR_F64)); }
+    void stepJobs(const std::vector<const T*>& in, const std::vector<T*>& out)
+    {
+        if (in.size() != out.size()) throw std::invalid_argument("ziran_gb300: stepJobs needs one output per input");
+        push_params();
+        check(zr_scene_step_stream(h_, (int)in.size(), reinterpret_cast<const void* const*>(in.data()), reinterpret_cast<void* const*>(out.data()),
+            sizeof(T) == 4 ? ZR_F32 : ZR_F64));
+    }
     // conjugate-gradient iterations of the last substep's implicit damage solve
     int cgIterations() const
     {

@@ -135,3 +135,15 @@ def test_step_stream_recovers_the_jobs_after_a_failure_inside_the_pipeline(bad_j
         s.step_stream(ins, outs)
     for k in range(bad_job):
         assert np.abs(outs[k] - want[k]).max() < 1e-9, k
+
+
+def test_step_stream_refuses_an_output_that_is_a_later_input():
+    d = scenes.elastic_box(size=0.0625)
+    s = scenes.gpu_scene(d, zr.F32)
+    a = _buf(s.count, np.float32, True)
+    b = _buf(s.count, np.float32, True)
+    s.get_state(a)
+    b[:] = a
+    with pytest.raises(Exception):
+        s.step_stream([a, b], [b, a])  # job 0 would write the input of job 1
+    s.step_stream([a, b], [a, b])  # in place is fine

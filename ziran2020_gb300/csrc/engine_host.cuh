@@ -511,6 +511,12 @@ public:
             if (!in[i] || !out[i]) return arg("stream_steps: a null buffer");
         const RowFields rf = state_fields();
         const size_t bytes = (size_t)h_scenes_[s].count * rf.W * (f32 ? 4 : 8);
+        // a later job's input is copied while earlier results are written: no output may overlap a later input
+        for (int i = 0; i < nsteps; i++)
+            for (int j = i + 1; j < nsteps; j++) {
+                const char *o = (const char*)out[i], *q = (const char*)in[j];
+                if (bytes && o < q + bytes && q < o + bytes) return arg("stream_steps: an output overlaps the input of a later job");
+            }
         auto safe_job = [&](int i) -> int {
             int rc = set_state(s, in[i], f32);
             StepReport r;
