@@ -1461,42 +1461,64 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
     T* pay = reinterpret_cast<T*>(fused_dyn);
     __shared__ T tile[OffsetTiles<L>::ELEMS]; // one node tile per stencil x-offset
     __shared__ uint8_t cellof[CHUNK];
-    __shared__ int s_g, s_scene, s_bad;
-    __shared__ int32_t s_nbr[8];
-    __shared__ int s_org[3];
+    // the set-up of the current group (buffer b) and of the next one (b ^ 1): group, scene, a bad neighbour slot,
+    // the grid slots of the block and its +1 neighbours, the block origin, the sorted range
+    __shared__ int s_g[2], s_scene[2], s_bad[2];
+    __shared__ int32_t s_nbr[2][8];
+    __shared__ int s_org[2][3];
+    __shared__ uint32_t s_se[2][2];
     if (aborted_cta(a.st)) return;
     const uint32_t G = a.st->n_groups;
     const int tid = threadIdx.x;
+    // Groups are claimed one ahead: warp 0 claims the next group at the start of a group; around the group's flush
+    // lanes 0-7 load its range and neighbour slots (lane 0 also the key of its first particle) and write them into
+    // the other buffer before the group's last barrier, so no barrier waits on a claim alone.
+    auto claim = [&]() { // warp 0 only: the next group index, in every lane
+        int v = 0;
+        if (tid == 0) v = (int)atomicAdd(&a.st->work_p2g, 1u);
+        return __shfl_sync(0xffffffffu, v, 0);
+    };
+    auto setup_store = [&](int bb, int gn, uint32_t st, uint32_t en, int32_t slot, uint64_t key0) { // lanes 0-7 of warp 0
+        const unsigned badm = __ballot_sync(0xffu, slot < 0 || (uint32_t)slot >= a.b_cap); // a failed lookup raised FLAG_CAPACITY
+        s_nbr[bb][tid] = slot;
+        if (tid == 0) {
+            uint32_t bi, bj, bk;
+            L::block_of_page(a.kl.page(key0), bi, bj, bk);
+            s_g[bb] = gn;
+            s_bad[bb] = badm != 0;
+            s_scene[bb] = (int)a.kl.scene(key0);
+            s_org[bb][0] = (int)(bi * L::sx);
+            s_org[bb][1] = (int)(bj * L::sy);
+            s_org[bb][2] = (int)(bk * L::sz);
+            s_se[bb][0] = st;
+            s_se[bb][1] = en;
+        }
+    };
     const int ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
     for (int q = tid; q < OffsetTiles<L>::ELEMS; q += NT) tile[q] = (T)0;
     uint32_t fallbacks = 0;
-    for (;;) {
-        if (tid == 0) {
-            s_g = (int)atomicAdd(&a.st->work_p2g, 1u);
-            s_bad = 0;
-        }
-        __syncthreads();
-        const int g = s_g;
-        if (g >= (int)G) break;
-        const uint32_t start = a.g_start[g], end = (g + 1 < (int)G) ? a.g_start[g + 1] : a.n_total;
-        if (tid < 8) {
-            const int slot = a.g_nbr[g * 8 + tid];
-            s_nbr[tid] = slot;
-            if (slot < 0 || (uint32_t)slot >= a.b_cap) s_bad = 1; // a failed lookup already raised FLAG_CAPACITY
-            if (tid == 0) {
-                const uint64_t key0 = a.kl.at(a.keys_sorted, start);
-                uint32_t bi, bj, bk;
-                L::block_of_page(a.kl.page(key0), bi, bj, bk);
-                s_scene = (int)a.kl.scene(key0);
-                s_org[0] = (int)(bi * L::sx);
-                s_org[1] = (int)(bj * L::sy);
-                s_org[2] = (int)(bk * L::sz);
+    if (tid < 32) { // the first group
+        const int g0 = claim();
+        if (g0 < (int)G) {
+            if (tid < 8) {
+                const uint32_t st = a.g_start[g0], en = g0 + 1 < (int)G ? a.g_start[g0 + 1] : a.n_total;
+                setup_store(0, g0, st, en, a.g_nbr[g0 * 8 + tid], tid == 0 ? a.kl.at(a.keys_sorted, st) : 0ull);
             }
         }
-        __syncthreads();
-        const bool bad = s_bad != 0;
-        const SceneParams<T>& sp = a.scenes[s_scene];
+        else if (tid == 0)
+            s_g[0] = g0;
+    }
+    __syncthreads();
+    int bcur = 0;
+    for (;;) {
+        const int g = s_g[bcur];
+        if (g >= (int)G) break;
+        // the next group, claimed now (its set-up is loaded around this group's flush)
+        const int gn = tid < 32 ? claim() : (int)G;
+        const uint32_t start = s_se[bcur][0], end = s_se[bcur][1];
+        const bool bad = s_bad[bcur] != 0;
+        const SceneParams<T>& sp = a.scenes[s_scene[bcur]];
         const int nf = sp.damage ? NACC : 4;
         // The state of the group one round of claims ahead (whichever CTA takes it) is prefetched into L2 while this
         // group runs, so that its phase 1 reads L2: the lanes of warp 1 take one array each (state fields P_X .. P_D
@@ -1525,7 +1547,7 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
                 if (q >= cnt) break;
                 int b[3];
                 particle_payload<T, MODELS>(a.pin, js[k], sp, pay + (q + (q >> 3)), CPAD, b, fallbacks);
-                const int l0 = b[0] - s_org[0], l1 = b[1] - s_org[1], l2 = b[2] - s_org[2];
+                const int l0 = b[0] - s_org[bcur][0], l1 = b[1] - s_org[bcur][1], l2 = b[2] - s_org[bcur][2];
                 const bool inside = l0 >= 0 && l0 < L::sx && l1 >= 0 && l1 < L::sy && l2 >= 0 && l2 < L::sz;
                 if (!inside) raise_flag(a.st, FLAG_CAPACITY); // keys and positions disagree: abort the substep
                 cellof[q] = inside ? (uint8_t)L::element(l0, l1, l2) : (uint8_t)0xff;
@@ -1553,11 +1575,18 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
             add_to_offset_tile<T, L>(acc, tile, cx, cy, cz, ii, nf); // all lanes (an empty cell adds zeros)
             __syncthreads();
         }
+        uint32_t n_st = 0, n_en = 0;
+        int32_t n_slot = -1;
+        if (tid < 8 && gn < (int)G) {
+            n_st = a.g_start[gn];
+            n_en = gn + 1 < (int)G ? a.g_start[gn + 1] : a.n_total;
+            n_slot = a.g_nbr[gn * 8 + tid];
+        }
         if (pf && pf_b > pf_a && pf_b <= a.n_total) {
             pf_j0 = a.vals_sorted[pf_a];
             pf_j1 = a.vals_sorted[pf_b - 1];
         }
-        if (!bad) flush_offset_tiles<T, L>(a, tile, s_nbr, nf, tid, NT);
+        if (!bad) flush_offset_tiles<T, L>(a, tile, s_nbr[bcur], nf, tid, NT);
         if (pf && pf_j1 >= pf_j0 && pf_j1 - pf_j0 < 2 * (pf_b - pf_a) + 64) {
             const Pool<T>& P = a.pin;
             if (pfl < NPF - 1)
@@ -1565,7 +1594,15 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
             else
                 prefetch_l2_range(P.pid, pf_j0, pf_j1, P.pid, P.pid + P.stride);
         }
+        // the next group's set-up into the other buffer (the flush above read this one)
+        if (tid < 8) {
+            if (gn < (int)G)
+                setup_store(bcur ^ 1, gn, n_st, n_en, n_slot, tid == 0 ? a.kl.at(a.keys_sorted, n_st) : 0ull);
+            else if (tid == 0)
+                s_g[bcur ^ 1] = gn;
+        }
         __syncthreads();
+        bcur ^= 1;
     }
     if (fallbacks) atomicAdd(&a.st->fallback, fallbacks);
 }
