@@ -1729,7 +1729,10 @@ private:
                 best = sc;
             }
         }
-        for (int gc = 0; gc < 12; gc++) {
+        // G2P: 3 thread counts x 2 register budgets. The variants with the halo staged by bulk copies (g2p_tight + 2)
+        // stay selectable by set_schedule but are not tried: as fast as the others in the first substeps of a pull,
+        // where the trials run, and 4% slower late in it (0.290 against 0.279 ms per substep on the 3.4 M slab)
+        for (int gc = 0; gc < 6; gc++) {
             const int gi = gc % 3;
             Schedule sc = best;
             sc.g2p_threads = G2P_NT[gi];
