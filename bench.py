@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="with --profile-only: launch kernels one at a time, not as graphs")
     ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
+    ap.add_argument("--state-out", default=None, help="with --profile-only: write the scene's state to this file at the end")
+    ap.add_argument("--state-in", default=None,
+                    help="with --profile-only: start from a state file written by --state-out (a late state to profile after "
+                         "few launches)")
     ap.add_argument("--schedule", default="auto",
                     help="auto (the autotuner), or fused:CTAS:G2P[:TIGHT], fused2:CTAS:G2P[:TIGHT], ws:CTAS:G2P[:TIGHT] or "
                          "split:CHUNK:BUFFERS:CTAS:G2P[:TIGHT] "
@@ -494,10 +498,14 @@ def run_ours(args, world, rank):
     s.from_recipe(r)
     apply_schedule(s, args.schedule)
     if args.profile_only:
+        if args.state_in:
+            s.read_state(args.state_in)
         if args.eager:  # substeps launched one kernel at a time (ncu lists no kernel of a graph holding a conditional loop)
             s.set_timing(True)
         s.step(args.warmup)
         s.step(args.steps)
+        if args.state_out:
+            s.write_state(args.state_out)
         g, b = s.last_grid()
         print(json.dumps({"profile_only": True, "particles": n, "groups": g, "blocks": b, "ms_per_step": s.last_step_ms / max(1, args.steps)}))
         return None
