@@ -91,3 +91,49 @@ def test_batch_with_a_one_particle_scene(prec):
         for f in ("x", "v", "F"):
             a, c = b.get(k, f), sc.get(f)
             assert np.abs(a - c).max() <= tol * max(1.0, np.abs(c).max()), (k, f, np.abs(a - c).max())
+
+
+@pytest.mark.parametrize("prec", [zr.F64, zr.F32])
+def test_two_materials_collide(prec):
+    """Two cubes of different models in one scene (a fixed-corotated one, and a Neo-Hookean (Borden) one with
+    anisotropic damage and a low critical stress) driven into each other: the kernels for mixed models (material
+    per particle) against the oracle with the same per-particle materials; damage grows where they meet."""
+    dx, dt = 1 / 64, 1e-4
+    rng = np.random.default_rng(9)
+
+    def cube(c0, n=4):
+        cells = [(c0[0] + i, c0[1] + j, c0[2] + k) for i in range(n) for j in range(n) for k in range(n)]
+        x = [[(c[a] + (((s >> (2 - a)) & 1) + 0.5) * 0.5) * dx for a in range(3)] for c in cells for s in range(8)]
+        return np.asarray(x) + rng.uniform(-0.1, 0.1, (len(x), 3)) * dx
+
+    xa, xb = cube((26, 30, 30)), cube((32, 31, 30))
+    na, nb = len(xa), len(xb)
+    vol = dx ** 3 / 8
+    va, vb = np.tile([[4.0, 0.0, 0.3]], (na, 1)), np.tile([[-4.0, 0.2, 0.0]], (nb, 1))
+    eye = np.tile(np.eye(3).reshape(1, 9), (na + nb, 1))
+    m = np.full(na + nb, 1000.0 * vol)
+    sc_b = rng.normal(30.0, 3.0, nb)
+    dmg = dict(alpha=-1.0, l0=0.5 * dx, eta=0.1, zeta=1.0, residual=0.01)
+
+    s = zr.Scene(prec)
+    s.set_params(dx, dt, (0.0, 0.0, 0.0), 1.0, 0.6, int(round(1 / dx)) + 4)
+    fa = s.add_particles(xa, m[:na], np.full(na, vol), v=va, F=eye[:na])
+    s.add_corotated(fa, na, 1e4, 0.3)
+    fb = s.add_particles(xb, m[na:], np.full(nb, vol), v=vb, F=eye[na:])
+    s.add_neohookean_borden(fb, nb, 3e4, 0.25)
+    s.add_aniso_damage(fb, nb, dmg["alpha"], dmg["l0"], dmg["eta"], dmg["zeta"], dmg["residual"], sc_b)
+
+    import pyoracle as po
+
+    o = po.OracleScene(8, dx, dt, (0.0, 0.0, 0.0), 1.0, 0.6)
+    o.add_material(zr.COROTATED, 1e4, 0.3)
+    o.add_material(zr.NEOHOOKEAN_BORDEN, 3e4, 0.25, True, dmg["alpha"], dmg["l0"], dmg["eta"], dmg["zeta"], dmg["residual"])
+    o.set_particles(np.vstack([xa, xb]), np.vstack([va, vb]), m, np.full(na + nb, vol), F=eye,
+                    sigma_c=np.concatenate([np.full(na, 1e30), sc_b]), material=np.r_[np.zeros(na, np.int32), np.ones(nb, np.int32)])
+    s.step(60)
+    o.step(60)
+    e = scenes.errors(scenes.gpu_state(s), o.state())
+    assert e["x"][0] < (1e-12 if prec == zr.F64 else 1e-5), e
+    assert e["v"][0] < (1e-9 if prec == zr.F64 else 1e-3), e
+    assert e["d"][0] < (1e-9 if prec == zr.F64 else 1e-3), e
+    assert o.state()["d"][na:].max() > 0.01  # the cubes met and the damageable one took damage
