@@ -64,6 +64,19 @@ def cases(rng):
     dxw = 1.0 / 2048
     w = rng.random((3000, 3)) * np.array([1.9, 1.2, 1.95]) + 0.01
     out["wide"] = (dxw, w)
+    # a cell size whose reciprocal is not exact in binary (1/100, 1/75): x * (1/dx) rounds in T, so positions on
+    # and next to cell faces and centres land on either side of the floor depending on the T-precision product
+    for name, dxo in (("odd100", 1.0 / 100), ("odd75", 1.0 / 75)):
+        o = []
+        for i in range(30, 42):
+            for j in range(33, 36):
+                for f in (0.0, 0.5):
+                    for eps in (-2e-9, 0.0, 2e-9):
+                        o.append([(i + f) * dxo + eps, (j + f) * dxo - eps, (i + j + f) * dxo * 0.5 + eps])
+        o += list(rng.random((400, 3)) * 0.2 + 0.3)
+        o = np.array(o)
+        rng.shuffle(o)
+        out[name] = (dxo, o)
     return out
 
 

@@ -12,7 +12,7 @@ GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "bin
 
 
 def test_golden_fixtures_present():
-    assert len(GOLDEN) == 6
+    assert len(GOLDEN) == 10
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[8:-4] for p in GOLDEN])

@@ -8,6 +8,8 @@ other test has run. Its output must equal, bit for bit, the binning of the alloc
 so stale scratch from the first call would show up); a call after the warm-up calls must leave the device's
 free memory unchanged; a particle outside the stated domain is reported."""
 import ctypes as C
+import glob
+import os
 
 import numpy as np
 import pytest
@@ -64,6 +66,20 @@ def test_noalloc_binning_equals_scene_binning_on_two_calls(prec):
         assert np.array_equal(got["sorted"], want["sorted"])
         assert np.array_equal(got["order"], want["order"])
         assert np.array_equal(got["group_first"], want["group_first"])
+
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "binning_*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[8:-4] for p in GOLDEN])
+def test_noalloc_binning_matches_reference_spgrid(path):
+    """The golden vectors made by the reference's own SPGrid code (cell-face positions, duplicates, coordinates up
+    to ~4000 cells, cell sizes whose reciprocal is inexact): sorted keys, order and group starts bit for bit."""
+    g = np.load(path)
+    got = noalloc_binning(int(g["precision"]), g["x"], float(g["dx"]))
+    assert np.array_equal(got["sorted"], g["sorted"])
+    assert np.array_equal(got["order"], g["order"])
+    assert np.array_equal(got["group_first"], g["group_first"])
 
 
 def test_noalloc_rejects_sizes_beyond_its_static_scratch():
