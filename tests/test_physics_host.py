@@ -265,6 +265,43 @@ def test_qrnh_damage_update_matches_reference_formula(shim):
         assert abs(got - want) < 1e-10, t
 
 
+@pytest.mark.parametrize("alpha", [-1.0, -0.5, 0.5, 2.0])
+def test_borden_drive_in_the_material_frame_equals_the_rotated_director_form(shim, alpha):
+    """The Borden drive is evaluated on F^T F with A = diag(1 + alpha, 1, 1), without the polar rotation; the
+    reference rotates the director, a = R e1 with F = R S (AnisoFractureSimulation.h:224-270, :365-391), and builds
+    sigma+ from F F^T. Large rotations and stretches up to 1.6, critical stresses that put phi between 0.5 and 20:
+    the two forms agree to rounding (FP64) and to FP32 rounding of the stress (FP32)."""
+    shim.shim_drive.restype = C.c_double
+    shim.shim_drive.argtypes = [C.c_int, C.c_int] + [C.c_double] * 6 + [C.POINTER(C.c_double)]
+    rng = np.random.default_rng(33)
+    E, nu, zeta = 5e4, 0.25, 1.0
+    nonzero = 0
+    for t in range(200):
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        if np.linalg.det(q) < 0:
+            q[:, 0] = -q[:, 0]
+        w, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        S = w @ np.diag(rng.uniform(0.7, 1.6, 3)) @ w.T
+        F = np.ascontiguousarray(q @ S)
+        J = np.linalg.det(F)
+        sig = tau_reference(1, E, nu, F, 1.0) / J
+        ev, Q = np.linalg.eigh((sig + sig.T) / 2)
+        sp = Q @ np.diag(np.maximum(ev, 0)) @ Q.T
+        a = oracle_R(8, F)[:, 0]
+        A = np.eye(3) + alpha * np.outer(a, a)
+        c = np.sum((A @ sp) * (sp @ A))
+        if c <= 0:
+            continue
+        sc = np.sqrt(c / rng.uniform(0.5, 20.0))
+        want = zeta * max(c / sc ** 2 - 1, 0)
+        nonzero += want > 0
+        got = shim.shim_drive(8, 1, E, nu, 0.0, alpha, zeta, sc, p(F))
+        assert abs(got - want) <= 1e-11 * max(1.0, want), (t, got, want)
+        got32 = shim.shim_drive(4, 1, E, nu, 0.0, alpha, zeta, sc, p(F))
+        assert abs(got32 - want) <= 2e-4 * max(1.0, c / sc ** 2), (t, got32, want)
+    assert nonzero > 100
+
+
 @pytest.mark.parametrize("alpha", [-1.0, 0.5, 2.0])
 def test_damage_drive_zero_bound_changes_nothing(shim, alpha):
     """The drive skips the tensile split and the polar decomposition when max(1, (1+alpha)^2) |sigma|_F^2 is at

@@ -576,46 +576,64 @@ ZR_HD T degradation(T d, T k)
 }
 
 // The damage drive D~ = zeta <phi - 1> of one particle, phi = (A sigma+) : (sigma+ A) / sigma_c^2 with the
-// undegraded Cauchy stress's tensile part sigma+ and the structural tensor A = I + alpha (R e1)(R e1)^T
-// (AnisoFractureSimulation.h:224-270; updateDTildeHelper :292-333 for the implicit solve).
+// undegraded Cauchy stress's tensile part sigma+ and the structural tensor A = I + alpha (R e1)(R e1)^T, R the
+// rotation of F = R S (AnisoFractureSimulation.h:224-270, :365-391; updateDTildeHelper :292-333 for the implicit
+// solve).
+//
+// For the Borden model the polar decomposition is not needed. Its stress is an isotropic function of B = F F^T, and
+// B = R C R^T with C = F^T F = S^2, so sigma(F) = R sigma~ R^T where sigma~ is the same formula evaluated on C
+// (tau_nhb of F^T), and sigma+ = R sigma~+ R^T. The contraction is invariant under that rotation, and
+// R^T A R = I + alpha e1 e1^T = diag(w) with w = (1 + alpha, 1, 1). So phi sigma_c^2 = sum_ij w_i w_j (sigma~+_ij)^2.
+// This is the same quantity with different rounding. The QR-stable model's fibre term makes its stress
+// anisotropic, so it keeps the polar rotation.
 template <class T>
 ZR_HD T damage_drive(const Material<T>& mt, const T* F, T sigma_c, bool& fallback)
 {
     T tau[9], invJ;
-    if (mt.model == MODEL_QR_STABLE_NEOHOOKEAN) {
+    const bool qr = mt.model == MODEL_QR_STABLE_NEOHOOKEAN;
+    if (qr) {
         invJ = (T)1 / tau_qrnh(mt, F, (T)1, tau, true); // cauchy = P F^T / J with J from the QR (QRStableNeoHookean.h:86-96)
     }
     else {
-        tau_nhb(mt, F, (T)1, tau);
+        const T Ft[9] = { F[0], F[3], F[6], F[1], F[4], F[7], F[2], F[5], F[8] };
+        tau_nhb(mt, Ft, (T)1, tau); // tau~ = R^T tau R: the formula on F^T F
         invJ = (T)1 / det3(F);
     }
     T S[9], sp[9], s2 = 0;
     for (int i = 0; i < 9; i++) {
-        S[i] = tau[i] * invJ; // undegraded Cauchy stress
+        S[i] = tau[i] * invJ; // undegraded Cauchy stress (in the material frame for the Borden model)
         s2 += S[i] * S[i];
     }
     // phi sigma_c^2 = tr((A sigma+)^2) <= |A|_2^2 |sigma+|_F^2 <= max(1, (1 + alpha)^2) |sigma|_F^2 (A = I + alpha a a^T
     // with |a| = 1; sigma+ keeps a subset of sigma's eigenvalues). Below that bound, with a margin far above
-    // rounding, the drive is exactly zero: skip the eigen split and the polar decomposition.
+    // rounding, the drive is exactly zero: skip the eigen split (and the polar decomposition).
     const T ap1 = (T)1 + mt.alpha, anorm2 = ap1 * ap1 > (T)1 ? ap1 * ap1 : (T)1;
     if (s2 * anorm2 <= (T)0.999 * sigma_c * sigma_c) {
         fallback = false;
         return (T)0;
     }
     tension_part(S, sp); // sum of Macaulay-bracketed principal stresses times their projectors
-    T R[9];
-    fallback = polar_rotation(F, R);
-    T a[3] = { R[0], R[3], R[6] }; // R e1
-    T M[9]; // A sigma+ with A = I + alpha a a^T
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) {
-            T as = a[0] * sp[c] + a[1] * sp[3 + c] + a[2] * sp[6 + c];
-            M[3 * r + c] = sp[3 * r + c] + mt.alpha * a[r] * as;
-        }
-    // (A sigma+) : (sigma+ A) = sum_ij M_ij M_ji since sigma+ A = (A sigma+)^T
     T contraction = 0;
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) contraction += M[3 * r + c] * M[3 * c + r];
+    if (qr) {
+        T R[9];
+        fallback = polar_rotation(F, R);
+        T a[3] = { R[0], R[3], R[6] }; // R e1
+        T M[9]; // A sigma+ with A = I + alpha a a^T
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                T as = a[0] * sp[c] + a[1] * sp[3 + c] + a[2] * sp[6 + c];
+                M[3 * r + c] = sp[3 * r + c] + mt.alpha * a[r] * as;
+            }
+        // (A sigma+) : (sigma+ A) = sum_ij M_ij M_ji since sigma+ A = (A sigma+)^T
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) contraction += M[3 * r + c] * M[3 * c + r];
+    }
+    else {
+        fallback = false;
+        // sum_ij w_i w_j sp_ij^2, w = (1 + alpha, 1, 1): the first row and column carry 1 + alpha once each
+        const T s00 = sp[0], s01 = sp[1], s02 = sp[2], s11 = sp[4], s12 = sp[5], s22 = sp[8];
+        contraction = ap1 * ap1 * (s00 * s00) + (T)2 * ap1 * (s01 * s01 + s02 * s02) + (s11 * s11 + s22 * s22) + (T)2 * (s12 * s12);
+    }
     T phi = contraction / (sigma_c * sigma_c);
     return mt.zeta * (phi > (T)1 ? phi - (T)1 : (T)0);
 }
