@@ -1294,7 +1294,8 @@ private:
         }
         else // its last kernel places the group heads and activates their blocks (after ev[1]: the activate phase)
             ZR_CUDA(sort_and_activate_incremental(n, a, ev ? ev[1] : nullptr));
-        k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a); // also zeroes the per-scene grid mass
+        if (sched_.fused == 0 || sched_.fused == 3) // these P2G forms read grid slots; the fused one translates its groups' entries
+            k_nbr<T><<<nsm_ * 4, 256, 0, stream_>>>(a);
         if (ev) ZR_CUDA(cudaEventRecord(ev[2], stream_));
         if (sched_.fused == 3)
             launch_ws(a, nsm_ * std::min(sched_.scatter_ctas_per_sm, occ_ws_[models_slot()]));

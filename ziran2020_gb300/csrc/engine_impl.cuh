@@ -154,18 +154,6 @@ __device__ inline bool aborted_cta(const DevStatus* st)
     return r;
 }
 
-__device__ inline int hash_find(const uint64_t* hk, const int32_t* hv, uint32_t mask, uint64_t key)
-{
-    uint32_t h = (uint32_t)hash64(key) & mask;
-    for (int p = 0; p < HASH_PROBES; p++) {
-        uint64_t k = hk[h];
-        if (k == key) return hv[h];
-        if (k == HASH_EMPTY) return -1;
-        h = (h + 1) & mask;
-    }
-    return -1;
-}
-
 // ---------------------------------------------------------------------------------------------------
 // keys of the current particle positions (used after a load or a host upload; afterwards G2P writes
 // the keys of the next substep). Also checks that every base node lies in its scene's domain.
@@ -642,7 +630,7 @@ static __global__ void __launch_bounds__(SORT_NT) k_group_heads(const uint64_t* 
 // Block dl (x*4 + y*2 + z, at +1 block) of the group whose first sorted key is key0, into the block hash; a block
 // seen for the first time takes the next grid slot (one slot counter atomic per group of converged lanes).
 template <class T>
-__device__ __forceinline__ void activate_block(const StepArgs<T>& a, uint64_t key0, uint32_t dl)
+__device__ __forceinline__ void activate_block(const StepArgs<T>& a, uint64_t key0, uint32_t dl, int32_t* hpos)
 {
     using L = typename LayoutOf<T>::type;
     const uint64_t scene = a.kl.scene(key0);
@@ -661,7 +649,9 @@ __device__ __forceinline__ void activate_block(const StepArgs<T>& a, uint64_t ke
             h = (h + 1) & a.h_mask;
     }
     if (!done) raise_flag(a.st, FLAG_CAPACITY);
-    // the entry's slot is written after the probe: nothing reads h_vals before the next kernel (k_nbr)
+    // The group's neighbour entry gets the block's hash position, whether this thread inserted the block or found
+    // it: the slot is written by the inserting thread below, so it is read (nbr_slot) only by a later kernel.
+    *hpos = done ? (int32_t)h : -1;
     const unsigned am = __activemask();
     const unsigned nw = __ballot_sync(am, fresh);
     if (nw) {
@@ -687,6 +677,8 @@ __device__ __forceinline__ void activate_block(const StepArgs<T>& a, uint64_t ke
 template <class T>
 __global__ void k_activate(StepArgs<T> a)
 {
+    if (blockIdx.x == 0) // the per-scene grid mass k_grid accumulates
+        for (int s = threadIdx.x; s < a.n_scenes; s += blockDim.x) a.grid_mass[s] = 0;
     if (aborted(a.st)) return;
     const uint32_t G = a.st->n_groups;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->max_groups_seen = max(a.st->max_groups_seen, G);
@@ -695,7 +687,7 @@ __global__ void k_activate(StepArgs<T> a)
         return;
     }
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x)
-        activate_block(a, a.kl.at(a.keys_sorted, a.g_start[t >> 3]), t & 7);
+        activate_block(a, a.kl.at(a.keys_sorted, a.g_start[t >> 3]), t & 7, a.g_nbr + t);
 }
 
 // After the incremental sort's merge, per tile: the group heads of the tile's output (sorted positions
@@ -709,6 +701,8 @@ __global__ void __launch_bounds__(SORT_NT) k_heads_activate(StepArgs<T> a, SortB
     __shared__ uint32_t s_c[RMAX][SORT_NT / 32], s_part[SORT_NT / 32];
     __shared__ uint32_t s_pos[RMAX * SORT_NT]; // sorted positions of the tile's heads, in order
     __shared__ uint32_t s_g0, s_nh;
+    if (blockIdx.x == 0) // the per-scene grid mass k_grid accumulates
+        for (int s = threadIdx.x; s < a.n_scenes; s += blockDim.x) a.grid_mass[s] = 0;
     if (aborted_cta(a.st)) return; // FLAG_SORT from the merge, or an earlier failure: the substep is repeated
     const int j = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t* keys = reinterpret_cast<const uint32_t*>(a.keys_sorted); // the incremental sort's keys are 32-bit
@@ -788,31 +782,30 @@ __global__ void __launch_bounds__(SORT_NT) k_heads_activate(StepArgs<T> a, SortB
             raise_flag(a.st, FLAG_CAPACITY);
             continue;
         }
-        activate_block(a, (uint64_t)keys[s_pos[t >> 3]], t & 7);
+        activate_block(a, (uint64_t)keys[s_pos[t >> 3]], t & 7, a.g_nbr + (size_t)g0 * 8 + t);
     }
 }
 
 // ---------------------------------------------------------------------------------------------------
-// neighbour slots: the grid slots of every group's block and its 7 neighbours at +1 block (read by the
-// P2G scatter and by G2P). A separate pass after activation, so that every slot is final when read.
+// neighbour slots: the grid slots of every group's block and its 7 neighbours at +1 block (read by P2G and
+// G2P). Activation leaves the hash position of each of these blocks in g_nbr; the slot behind it is final once
+// activation has ended. The fused P2G translates its groups' entries itself while it sets them up (and writes
+// the slots back for G2P); the other P2G forms read slots, so k_nbr translates every entry before them.
 // ---------------------------------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ int32_t nbr_slot(const StepArgs<T>& a, int32_t hpos)
+{
+    return (uint32_t)hpos <= a.h_mask ? a.h_vals[hpos] : -1; // -1: the probe failed and raised FLAG_CAPACITY
+}
+
 template <class T>
 __global__ void k_nbr(StepArgs<T> a)
 {
-    using L = typename LayoutOf<T>::type;
-    if (blockIdx.x == 0) // the per-scene grid mass k_grid accumulates
-        for (int s = threadIdx.x; s < a.n_scenes; s += blockDim.x) a.grid_mass[s] = 0;
     if (aborted(a.st)) return;
     const uint32_t G = a.st->n_groups;
     if (G > a.b_cap) return; // activation already raised FLAG_CAPACITY
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < G * 8; t += gridDim.x * blockDim.x) {
-        const uint32_t g = t >> 3, dl = t & 7;
-        const uint64_t key0 = a.kl.at(a.keys_sorted, a.g_start[g]);
-        uint32_t bi, bj, bk;
-        L::block_of_page(a.kl.page(key0), bi, bj, bk);
-        const uint64_t scene = a.kl.scene(key0);
-        const uint64_t hk = (scene << 40) | L::page_of_block(bi + (dl >> 2), bj + ((dl >> 1) & 1), bk + (dl & 1));
-        const int slot = hash_find(a.h_keys, a.h_vals, a.h_mask, hk);
+        const int32_t slot = nbr_slot(a, a.g_nbr[t]);
         if (slot < 0) raise_flag(a.st, FLAG_CAPACITY);
         a.g_nbr[t] = slot;
     }
@@ -1494,6 +1487,13 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
             s_se[bb][1] = en;
         }
     };
+    // A group's neighbour entries hold hash positions (activation); the set-up translates them into grid slots and
+    // writes the slots back for G2P.
+    auto take_slot = [&](int gg, int32_t hpos) { // lanes 0-7 of warp 0
+        const int32_t slot = nbr_slot(a, hpos);
+        a.g_nbr[gg * 8 + tid] = slot;
+        return slot;
+    };
     const int ii = tid / NC, c = tid % NC;
     const int cx = c >> (L::zbits + L::ybits), cy = (c >> L::zbits) & (L::sy - 1), cz = c & (L::sz - 1);
     for (int q = tid; q < OffsetTiles<L>::ELEMS; q += NT) tile[q] = (T)0;
@@ -1503,7 +1503,7 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
         if (g0 < (int)G) {
             if (tid < 8) {
                 const uint32_t st = a.g_start[g0], en = g0 + 1 < (int)G ? a.g_start[g0 + 1] : a.n_total;
-                setup_store(0, g0, st, en, a.g_nbr[g0 * 8 + tid], tid == 0 ? a.kl.at(a.keys_sorted, st) : 0ull);
+                setup_store(0, g0, st, en, take_slot(g0, a.g_nbr[g0 * 8 + tid]), tid == 0 ? a.kl.at(a.keys_sorted, st) : 0ull);
             }
         }
         else if (tid == 0)
@@ -1576,11 +1576,11 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
             __syncthreads();
         }
         uint32_t n_st = 0, n_en = 0;
-        int32_t n_slot = -1;
+        int32_t n_hpos = -1;
         if (tid < 8 && gn < (int)G) {
             n_st = a.g_start[gn];
             n_en = gn + 1 < (int)G ? a.g_start[gn + 1] : a.n_total;
-            n_slot = a.g_nbr[gn * 8 + tid];
+            n_hpos = a.g_nbr[gn * 8 + tid];
         }
         if (pf && pf_b > pf_a && pf_b <= a.n_total) {
             pf_j0 = a.vals_sorted[pf_a];
@@ -1597,7 +1597,7 @@ __global__ void __launch_bounds__(FusedShape<T, CH>::NT, MINB) k_p2g_fused(StepA
         // the next group's set-up into the other buffer (the flush above read this one)
         if (tid < 8) {
             if (gn < (int)G)
-                setup_store(bcur ^ 1, gn, n_st, n_en, n_slot, tid == 0 ? a.kl.at(a.keys_sorted, n_st) : 0ull);
+                setup_store(bcur ^ 1, gn, n_st, n_en, take_slot(gn, n_hpos), tid == 0 ? a.kl.at(a.keys_sorted, n_st) : 0ull);
             else if (tid == 0)
                 s_g[bcur ^ 1] = gn;
         }
