@@ -572,10 +572,14 @@ def run_ours(args, world, rank):
         s.exchange_state(host, res[0])
         s.step(1)
         s.get_state(res[0])
-        # jobs through zr_scene_step_stream: the copies of later inputs and earlier results overlap the substeps
-        t0 = time.perf_counter()
-        s.step_stream([host] * K, [res[k % 2] for k in range(K)])
-        el = time.perf_counter() - t0
+        # jobs through zr_scene_step_stream: the copies of later inputs and earlier results overlap the substeps. The
+        # host link is shared with the node's other work, so the K jobs run three times and the median is reported
+        # (all three beside it)
+        runs = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            s.step_stream([host] * K, [res[k % 2] for k in range(K)])
+            runs.append(allreduce_sum(world, n) * K / allreduce_max(world, time.perf_counter() - t0))
         # the same jobs with zr_scene_exchange_state: each step's download and the next upload in one kernel
         t0 = time.perf_counter()
         s.set_state(host)  # step 0's input
@@ -595,12 +599,12 @@ def run_ours(args, world, rank):
                 s.step(1)
                 s.get_state(res[0])
             e2e_seq = allreduce_sum(world, n) * K / allreduce_max(world, time.perf_counter() - t0)
-        e2e = {"value": allreduce_sum(world, n) * K / allreduce_max(world, el), "unit": "particle-substeps/s",
+        e2e = {"value": sorted(runs)[1], "unit": "particle-substeps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "what": f"{K} jobs, each the whole FP32 state (x,v,C,F,d) uploaded from pinned host memory, one substep, the "
                        "result downloaded to pinned host memory, through zr_scene_step_stream (the copies of the next inputs and "
-                       "the last results run on the copy engines during the substeps)",
-               "exchange_value": e2e_x, "sequential_value": e2e_seq}
+                       "the last results run on the copy engines during the substeps); the median of three runs of the jobs",
+               "runs": runs, "exchange_value": e2e_x, "sequential_value": e2e_seq}
     except Exception as ex:  # pinned memory needs torch; report instead of failing the line
         e2e = {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None, "error": str(ex)}
     cg_iterations = s.cg_iterations
