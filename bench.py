@@ -604,7 +604,7 @@ def run_ours(args, world, rank):
                "what": f"{K} jobs, each the whole FP32 state (x,v,C,F,d) uploaded from pinned host memory, one substep, the "
                        "result downloaded to pinned host memory, through zr_scene_step_stream (the copies of the next inputs and "
                        "the last results run on the copy engines during the substeps); the median of three runs of the jobs",
-               "runs": runs, "exchange_value": e2e_x, "sequential_value": e2e_seq}
+               "runs": runs, "reruns": s.stream_reruns, "exchange_value": e2e_x, "sequential_value": e2e_seq}
     except Exception as ex:  # pinned memory needs torch; report instead of failing the line
         e2e = {"value": None, "unit": "particle-substeps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None, "error": str(ex)}
     cg_iterations = s.cg_iterations

@@ -140,6 +140,9 @@ int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype);
  * and the later output buffers hold unspecified values. The reference has no counterpart (one scene per process, frames written to files); it serves a
  * pipeline that runs many independent states (ensembles, parameter sweeps, a host-side coupler) through one GPU. */
 int zr_scene_step_stream(zr_scene* s, int nsteps, const void* const* in, void* const* out, int dtype);
+/* Jobs of zr_scene_step_stream calls that ran again the safe way because a job aborted on the pipelined path
+ * (cumulative over the scene's life; 0 while every job ran pipelined). No reference counterpart. */
+int zr_scene_stream_reruns(zr_scene* s, int64_t* reruns);
 /* FP64-accumulated reductions (MpmSimulationDataAnalysis.h:67-151): total mass, momentum x/y/z, kinetic
  * energy, max particle speed, grid mass of the last substep. */
 int zr_scene_reductions(zr_scene* s, double out[7]);

@@ -203,6 +203,13 @@ public:
         check(zr_scene_step_stream(h_, (int)in.size(), reinterpret_cast<const void* const*>(in.data()), reinterpret_cast<void* const*>(out.data()),
             sizeof(T) == 4 ? ZR_F32 : ZR_F64));
     }
+    // jobs of stepJobs calls that ran again the safe way after an aborted job (cumulative)
+    long long stepJobsRerun() const
+    {
+        int64_t n = 0;
+        check(zr_scene_stream_reruns(h_, &n));
+        return (long long)n;
+    }
     // conjugate-gradient iterations of the last substep's implicit damage solve
     int cgIterations() const
     {

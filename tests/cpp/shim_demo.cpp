@@ -88,6 +88,6 @@ int main()
             jd = std::max(jd, std::abs((double)r0[q + a] - (double)r1[q + a]));
             moved = std::max(moved, std::abs((double)r0[q + a] - (double)st[q + a]));
         }
-    std::printf("jobs_diff %.3e moved %.3e\n", jd, moved);
+    std::printf("jobs_diff %.3e moved %.3e reruns %lld\n", jd, moved, sim.stepJobsRerun());
     return 0;
 }

@@ -42,5 +42,6 @@ def test_shim_demo_runs(tmp_path):
     n3, dmax3, cg3 = int(out[13]), float(out[15]), int(out[17])
     assert n3 == n2 and 0 < dmax3 <= 1 and cg3 > 0
     # two one-substep jobs of the same state through stepJobs (zr_scene_step_stream): the same result, and it moved
-    jobs_diff, moved = float(out[19]), float(out[21])
+    jobs_diff, moved, reruns = float(out[19]), float(out[21]), int(out[23])
     assert jobs_diff < 1e-6 and 1e-5 < moved < 1e-3
+    assert reruns == 0  # the second job ran on the pipelined path

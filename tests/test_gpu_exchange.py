@@ -77,6 +77,7 @@ def test_step_stream_equals_set_step_get(prec, pinned):
         a[:] = st
     s = scenes.gpu_scene(d, prec)
     s.step_stream(ins, outs)
+    assert s.stream_reruns == 0  # every job after the first ran on the pipelined path
     ref = scenes.gpu_scene(d, prec)
     tol = 1e-12 if prec == zr.F64 else 1e-5
     for a, o in zip(ins, outs):
@@ -133,6 +134,7 @@ def test_step_stream_recovers_the_jobs_after_a_failure_inside_the_pipeline(bad_j
         ins[k][:] = fast if k == bad_job else good
     with pytest.raises(Exception):
         s.step_stream(ins, outs)
+    assert s.stream_reruns == 6 - bad_job  # the failing job and the ones after it ran again the safe way
     for k in range(bad_job):
         assert np.abs(outs[k] - want[k]).max() < 1e-9, k
 

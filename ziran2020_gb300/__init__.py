@@ -82,6 +82,7 @@ def load_library(build_if_needed=True):
         "zr_scene_set_state": (i32, [vp, vp, i32]),
         "zr_scene_exchange_state": (i32, [vp, vp, vp, i32]),
         "zr_scene_step_stream": (i32, [vp, i32, vp, vp, i32]),
+        "zr_scene_stream_reruns": (i32, [vp, P(i64)]),
         "zr_scene_reductions": (i32, [vp, pd]),
         "zr_scene_set_dt": (i32, [vp, d]),
         "zr_scene_set_implicit_damage": (i32, [vp, i32]),
@@ -323,6 +324,13 @@ class Scene:
         pout = (C.c_void_p * n)(*[b.ctypes.data for b in outputs])
         self._check(self.L.zr_scene_step_stream(self.h, n, C.cast(pin, C.c_void_p), C.cast(pout, C.c_void_p), F32 if dtype == np.float32 else F64))
         return outputs
+
+    @property
+    def stream_reruns(self):
+        """Jobs of step_stream calls run again the safe way after an aborted job (cumulative)."""
+        v = C.c_int64()
+        self._check(self.L.zr_scene_stream_reruns(self.h, C.byref(v)))
+        return v.value
 
     def reductions(self):
         out = np.zeros(7)

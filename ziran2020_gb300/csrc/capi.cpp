@@ -492,6 +492,14 @@ int zr_scene_step_stream(zr_scene* s, int nsteps, const void* const* in, void* c
     return rc;
 }
 
+int zr_scene_stream_reruns(zr_scene* s, int64_t* reruns)
+{
+    NEED_ENGINE(s);
+    if (!reruns) return ZR_ERR_ARG;
+    *reruns = s->eng->stream_reruns();
+    return ZR_OK;
+}
+
 int zr_scene_exchange_state(zr_scene* s, const void* in, void* out, int dtype)
 {
     NEED_ENGINE(s);

@@ -107,6 +107,7 @@ public:
     // nsteps jobs, each: set_state(in25[i]), one substep, get_state(out25[i]); the host copies of the next inputs and
     // the last outputs run on copy engines while the GPU computes (the buffers stay in use until the call returns)
     virtual int stream_steps(int scene, int nsteps, const void* const* in25, void* const* out25, int is_f32) = 0;
+    virtual int64_t stream_reruns() const = 0; // jobs stream_steps ran again the safe way (cumulative)
     // FP64-accumulated reductions: mass, momentum(3), kinetic energy, max speed, grid mass
     virtual int reductions(int scene, double* out7) = 0;
     virtual int set_dt(int scene, double dt) = 0;

@@ -593,10 +593,12 @@ public:
         ZR_CUDA(cudaMemsetAsync(h_keys_, 0xff, 8 * (size_t)(h_mask_ + 1), stream_));
         if (cg_) ZR_CUDA(cudaMemsetAsync(cg_, 0, sizeof(T) * CG_NF * (size_t)b_cap_ * L::nodes, stream_));
         ZR_CUDA(cudaStreamSynchronize(stream_));
+        stream_reruns_ += nsteps - k;
         for (int i = k; i < nsteps; i++)
             if ((rc = safe_job(i))) return rc;
         return 0;
     }
+    int64_t stream_reruns() const override { return stream_reruns_; }
     int ensure_io(size_t bytes)
     {
         if (!h2d_) {
@@ -861,6 +863,7 @@ private:
     int occ_fused_[2][4] = { { 1, 1, 1, 1 }, { 1, 1, 1, 1 } }; // [fused variant][model set]
     int occ_ws_[4] = { 1, 1, 1, 1 }; // warp-specialised P2G, per model set
     int occ_grid_ = 1; // grid update CTAs per SM
+    int64_t stream_reruns_ = 0; // stream_steps jobs run again the safe way after an abort
     int models_ = 7; // bit m set: a material of model m (corotated, Neo-Hookean Borden, QR-stable Neo-Hookean) is present
     bool any_damage_ = false;
     bool implicit_ = false; // some scene solves its damage implicitly
