@@ -17,9 +17,10 @@ def elastic_box(size=0.125, dx=1 / 64, seed=7, E=1e4, nu=0.3, rho=1000.0, v0=(0.
 
 
 def aniso_slab(size=(0.1, 0.05, 0.1), dx=1 / 128, seed=11, sigma_c=(400.0, 40.0), pull=0.5, dt=5e-5, E=5e4, nu=0.25, rho=800.0, apic=0.0,
-               grip=2, model=None, fiber=0.0, implicit=False):
+               grip=2, model=None, fiber=0.0, implicit=False, alpha=-1.0):
     """model: zr.NEOHOOKEAN_BORDEN (default) or zr.QR_STABLE_NEOHOOKEAN with fibre stiffness kx = fiber mu;
-    implicit: the implicit damage solve instead of the explicit update."""
+    implicit: the implicit damage solve instead of the explicit update; alpha: the structural tensor's weight
+    (A = I + alpha a a^T; -1, the demos' value, removes the stress along the fibre)."""
     model = zr.NEOHOOKEAN_BORDEN if model is None else model
     r = zr.recipe(zr.RECIPE_ANISO_SLAB, dx=dx, seed=seed, size=size, l0=0.5 * dx, sigma_c_mean=sigma_c[0], sigma_c_std=sigma_c[1],
                   pull_speed=pull, dt=dt, E=E, nu=nu, rho=rho, apic_rpic_ratio=apic, grip_cells=grip)
@@ -29,7 +30,7 @@ def aniso_slab(size=(0.1, 0.05, 0.1), dx=1 / 128, seed=11, sigma_c=(400.0, 40.0)
     x_lo, x_hi = lo[0] * dx, (lo[0] + nc[0]) * dx
     return {"dx": dx, "dt": dt, "gravity": (0.0, 0.0, 0.0), "apic": apic, "cfl": 0.6, "domain": int(round(1 / dx)) + 4, **g,
             "materials": [dict(model=model, E=E, nu=nu, kx=fiber)],
-            "damage": dict(alpha=-1.0, l0=0.5 * dx, eta=0.1, zeta=1.0, residual=0.01), "implicit": implicit,
+            "damage": dict(alpha=alpha, l0=0.5 * dx, eta=0.1, zeta=1.0, residual=0.01), "implicit": implicit,
             "objects": [dict(origin=(x_lo + grip * dx, 0, 0), normal=(1, 0, 0), type=zr.STICKY, friction=0.0, velocity=(-pull, 0, 0)),
                         dict(origin=(x_hi - grip * dx, 0, 0), normal=(-1, 0, 0), type=zr.STICKY, friction=0.0, velocity=(pull, 0, 0))]}
 

@@ -71,6 +71,28 @@ def test_aniso_slab_fp64_matches_oracle(steps):
         assert r["d"].max() > 0  # damage actually grew, so the comparison covers the damage path
 
 
+@pytest.mark.parametrize("alpha,sigma_c", [(-0.5, 400.0), (0.5, 800.0), (2.0, 800.0)])
+def test_aniso_slab_structural_weights_match_oracle(alpha, sigma_c):
+    """The damage drive for structural-tensor weights other than the demos' -1 (which removes the stress along the
+    fibre): the GPU evaluates the Borden drive in the material frame with A = diag(1 + alpha, 1, 1), the oracle as
+    the reference does, with the director rotated by the polar rotation of F (AnisoFractureSimulation.h:224-270,
+    :365-391). 30 substeps of a damaging slab, the critical stress set so that damage grows without saturating
+    (the oracle's largest damage 0.33 to 0.86): FP64 within 1e-12 (positions) and 1e-9 (damage; measured 3e-14),
+    FP32 within 1e-5 and 2e-4 (measured 7.5e-7 and 5.4e-5)."""
+    d = scenes.aniso_slab(size=(0.1, 0.05, 0.1), sigma_c=(sigma_c, 0.1 * sigma_c), pull=1.0, alpha=alpha)
+    o = scenes.oracle_scene(d, 8)
+    o.step(30)
+    r = o.state()
+    assert 0.1 < r["d"].max() < 1  # damage grew and did not saturate
+    for prec, xtol, dtol in ((zr.F64, 1e-12, 1e-9), (zr.F32, 1e-5, 2e-4)):
+        s = scenes.gpu_scene(d, prec)
+        s.step(30)
+        e = scenes.errors(scenes.gpu_state(s), r)
+        print(f"slab, alpha {alpha}, precision {prec}: {e}")
+        assert e["x"][0] < xtol, (prec, e)
+        assert e["d"][0] < dtol, (prec, e)
+
+
 @pytest.mark.parametrize("fiber", [0.0, 10.0])
 def test_qr_stable_slab_matches_oracle(fiber):
     """QR-stable Neo-Hookean (the AnisoMPM demos' model, fibre stiffness kx = fiber mu as in
