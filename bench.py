@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=24, help="default workload: requests per rate in the serving summary")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="with --profile-only: launch kernels one at a time, not as graphs")
-    ap.add_argument("--profile-only", action="store_true", help="FP32 scene only: warmup + timed substeps (for ncu captures)")
+    ap.add_argument("--profile-only", action="store_true", help="one scene only: warmup + timed substeps (for ncu captures)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="with --profile-only: the scene's precision")
     ap.add_argument("--state-out", default=None, help="with --profile-only: write the scene's state to this file at the end")
     ap.add_argument("--state-in", default=None,
                     help="with --profile-only: start from a state file written by --state-out (a late state to profile after "
@@ -494,7 +495,7 @@ def run_ours(args, world, rank):
     n = zr.recipe_count(r)
     damage = kind == 1
 
-    s = zr.Scene(zr.F32)
+    s = zr.Scene(zr.F64 if args.profile_only and args.precision == "fp64" else zr.F32)
     s.from_recipe(r)
     apply_schedule(s, args.schedule)
     if args.profile_only:
